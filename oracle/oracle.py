@@ -1,0 +1,331 @@
+"""CPU oracle for the minkasi mapmaking hot path.
+
+TEST INFRASTRUCTURE ONLY.  Only tests/, ``__graft_entry__.smoke()`` and the
+``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may import this
+module, and only as the checker or as the timed CPU baseline.  The product
+package (``minkasi_gb300``) never imports it.
+
+Each function restates one piece of the reference's FP64 arithmetic, with the
+reference file:line it follows (paths relative to the minkasi project root):
+
+* ``map2tod`` / ``tod2map``  -> minkasi/lib/minkasi.c:131-144 / :97-112
+  (through the C restatement in ``oracle/mk_oracle.c``)
+* ``dct1``                   -> FFTW REDFT00 as called by
+  minkasi/tools/fft.py:290-344 -> minkasi/lib/mkfftw.c:174-212, and its
+  scipy fallback minkasi/tools/py_fft.py:254-285 (``scipy.fft.dct(type=1)``)
+* ``apply_noise``            -> NoiseSmoothedSVD.apply_noise,
+  minkasi/mapmaking/noise.py:680-714
+* ``smooth_many_vecs``       -> minkasi/tools/smooth.py:49-78
+* ``noise_model``            -> NoiseSmoothedSVD.__init__,
+  minkasi/mapmaking/noise.py:604-678
+* ``det_weights``            -> NoiseSmoothedSVD.get_det_weights, noise.py:761-772
+* ``todvec_dot``             -> Tod.dot / TodVec.dot, minkasi/tods/core.py:649-691,967-1026
+* ``make_rhs``               -> TodVec.make_rhs, minkasi/tods/core.py:1028-1047
+* ``make_hits``              -> minkasi/mapmaking/tod2map.py:343-400
+* ``run_pcg``                -> minkasi/mapmaking/pcg.py:22-238
+* ``find_good_fft_lens`` / ``truncate_len`` -> minkasi/tools/py_fft.py:300-395,
+  minkasi/tods/processing.py:648-682
+
+Parity of this oracle with the reference itself is pinned by
+``tests/test_oracle_golden.py`` against fixtures that
+``tests/golden/make_golden.py`` produced by running the reference code.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+from typing import List, Optional, Sequence
+
+import numpy as np
+import scipy.fft
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+
+def build() -> str:
+    """Compile oracle/mk_oracle.so (gcc + OpenMP) if it is missing or stale."""
+    so = os.path.join(_HERE, "mk_oracle.so")
+    src = os.path.join(_HERE, "mk_oracle.c")
+    if not os.path.exists(so) or os.path.getmtime(so) < os.path.getmtime(src):
+        subprocess.run(["make", "-s", "-C", _HERE, "mk_oracle.so"], check=True)
+    return so
+
+
+def lib():
+    """ctypes handle on the C restatement (built on first use)."""
+    global _LIB
+    if _LIB is None:
+        h = ctypes.CDLL(build())
+        vp, i64, i32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+        for name in ("orc_map2tod", "orc_map2tod_f32"):
+            getattr(h, name).argtypes = [vp, vp, i64, i64, vp, i32, i32]
+            getattr(h, name).restype = None
+        h.orc_map2tod_serial.argtypes = [vp, vp, i64, i64, vp, i32]
+        for name in ("orc_tod2map", "orc_tod2map_f32"):
+            getattr(h, name).argtypes = [vp, vp, i64, i64, vp, i64, i32]
+            getattr(h, name).restype = ctypes.c_int
+        h.orc_tod2map_serial.argtypes = [vp, vp, i64, i64, vp]
+        h.orc_tod2map_atomic.argtypes = [vp, vp, i64, i64, vp, i32]
+        h.orc_count_bad_pix.argtypes = [vp, i64, i64]
+        h.orc_count_bad_pix.restype = ctypes.c_int64
+        h.orc_max_threads.restype = ctypes.c_int
+        _LIB = h
+    return _LIB
+
+
+def ref_lib():
+    """ctypes handle on oracle/_ref/libminkasi.so (the reference's own C,
+    compiled by ``make -C oracle ref``), or None where it was not built."""
+    p = os.path.join(_HERE, "_ref", "libminkasi.so")
+    if not os.path.exists(p):
+        return None
+    h = ctypes.CDLL(p)
+    vp, i32 = ctypes.c_void_p, ctypes.c_int
+    h.map2tod_omp.argtypes = [vp, vp, i32, i32, vp, i32]
+    h.tod2map_omp.argtypes = [vp, vp, i32, i32, vp, i32]
+    h.tod2map_simple.argtypes = [vp, vp, i32, i32, vp]
+    h.set_nthread.argtypes = [i32]
+    return h
+
+
+def _c(a: np.ndarray) -> int:
+    assert a.flags.c_contiguous
+    return a.ctypes.data
+
+
+# --------------------------------------------------------------------------
+# projections
+# --------------------------------------------------------------------------
+def map2tod(dat: np.ndarray, map: np.ndarray, ipix: np.ndarray, do_add: bool = True,
+            nthread: int = 0) -> None:
+    """dat (+)= map.flat[ipix]  (minkasi.c:131-144)."""
+    assert ipix.dtype == np.int32 and ipix.shape == dat.shape
+    ndet, ndata = dat.shape
+    if dat.dtype == np.float64:
+        assert map.dtype == np.float64
+        lib().orc_map2tod(_c(dat), _c(map), ndet, ndata, _c(ipix), int(do_add), nthread)
+    else:
+        assert dat.dtype == np.float32 and map.dtype == np.float32
+        lib().orc_map2tod_f32(_c(dat), _c(map), ndet, ndata, _c(ipix), int(do_add), nthread)
+
+
+def tod2map(map: np.ndarray, dat: np.ndarray, ipix: np.ndarray, nthread: int = 0) -> None:
+    """map.flat[ipix] += dat  (minkasi.c:97-112), deterministic for fixed nthread."""
+    assert ipix.dtype == np.int32 and ipix.shape == dat.shape
+    ndet, ndata = dat.shape
+    fn = lib().orc_tod2map if dat.dtype == np.float64 else lib().orc_tod2map_f32
+    assert map.dtype == dat.dtype
+    rc = fn(_c(map), _c(dat), ndet, ndata, _c(ipix), map.size, nthread)
+    if rc != 0:
+        raise MemoryError("oracle tod2map could not allocate its private maps")
+
+
+def tod2map_serial(map: np.ndarray, dat: np.ndarray, ipix: np.ndarray) -> None:
+    """Serial scatter in sample order (minkasi.c:50-55)."""
+    ndet, ndata = dat.shape
+    lib().orc_tod2map_serial(_c(map), _c(dat), ndet, ndata, _c(ipix))
+
+
+# --------------------------------------------------------------------------
+# DCT-I and the SmoothedSVD noise filter
+# --------------------------------------------------------------------------
+def dct1(x: np.ndarray, workers: int = 1) -> np.ndarray:
+    """Unnormalised DCT-I (FFTW REDFT00) along the last axis:
+    X_k = x_0 + (-1)^k x_{n-1} + 2 sum_{j=1}^{n-2} x_j cos(pi j k/(n-1)).
+    Same transform the reference's fallback applies row by row
+    (py_fft.py:254-285 -> scipy.fft.dct(type=1))."""
+    return scipy.fft.dct(np.asarray(x), type=1, axis=-1, workers=workers)
+
+
+def apply_noise(v: np.ndarray, vT: np.ndarray, mywt: np.ndarray, dat: np.ndarray,
+                noisevec: Optional[np.ndarray] = None, workers: int = 1) -> np.ndarray:
+    """NoiseSmoothedSVD.apply_noise (noise.py:680-714):
+    dd = vT . DCT1(mywt[:, :n] * DCT1(v . dat)), columns 0 and -1 halved,
+    with the optional prewhitening division before and after."""
+    noisemat = None
+    if noisevec is not None:
+        noisemat = np.repeat([noisevec], dat.shape[1], axis=0).T
+        dat = dat / noisemat
+    dat_rot = np.dot(v, dat)
+    datft = dct1(dat_rot, workers)
+    nn = datft.shape[1]
+    datft = datft * mywt[:, :nn]
+    dat_rot = dct1(datft, workers)
+    dd = np.dot(vT, dat_rot)
+    dd[:, 0] = 0.5 * dd[:, 0]
+    dd[:, -1] = 0.5 * dd[:, -1]
+    if noisemat is not None:
+        dd = dd / noisemat
+    return dd
+
+
+def smooth_many_vecs(vecs: np.ndarray, fwhm: float = 20.0) -> np.ndarray:
+    """Gaussian smoothing of each row as a DCT-I convolution (smooth.py:49-78)."""
+    n = vecs.shape[1]
+    x = np.arange(n)
+    sig = fwhm / np.sqrt(8 * np.log(2))
+    to_conv = np.exp(-0.5 * (x / sig) ** 2)
+    tot = to_conv[0] + to_conv[-1] + 2 * to_conv[1:-1].sum()
+    to_conv = to_conv / tot
+    to_conv_ft = dct1(to_conv)
+    xtrans = dct1(vecs)
+    xtrans *= to_conv_ft
+    back = dct1(xtrans)
+    return back / (2 * (n - 1))
+
+
+def noise_model(dat: np.ndarray, fwhm: float = 50.0, u: Optional[np.ndarray] = None,
+                prewhiten: bool = False):
+    """NoiseSmoothedSVD.__init__ (noise.py:604-678).  Returns (v, vT, mywt, noisevec).
+
+    ``u`` plays the role of the reference's ``u_in``: when given, vT = inv(v)
+    (noise.py:657-663).  When it is None the left singular vectors come from a
+    thin SVD, which equals the reference's full-matrices SVD in its ``u``
+    factor (the reference's own full SVD needs an nsamp x nsamp matrix) and
+    vT = v.T as in the reference."""
+    noisevec = None
+    if prewhiten:
+        noisevec = np.median(np.abs(np.diff(dat, axis=1)), axis=1)
+        dat = dat / np.repeat([noisevec], dat.shape[1], axis=0).T
+    if u is None:
+        uu, _, _ = np.linalg.svd(dat, full_matrices=False)
+        v = np.array(uu.T)
+        vT = v.T.copy()
+    else:
+        v = np.array(u.T)
+        vT = np.linalg.inv(v)
+    dat_rot = np.dot(v, dat)
+    dat_trans = dct1(dat_rot)
+    spec = smooth_many_vecs(dat_trans ** 2, fwhm)
+    spec[:, 1:] = 1.0 / spec[:, 1:]
+    spec[:, 0] = 0
+    return v, vT, spec, noisevec
+
+
+def det_weights(v: np.ndarray, vT: np.ndarray, mywt: np.ndarray) -> np.ndarray:
+    """NoiseSmoothedSVD.get_det_weights (noise.py:761-772)."""
+    mode_wt = np.sum(mywt, axis=1)
+    tmp = np.dot(vT, np.dot(np.diag(mode_wt), v))
+    return np.diag(tmp).copy() * 2.0
+
+
+# --------------------------------------------------------------------------
+# the operator A = sum_tod P^T N P, the RHS, hits and PCG
+# --------------------------------------------------------------------------
+@dataclass
+class OracleTod:
+    ipix: np.ndarray            # (ndet, ndata) int32
+    v: np.ndarray               # (ndet, ndet)
+    vT: np.ndarray              # (ndet, ndet)
+    mywt: np.ndarray            # (ndet, >= ndata)
+    dat: Optional[np.ndarray] = None      # dat_calib (ndet, ndata)
+    noisevec: Optional[np.ndarray] = None
+
+
+def todvec_dot(tods: Sequence[OracleTod], x: np.ndarray, workers: int = 1,
+               nthread: int = 0) -> np.ndarray:
+    """TodVec.dot with one SkyMap (core.py:967-1026 -> Tod.dot :649-691):
+    out = sum_tod P^T N P x."""
+    out = np.zeros_like(x)
+    for t in tods:
+        tmp = np.zeros(t.ipix.shape, dtype=x.dtype)
+        map2tod(tmp, x, t.ipix, True, nthread)
+        tmp = apply_noise(t.v, t.vT, t.mywt, tmp, t.noisevec, workers)
+        tod2map(out, np.ascontiguousarray(tmp), t.ipix, nthread)
+    return out
+
+
+def make_rhs(tods: Sequence[OracleTod], npix_shape, workers: int = 1) -> np.ndarray:
+    """TodVec.make_rhs (core.py:1028-1047): b = sum_tod P^T N d."""
+    b = np.zeros(npix_shape)
+    for t in tods:
+        dd = apply_noise(t.v, t.vT, t.mywt, t.dat, t.noisevec, workers)
+        tod2map(b, np.ascontiguousarray(dd), t.ipix)
+    return b
+
+
+def make_hits(tods: Sequence[OracleTod], npix_shape, do_weights: bool = False) -> np.ndarray:
+    """make_hits (tod2map.py:343-400): tod2map of ones (or of per-detector
+    weights from det_weights) summed over TODs."""
+    hits = np.zeros(npix_shape)
+    for t in tods:
+        if do_weights:
+            w = det_weights(t.v, t.vT, t.mywt)
+            tmp = np.outer(w, np.ones(t.ipix.shape[1]))
+        else:
+            tmp = np.ones(t.ipix.shape)
+        tod2map(hits, tmp, t.ipix)
+    return hits
+
+
+def jacobi_from_hits(hits: np.ndarray) -> np.ndarray:
+    """precon = 1/hits where hits > 0, else 0
+    (examples/minkasi_mpi_example.py:99-105)."""
+    p = np.zeros_like(hits)
+    ii = hits > 0
+    p[ii] = 1.0 / hits[ii]
+    return p
+
+
+def run_pcg(b: np.ndarray, x0: np.ndarray, apply_A, precon: Optional[np.ndarray] = None,
+            maxiter: int = 25, history: Optional[List[dict]] = None) -> np.ndarray:
+    """run_pcg_wprior without prior (pcg.py:22-200, wrapper :203-238): fixed
+    ``maxiter`` iterations, same order of updates, np.sum dots."""
+    Ax = apply_A(x0)
+    r = b - Ax
+    z = precon * r if precon is not None else r.copy()
+    p = z.copy()
+    zr = float(np.sum(r * z))
+    x = x0.copy()
+    for i in range(maxiter):
+        Ap = apply_A(p)
+        pAp = float(np.sum(p * Ap))
+        alpha = zr / pAp
+        x = x + alpha * p
+        r = r + (-alpha) * Ap
+        z = precon * r if precon is not None else r.copy()
+        zr_new = float(np.sum(r * z))
+        beta = zr_new / zr
+        p = z + beta * p
+        zr = zr_new
+        if history is not None:
+            history.append({"iter": i, "alpha": alpha, "beta": beta, "zr": zr})
+    return x
+
+
+# --------------------------------------------------------------------------
+# TOD length truncation
+# --------------------------------------------------------------------------
+def _nsphere_vol(npp: int) -> float:
+    if npp % 2:
+        nn = (npp - 1) / 2
+        return 2 ** (nn + 1) * np.pi ** nn / np.prod(np.arange(1, npp + 1, 2))
+    nn = npp / 2
+    return (np.pi ** nn) / np.prod(np.arange(1, nn + 1))
+
+
+def find_good_fft_lens(n: int, primes: Sequence[int] = (2, 3, 5, 7)) -> np.ndarray:
+    """All products of ``primes`` up to about n, enumerated in log2 space
+    (py_fft.py:300-395)."""
+    lp = np.log2(np.asarray(primes, dtype=float))
+    r = np.log2(n + 0.5)
+    out: List[float] = []
+
+    def rec(level: int, lcur: float):
+        if level == len(lp) - 1:
+            out.extend(np.arange(lcur, r + 1e-3, lp[level]).tolist())
+            return
+        for fac in np.arange(lcur, r, lp[level]):
+            rec(level + 1, fac)
+
+    rec(0, 0.0)
+    return np.sort(np.asarray(np.round(2 ** np.asarray(out)), dtype=int))
+
+
+def truncate_len(ndata: int, primes: Sequence[int] = (2, 3, 5, 7, 11)) -> int:
+    """Length that truncate_tod (processing.py:648-682) cuts ndata down to."""
+    new = int(find_good_fft_lens(ndata - 1, primes).max()) + 1
+    return new if new < ndata else ndata

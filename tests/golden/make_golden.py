@@ -1,0 +1,196 @@
+"""Generate the golden fixtures in tests/golden/*.npz by running the REFERENCE
+minkasi code (its Python + its own C library compiled from source) on small
+seeded inputs.  Run here, where the reference tree is mounted:
+
+    python tests/golden/make_golden.py
+
+Every fixture stores its inputs and the reference's outputs, so the tests
+(oracle and GPU) need neither the reference nor this script at run time.
+
+Reference entry points exercised (paths in the minkasi project):
+  map2tod            minkasi/mapmaking/map2tod.py:19-54  -> minkasi/lib/minkasi.c:116-144
+  tod2map_omp/simple minkasi/mapmaking/tod2map.py:29-128 -> minkasi/lib/minkasi.c:50-112
+  fft_r2r            minkasi/tools/py_fft.py:254-285 (scipy DCT-I, the shipped default)
+  NoiseSmoothedSVD   minkasi/mapmaking/noise.py:584-772
+  smooth_many_vecs   minkasi/tools/smooth.py:49-78
+  Tod / TodVec.dot / make_rhs   minkasi/tods/core.py:517-691,967-1047
+  make_hits          minkasi/mapmaking/tod2map.py:343-400
+  run_pcg            minkasi/mapmaking/pcg.py:22-238
+  truncate_tod / find_good_fft_lens  minkasi/tods/processing.py:648-682, minkasi/tools/py_fft.py:364-395
+"""
+import contextlib
+import io
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+import ref_import  # noqa: E402
+
+mk = ref_import.import_reference()
+from minkasi.mapmaking import map2tod as ref_m2t  # noqa: E402
+from minkasi.mapmaking import tod2map as ref_t2m  # noqa: E402
+from minkasi.mapmaking.noise import NoiseSmoothedSVD  # noqa: E402
+from minkasi.mapmaking.pcg import run_pcg  # noqa: E402
+from minkasi.maps import Mapset, SkyMap  # noqa: E402
+from minkasi.tods import Tod, TodVec  # noqa: E402
+from minkasi.tods import processing  # noqa: E402
+from minkasi.tools import py_fft, smooth  # noqa: E402
+
+
+def quiet(fn, *a, **k):
+    with contextlib.redirect_stdout(io.StringIO()):
+        return fn(*a, **k)
+
+
+def save(name, **arrs):
+    path = os.path.join(HERE, name)
+    np.savez_compressed(path, **arrs)
+    print(f"wrote {name}: {os.path.getsize(path)/1024:.1f} KiB")
+
+
+def bare_skymap(nx, ny):
+    """A SkyMap without astropy: the attributes SkyMap.map2tod/tod2map/dot/
+    axpy/copy/__mul__ read (skymap.py:400-440,542-609,651-666,724-740)."""
+    m = SkyMap.__new__(SkyMap)
+    m.nx, m.ny = nx, ny
+    m.map = np.zeros((nx, ny))
+    m.caches = None
+    m.tag = "ipix"
+    m.purge_pixellization = False
+    return m
+
+
+def synth_tod(rng, ndet, ndata, nx, ny, cm_amp=3.0, knee_frac=0.02):
+    """Small daisy-like pointing + white / 1-f / common-mode noise."""
+    t = np.arange(ndata)
+    r = 0.4 * min(nx, ny) * np.sin(2 * np.pi * t / 611.0 + rng.uniform(0, 6))
+    th = 2 * np.pi * t / 1777.0 + rng.uniform(0, 6)
+    offs = rng.uniform(-1.5, 1.5, size=(ndet, 2))
+    x = nx / 2 + r * np.cos(th) + offs[:, :1]
+    y = ny / 2 + r * np.sin(th) + offs[:, 1:]
+    x = np.clip(np.round(x), 0, nx - 1)
+    y = np.clip(np.round(y), 0, ny - 1)
+    ipix = np.asarray(x * ny + y, dtype=np.int32)
+    white = rng.standard_normal((ndet, ndata))
+    f = np.fft.rfftfreq(ndata)
+    f[0] = f[1]
+    amp = np.sqrt(1 + (knee_frac / f) ** 2)
+    red = np.fft.irfft(np.fft.rfft(rng.standard_normal((ndet, ndata))) * amp, n=ndata)
+    cm = cm_amp * np.fft.irfft(np.fft.rfft(rng.standard_normal(ndata)) * amp, n=ndata)
+    return ipix, white + red + cm[None, :]
+
+
+def case_proj(rng):
+    ndet, ndata, nx, ny = 7, 1001, 37, 23
+    npix = nx * ny
+    ipix = rng.integers(0, npix, size=(ndet, ndata)).astype(np.int32)
+    ipix[0, 0], ipix[-1, -1] = 0, npix - 1
+    # runs of repeated pixels, as a slow scan produces
+    ipix[3] = np.repeat(rng.integers(0, npix, size=ndata // 7 + 1), 7)[:ndata]
+    dat = rng.standard_normal((ndet, ndata))
+    map_ = rng.standard_normal((nx, ny))
+    d_add = dat.copy()
+    ref_m2t.map2tod(d_add, map_, ipix, do_add=True, do_omp=True)
+    d_set = dat.copy()
+    ref_m2t.map2tod(d_set, map_, ipix, do_add=False, do_omp=True)
+    d_add_s = dat.copy()
+    ref_m2t.map2tod(d_add_s, map_, ipix, do_add=True, do_omp=False)
+    m_omp = map_.copy()
+    quiet(ref_t2m.tod2map_omp, m_omp, dat, ipix)
+    m_simple = map_.copy()
+    quiet(ref_t2m.tod2map_simple, m_simple, dat, ipix)
+    save("proj.npz", ipix=ipix, dat=dat, map=map_, map2tod_add=d_add, map2tod_set=d_set,
+         map2tod_add_simple=d_add_s, tod2map_omp=m_omp, tod2map_simple=m_simple)
+
+
+def case_dct(rng):
+    out = {}
+    for i, shape in enumerate([(3, 2), (2, 3), (4, 17), (4, 257), (3, 1000), (5, 1025), (1, 4097)]):
+        x = rng.standard_normal(shape)
+        out[f"x{i}"] = x
+        out[f"y{i}"] = py_fft.fft_r2r(x)
+    v = rng.standard_normal(513)
+    out["vec_x"], out["vec_y"] = v, py_fft.fft_r2r(v)
+    s = np.abs(rng.standard_normal((3, 600))) + 0.1
+    out["smooth_x"], out["smooth_y"] = s, smooth.smooth_many_vecs(s, 50.0)
+    save("dct.npz", **out)
+
+
+def case_noise(rng):
+    ndet, ndata = 10, 1025
+    _, dat = synth_tod(rng, ndet, ndata, 16, 16)
+    nm = quiet(NoiseSmoothedSVD, dat, fwhm=50.0)
+    nm_pw = quiet(NoiseSmoothedSVD, dat, fwhm=50.0, prewhiten=True)
+    u_thin, _, _ = np.linalg.svd(dat, full_matrices=False)
+    nm_u = quiet(NoiseSmoothedSVD, dat, fwhm=50.0, u_in=u_thin)
+    x = rng.standard_normal((ndet, ndata))
+    x_short = rng.standard_normal((ndet, 700))
+    save("noise.npz", dat=dat, x=x, x_short=x_short,
+         v=nm.v, vT=nm.vT, mywt=nm.mywt, dd=nm.apply_noise(x), dd_short=nm.apply_noise(x_short),
+         detw=nm.get_det_weights(),
+         pw_v=nm_pw.v, pw_vT=nm_pw.vT, pw_mywt=nm_pw.mywt, pw_noisevec=nm_pw.noisevec,
+         pw_dd=nm_pw.apply_noise(x),
+         u_thin=u_thin, u_v=nm_u.v, u_vT=nm_u.vT, u_mywt=nm_u.mywt, u_dd=nm_u.apply_noise(x))
+
+
+def case_solve(rng):
+    nx, ny = 20, 24
+    shapes = [(8, 1537), (6, 1201)]
+    todvec = TodVec()
+    store = {}
+    for k, (ndet, ndata) in enumerate(shapes):
+        ipix, noise = synth_tod(rng, ndet, ndata, nx, ny)
+        sky = np.exp(-((np.arange(nx)[:, None] - nx / 2) ** 2 + (np.arange(ny)[None, :] - ny / 2) ** 2) / 18.0)
+        dat = np.ascontiguousarray(sky.ravel()[ipix] * 5.0 + noise)
+        info = {"dat_calib": dat, "ipix": ipix}
+        tod = Tod(info)
+        quiet(tod.set_noise, NoiseSmoothedSVD)
+        quiet(todvec.add_tod, tod)
+        t = todvec.tods[-1]
+        store[f"t{k}_ipix"], store[f"t{k}_dat"] = ipix, dat
+        store[f"t{k}_v"], store[f"t{k}_vT"], store[f"t{k}_mywt"] = t.noise.v, t.noise.vT, t.noise.mywt
+    m = bare_skymap(nx, ny)
+    hits = quiet(ref_t2m.make_hits, todvec, m)
+    whits = quiet(ref_t2m.make_hits, todvec, m, do_weights=True)
+    mapset = Mapset()
+    mapset.add_map(m)
+    rhs = mapset.copy()
+    quiet(todvec.make_rhs, rhs)
+    xr = mapset.copy()
+    xr.maps[0].map[:] = rng.standard_normal((nx, ny))
+    ax = quiet(todvec.dot, xr)
+    x0 = rhs.copy()
+    x0.clear()
+    precon = mapset.copy()
+    tmp = hits.map.copy()
+    ii = tmp > 0
+    tmp[ii] = 1.0 / tmp[ii]
+    precon.maps[0].map[:] = tmp
+    xs = quiet(run_pcg, rhs, x0, todvec, precon, maxiter=8)
+    save("solve.npz", nx=nx, ny=ny, ntod=len(shapes), hits=hits.map, whits=whits.map,
+         rhs=rhs.maps[0].map, xr=xr.maps[0].map, Axr=ax.maps[0].map, precon=tmp,
+         pcg8=xs.maps[0].map, **store)
+
+
+def case_lens():
+    ndata = np.array([1000, 1025, 2049, 65536, 131072, 200001, 262144, 300000, 450001, 524288,
+                      600000, 50000, 123457, 499999])
+    new = []
+    for n in ndata:
+        info = {"dat_calib": np.zeros((1, int(n)), dtype=np.float32)}
+        quiet(processing.truncate_tod, info)
+        new.append(info["dat_calib"].shape[1])
+    good = py_fft.find_good_fft_lens(1000, [2, 3, 5, 7, 11])
+    save("lens.npz", ndata=ndata, truncated=np.array(new), good1000=good)
+
+
+if __name__ == "__main__":
+    rng = np.random.default_rng(0)
+    case_proj(rng)
+    case_dct(rng)
+    case_noise(rng)
+    case_solve(rng)
+    case_lens()

@@ -1,0 +1,87 @@
+"""Pin the CPU oracle against fixtures produced by the reference code itself
+(tests/golden/make_golden.py).  CPU only."""
+import numpy as np
+import pytest
+
+import oracle
+
+
+def test_projections_match_reference(gold):
+    g = gold("proj.npz")
+    ipix, dat, m = g["ipix"], g["dat"], g["map"]
+    d = dat.copy()
+    oracle.map2tod(d, m, ipix, do_add=True)
+    assert np.array_equal(d, g["map2tod_add"])          # gather: bit-exact
+    d = dat.copy()
+    oracle.map2tod(d, m, ipix, do_add=False)
+    assert np.array_equal(d, g["map2tod_set"])
+    mm = m.copy()
+    oracle.tod2map_serial(mm, dat, ipix)
+    assert np.array_equal(mm, g["tod2map_simple"])      # same summation order
+    mm = m.copy()
+    oracle.tod2map(mm, dat, ipix)
+    np.testing.assert_allclose(mm, g["tod2map_omp"], rtol=1e-12, atol=1e-12)
+
+
+def test_dct1_matches_reference(gold):
+    g = gold("dct.npz")
+    i = 0
+    while f"x{i}" in g:
+        np.testing.assert_array_equal(oracle.dct1(g[f"x{i}"]), g[f"y{i}"])
+        i += 1
+    np.testing.assert_array_equal(oracle.dct1(g["vec_x"]), g["vec_y"])
+    np.testing.assert_allclose(oracle.smooth_many_vecs(g["smooth_x"], 50.0), g["smooth_y"],
+                               rtol=1e-13, atol=0)
+
+
+def test_dct1_is_its_own_inverse_up_to_2n_minus_2():
+    x = np.random.default_rng(1).standard_normal((3, 129))
+    np.testing.assert_allclose(oracle.dct1(oracle.dct1(x)), 2 * 128 * x, rtol=1e-12, atol=1e-11)
+
+
+def test_noise_model_and_apply_match_reference(gold):
+    g = gold("noise.npz")
+    # apply_noise with the reference's own model arrays
+    np.testing.assert_allclose(oracle.apply_noise(g["v"], g["vT"], g["mywt"], g["x"]), g["dd"],
+                               rtol=0, atol=1e-12 * np.abs(g["dd"]).max())
+    np.testing.assert_allclose(oracle.apply_noise(g["v"], g["vT"], g["mywt"], g["x_short"]),
+                               g["dd_short"], rtol=0, atol=1e-12 * np.abs(g["dd_short"]).max())
+    np.testing.assert_allclose(
+        oracle.apply_noise(g["pw_v"], g["pw_vT"], g["pw_mywt"], g["x"], g["pw_noisevec"]),
+        g["pw_dd"], rtol=0, atol=1e-12 * np.abs(g["pw_dd"]).max())
+    np.testing.assert_allclose(oracle.det_weights(g["v"], g["vT"], g["mywt"]), g["detw"], rtol=1e-12)
+    # model construction through the u_in path reproduces v, vT, mywt
+    v, vT, mywt, _ = oracle.noise_model(g["dat"], 50.0, u=g["u_thin"])
+    np.testing.assert_allclose(v, g["u_v"], rtol=0, atol=1e-15)
+    np.testing.assert_allclose(vT, g["u_vT"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(mywt, g["u_mywt"], rtol=1e-10)
+    # prewhitened model: noisevec is a median, reproduced exactly
+    _, _, _, nv = oracle.noise_model(g["dat"], 50.0, prewhiten=True)
+    np.testing.assert_array_equal(nv, g["pw_noisevec"])
+
+
+def _tods(g):
+    return [oracle.OracleTod(ipix=g[f"t{k}_ipix"], v=g[f"t{k}_v"], vT=g[f"t{k}_vT"],
+                             mywt=g[f"t{k}_mywt"], dat=g[f"t{k}_dat"]) for k in range(int(g["ntod"]))]
+
+
+def test_operator_rhs_hits_pcg_match_reference(gold):
+    g = gold("solve.npz")
+    tods = _tods(g)
+    shape = (int(g["nx"]), int(g["ny"]))
+    np.testing.assert_array_equal(oracle.make_hits(tods, shape), g["hits"])
+    np.testing.assert_allclose(oracle.make_hits(tods, shape, do_weights=True), g["whits"], rtol=1e-12)
+    b = oracle.make_rhs(tods, shape)
+    np.testing.assert_allclose(b, g["rhs"], rtol=0, atol=1e-12 * np.abs(g["rhs"]).max())
+    ax = oracle.todvec_dot(tods, g["xr"])
+    np.testing.assert_allclose(ax, g["Axr"], rtol=0, atol=1e-12 * np.abs(g["Axr"]).max())
+    x = oracle.run_pcg(g["rhs"], np.zeros(shape), lambda m: oracle.todvec_dot(tods, m),
+                       g["precon"], maxiter=8)
+    np.testing.assert_allclose(x, g["pcg8"], rtol=0, atol=1e-9 * np.abs(g["pcg8"]).max())
+
+
+def test_truncation_lengths_match_reference(gold):
+    g = gold("lens.npz")
+    for n, t in zip(g["ndata"], g["truncated"]):
+        assert oracle.truncate_len(int(n)) == int(t), n
+    np.testing.assert_array_equal(oracle.find_good_fft_lens(1000, [2, 3, 5, 7, 11]), g["good1000"])
