@@ -1,0 +1,402 @@
+"""Benchmark: tod2map GB/s on the 32-TOD FP64 workload (plus the PCG iteration).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (the reference's "plain method at GPU scale" configuration): 32
+synthetic TODs, 256 detectors each, nsamp ~ U[2^17, 2^19] truncated to
+FFT-friendly lengths, daisy-scan pointing onto a 1024x1024 map at 1",
+FP64.  One step = one tod2map pass of every TOD's timestream into the map
+(the projection of TodVec.make_rhs / TodVec.dot), inputs resident in HBM.
+value = algorithmic bytes (4 B ipix + 8 B dat per sample) / step time.
+The inputs (32 GB) exceed the 129 MB L2, so no flush is needed between steps.
+
+e2e: the same step through the public API (SkyMap.tod2map per TOD) with the
+timestream in pinned host memory, copied to the device inside the timed
+region, and the map read back to the host every step; the pixel indices stay
+cached on the device as the API caches them (tod.info[tag]).
+
+Extra keys: per-iteration timings of the full hot path (FP64 Jacobi PCG
+iteration = batched A-apply + update, and the FP32 inner iteration of the
+mixed-precision solver) on the same TODs, and the CPU baseline.
+
+--impl reference times the reference's CPU tod2map (its own C compiled from
+source when available in oracle/_ref, else the C restatement in oracle/)
+with all host threads on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+WORKLOAD = "c2: 32 TODs x 256 det x U[2^17,2^19] samples (truncated), 1024x1024 map at 1in, FP64"
+METRIC = "tod2map GB/s"
+BYTES_PER_SAMPLE = 12  # int32 pixel index + float64 sample
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="c2")
+    ap.add_argument("--no-pcg", action="store_true", help="skip the PCG-iteration extras")
+    ap.add_argument("--method", default=None, help="force the tod2map kernel (atomic|fixed|sorted)")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- workload
+def build_workload(cfg_name, device, with_noise):
+    import torch
+    from minkasi_gb300 import synth
+    from minkasi_gb300.maps import SkyMap
+    from minkasi_gb300.tods import Tod, TodVec
+
+    cfg = synth.CONFIGS[cfg_name]
+    tv = TodVec()
+    gen = torch.Generator(device=device)
+    gen.manual_seed(1)
+    for k, (ndet, n) in enumerate(synth.tod_shapes(cfg)):
+        if with_noise:
+            info = synth.make_tod_info(cfg, k, ndet, n, device)
+            tod = Tod(info)
+            tod.set_noise()
+        else:
+            info = synth.make_tod_info(cfg, k, ndet, n, device, with_data=False)
+            info["dat_calib"] = torch.randn((ndet, n), generator=gen, dtype=torch.float64, device=device)
+            tod = Tod(info)
+        tv.add_tod(tod)
+    m = SkyMap(nx=cfg.nx, ny=cfg.ny, device=device)
+    return cfg, tv, m
+
+
+def time_steps(fn, steps, warmup, stream):
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    t0 = time.perf_counter()
+    for a, b in ev:
+        a.record(stream)
+        fn()
+        b.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    per = [a.elapsed_time(b) for a, b in ev]
+    return sum(per), per, wall
+
+
+# ---------------------------------------------------------------- CPU baseline
+def cpu_tod2map_sample(tods_host, npix, seconds=12.0, prefer_ref=True):
+    """Time the CPU tod2map over host copies of some TODs, all threads.
+    Returns (GB/s, description, kind, cores)."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+
+    ref = oracle.ref_lib() if prefer_ref else None
+    cores = os.cpu_count() or 1
+    mp = np.zeros(npix)
+    reps, nbytes, t_used = 0, 0, 0.0
+    t_start = time.perf_counter()
+    while time.perf_counter() - t_start < seconds:
+        for ip, d in tods_host:
+            t0 = time.perf_counter()
+            if ref is not None:
+                ref.tod2map_omp(mp.ctypes.data, d.ctypes.data, d.shape[0], d.shape[1], ip.ctypes.data,
+                                npix)
+            else:
+                oracle.tod2map(mp, d, ip, nthread=cores)
+            t_used += time.perf_counter() - t0
+            nbytes += d.size * BYTES_PER_SAMPLE
+        reps += 1
+    kind = "reference" if ref is not None else "port"
+    desc = (f"{len(tods_host)} of the workload's TODs ({sum(d.size for _, d in tods_host)} samples) "
+            f"x {reps} passes, {cores} threads, {'reference tod2map_omp (minkasi.c) built from source' if ref is not None else 'oracle C restatement of tod2map_omp'}")
+    return nbytes / t_used / 1e9, desc, kind, cores
+
+
+def host_sample(tv, max_samples=3.5e8):
+    out, tot = [], 0
+    for t in tv.tods:
+        if tot >= max_samples:
+            break
+        ip = t.info["ipix"].cpu().numpy()
+        d = t.info["dat_calib"].cpu().numpy()
+        out.append((np.ascontiguousarray(ip), np.ascontiguousarray(d)))
+        tot += d.size
+    return out
+
+
+# ---------------------------------------------------------------- arms
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    import torch
+    from minkasi_gb300 import synth
+
+    cfg = synth.CONFIGS[args.config]
+    shapes = synth.tod_shapes(cfg)
+    npix = cfg.nx * cfg.ny
+    # the same pointing and the same kind of data as our arm, generated on
+    # the CPU for a bounded sample of TODs
+    dev = torch.device("cpu")
+    sample = []
+    tot = 0
+    for k, (ndet, n) in enumerate(shapes):
+        if tot >= 2.0e8:
+            break
+        info = synth.make_tod_info(cfg, k, ndet, n, dev, with_data=False)
+        d = np.random.default_rng(k).standard_normal((ndet, n))
+        sample.append((info["ipix"].numpy(), d))
+        tot += d.size
+    vals = []
+    desc = kind = None
+    cores = os.cpu_count()
+    for _ in range(args.warmup):
+        cpu_tod2map_sample(sample, npix, seconds=0.5)
+    for _ in range(args.steps):
+        v, desc, kind, cores = cpu_tod2map_sample(sample, npix, seconds=2.0)
+        vals.append(v)
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": 0,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": desc},
+            "cpu_baseline": {"value": value, "unit": "GB/s", "cores": cores, "kind": kind,
+                             "sample": desc},
+            "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "vs_baseline": None}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    import minkasi_gb300  # noqa: F401
+    from minkasi_gb300 import kernels as K
+    from minkasi_gb300 import parallel
+
+    with_noise = not args.no_pcg
+    cfg, tv, m = build_workload(args.config, dev, with_noise)
+    # weak scaling: every rank runs the full workload on its own GPU and
+    # the map is summed over ranks once per step (the reference's reduction)
+    if args.method:
+        tv.tod2map_method = args.method
+    op = tv.engine(m)
+    S = op.S
+    for view, t in zip(op.views(op.tmp), tv.tods):
+        view.copy_(t.info["dat_calib"])
+    out = torch.zeros(op.npix, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def step():
+        op.project_out(out)
+        parallel.allreduce_(out)
+
+    # dominant-kernel timing: the scatter kernel alone, on the launching stream
+    parallel.barrier()
+    with ClockSampler(local) as clk:
+        total_ms, per, wall = time_steps(step, args.steps, args.warmup, stream)
+    parallel.barrier()
+    tmax = torch.tensor([total_ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
+    total_ms = float(tmax.item())
+    ms_step = total_ms / args.steps
+    gbs = world * S * BYTES_PER_SAMPLE / (ms_step * 1e-3) / 1e9
+    launches_per_step = {"atomic": 1, "fixed": 4, "sorted": len(tv.tods)}[op.method]
+
+    # e2e through the public API with host buffers
+    host = [t.info["dat_calib"].cpu().pin_memory() for t in tv.tods]
+    h2d = sum(h.numel() * 8 for h in host)
+    devbuf = [torch.empty_like(t.info["dat_calib"]) for t in tv.tods]
+
+    def e2e_step():
+        m.clear()
+        for t, h, d in zip(tv.tods, host, devbuf):
+            d.copy_(h, non_blocking=True)
+            m.tod2map(t, d)
+        return m.map.cpu()
+
+    for _ in range(args.warmup):
+        e2e_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_gbs = world * S * BYTES_PER_SAMPLE / e2e_s / 1e9
+    del devbuf, host
+
+    # extras: the full hot path per PCG iteration
+    extras = {}
+    if with_noise and rank == 0:
+        extras = pcg_extras(tv, m, dev)
+
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(REPO, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    cpu = None
+    if rank == 0 and world == 1:
+        v, desc, kind, cores = cpu_tod2map_sample(host_sample(tv), op.npix, seconds=12.0)
+        cpu = {"value": v, "unit": "GB/s", "cores": cores, "kind": kind, "sample": desc}
+    if rank != 0:
+        return
+    clocks = clk.summary()
+    traffic = None
+    tr_file = os.path.join(REPO, "profiles", "tod2map_c2_traffic.json")
+    if os.path.exists(tr_file):
+        try:
+            traffic = json.load(open(tr_file)).get(op.method)
+        except (OSError, ValueError):
+            traffic = None
+    line = {
+        "metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "samples": S, "ntod": len(tv.tods), "npix": op.npix,
+                   "tod2map_kernel": op.method, "l2": "inputs (12 B x samples) larger than L2; no flush",
+                   "parallelism": f"replicas x{world}, map all-reduce per step"},
+        "roofline": {"bound": "hbm", "achieved": gbs / world, "peak": peak, "unit": "GB/s",
+                     "frac": gbs / world / peak, "traffic": traffic,
+                     "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"},
+        "e2e": {"value": e2e_gbs, "unit": "GB/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": op.npix * 8},
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+        "wall_s_timed": wall,
+    }
+    line.update(extras)
+    print(json.dumps(line))
+
+
+def pcg_extras(tv, m, dev):
+    """Time FP64 Jacobi PCG iterations and FP32 inner iterations (graph replay)."""
+    import torch
+    import minkasi_gb300 as mk
+    from minkasi_gb300.pcg import DevicePCG
+
+    mapset = mk.Mapset()
+    mapset.add_map(m)
+    rhs = mapset.copy()
+    tv.make_rhs(rhs)
+    pre = mk.jacobi_precon(mk.make_hits(tv, m))
+    S = tv.get_nsamp()
+    res = {}
+    for name, dtype in (("pcg_iter_f64", torch.float64), ("pcg_iter_f32_inner", torch.float32)):
+        op = tv.engine(m, dtype)
+        b = rhs.maps[0].map.reshape(-1).to(dtype)
+        x = torch.zeros_like(b)
+        st = DevicePCG(op, b, x, pre.maps[0].map, graph=True)
+        st.start()
+        st.step()  # eager first iteration, then captured
+        st.step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        n = 3
+        e0.record()
+        for _ in range(n):
+            st.step()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / n
+        res[name] = {"ms": ms, "Msamp_per_s": S / (ms * 1e-3) / 1e6, "tod2map_kernel": op.method,
+                     "rot_mode": op.rot_mode}
+        del st
+    return res
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

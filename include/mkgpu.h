@@ -1,0 +1,199 @@
+/*
+ * mkgpu.h -- C ABI of libmkgpu.so, the GB300 (sm_103a) mapmaking hot path.
+ *
+ * Conventions shared by every entry point:
+ *  - All array pointers are DEVICE pointers (e.g. torch.Tensor.data_ptr()),
+ *    C-contiguous, owned by the caller.  The library owns only plan objects
+ *    (cuFFT plans, small reduction scratch) that it creates and destroys.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ *    stream).  Every call is stream-ordered and does not synchronise the host
+ *    unless its comment says so.
+ *  - Every function returns an int status: MK_OK (0) or an MK_ERR_* code;
+ *    mk_last_error() returns a message for the last failure on the calling
+ *    host thread.  Asynchronous kernel faults surface at the next call that
+ *    synchronises, like any CUDA call.
+ *  - dtype selects the arithmetic of the arrays named "dtype-typed":
+ *    MK_F64 (double) or MK_F32 (float).  Pixel indices are int32, flattened
+ *    as x*ny + y, exactly the reference's ipix.
+ *  - Layout of TOD arrays: (ndet, ndata) row-major, i.e. detector-major,
+ *    the reference's dat_calib layout.
+ *
+ * Reference interfaces replaced (paths in the minkasi project):
+ *  mk_map2tod          <- map2tod_omp / map2tod_simple, minkasi/lib/minkasi.c:116-144,
+ *                         bound in minkasi/lib/minkasi.py (map2tod_omp_c)
+ *  mk_tod2map          <- tod2map_omp / tod2map_atomic, minkasi/lib/minkasi.c:59-66,97-112,
+ *                         bound in minkasi/lib/minkasi.py:10-60 (tod2map_omp_c)
+ *  mk_tod2map_sorted   <- tod2map_everyone / tod2map_cached, minkasi/lib/minkasi.c:68-95
+ *                         (the reference's owner-computes variants; here deterministic)
+ *  mk_tod2map_rows     <- make_hits' tod2map of a ones / outer(weights, ones) TOD,
+ *                         minkasi/mapmaking/tod2map.py:343-400
+ *  mk_dct1_*           <- many_fft_r2r_1d / many_fftf_r2r_1d (REDFT00),
+ *                         minkasi/lib/mkfftw.c:174-254, bound in minkasi/lib/mkfftw.py
+ *  mk_noise_*          <- NoiseSmoothedSVD.apply_noise, minkasi/mapmaking/noise.py:680-714
+ *  mk_dot / mk_axpy / mk_mul / mk_pcg_*  <- SkyMap.dot/axpy/__mul__ and the
+ *                         run_pcg_wprior recurrence, minkasi/maps/skymap.py:428-440,651-666,724-740,
+ *                         minkasi/mapmaking/pcg.py:101-178
+ */
+#ifndef MKGPU_H
+#define MKGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  MK_OK = 0,
+  MK_ERR_ARG = 1,      /* bad argument (null pointer, size, dtype, alignment) */
+  MK_ERR_CUDA = 2,     /* CUDA runtime error */
+  MK_ERR_CUFFT = 3,    /* cuFFT error */
+  MK_ERR_CUBLAS = 4,   /* cuBLAS error */
+  MK_ERR_RANGE = 5,    /* pixel index outside [0, npix) */
+  MK_ERR_NOMEM = 6,    /* host or device allocation failed */
+  MK_ERR_NUMERIC = 7   /* CG breakdown (p.Ap <= 0) or non-finite scalar */
+};
+
+enum { MK_F64 = 0, MK_F32 = 1 };
+
+/* ---- library ---------------------------------------------------------- */
+const char *mk_last_error(void);
+int mk_version(void);          /* returns the ABI version number (not a status) */
+
+/* ---- pointing projections ---------------------------------------------- */
+
+/* dat[i] = map[ipix[i]] (do_add=0) or dat[i] += map[ipix[i]] (do_add=1),
+ * i over ndet*ndata samples.  dat, map dtype-typed.  A sample whose pixel is
+ * outside [0, npix) gathers 0 (the reference would read out of bounds).
+ * Replaces map2tod_omp, minkasi/lib/minkasi.c:131-144. */
+int mk_map2tod(void *dat, const void *map, const int32_t *ipix, int64_t ndet,
+               int64_t ndata, int64_t npix, int dtype, int do_add, void *stream);
+
+/* map[ipix[i]] += dat[i] with warp-aggregated atomic adds (runs of equal
+ * consecutive pixels are summed in registers first).  Summation order, and
+ * so the last bits, vary from run to run.  Out-of-range pixels are skipped.
+ * Replaces tod2map_omp / tod2map_atomic, minkasi/lib/minkasi.c:59-66,97-112. */
+int mk_tod2map(void *map, const void *dat, const int32_t *ipix, int64_t ndet,
+               int64_t ndata, int64_t npix, int dtype, void *stream);
+
+/* make_hits helper: map[ipix[d,t]] += w[d] (w == NULL: += 1).  w and map
+ * dtype-typed.  Replaces the tod2map of np.ones / np.outer(weights, ones)
+ * in make_hits, minkasi/mapmaking/tod2map.py:343-400. */
+int mk_tod2map_rows(void *map, const void *w, const int32_t *ipix, int64_t ndet,
+                    int64_t ndata, int64_t npix, int dtype, void *stream);
+
+/* Counts pixel indices outside [0, npix) into *nbad (host pointer).
+ * Synchronises `stream`.  The reference only warns on a non-int32 dtype
+ * (minkasi/mapmaking/tod2map.py:48-51); this is the bounds check it lacks. */
+int mk_check_pix(const int32_t *ipix, int64_t n, int64_t npix, int64_t *nbad,
+                 void *stream);
+
+/* Deterministic tod2map.  A pixel plan sorts the (fixed) pointing once:
+ * for each pixel, the list of sample indices that hit it, in sample order.
+ * mk_tod2map_sorted then sums each pixel's samples in that fixed order and
+ * adds the sum to map[p]: bitwise reproducible run to run.  Owner-computes
+ * like tod2map_everyone, minkasi/lib/minkasi.c:68-83.
+ * Plan device memory: 4*(n + npix + 1) bytes plus sort scratch during
+ * creation.  n must be < 2^31. */
+typedef struct mk_pixplan mk_pixplan;
+int mk_pixplan_create(mk_pixplan **plan, const int32_t *ipix, int64_t n,
+                      int64_t npix, void *stream);
+int mk_tod2map_sorted(void *map, const void *dat, const mk_pixplan *plan,
+                      int dtype, void *stream);
+int mk_pixplan_destroy(mk_pixplan *plan);
+
+/* Deterministic tod2map by 64-bit fixed-point accumulation: each sample
+ * contributes llrint(dat[i] * 2^s) to an int64 accumulator per pixel (integer
+ * atomics, so the result is bitwise independent of their order), then
+ * map[p] += acc[p] * 2^-s.  s is chosen on the device from max|dat| and
+ * `hmax`, an upper bound on the number of samples hitting any one pixel
+ * (fixed by the pointing; e.g. the max of the hit map), so no accumulator
+ * can overflow.  Rounding: |error| <= hits * max|dat| * 2^-(62-hbits) per
+ * pixel, below FP64 summation error for hmax <= 2^24.
+ * `scratch`: device, 256-byte aligned, mk_tod2map_fixed_scratch_bytes(npix)
+ * bytes, zeroed once before first use; every call leaves it zeroed again.
+ * Calls that share a scratch must be ordered on one stream. */
+size_t mk_tod2map_fixed_scratch_bytes(int64_t npix);
+int mk_tod2map_fixed(void *map, const void *dat, const int32_t *ipix, int64_t ndet,
+                     int64_t ndata, int64_t npix, int64_t hmax, int dtype, void *scratch,
+                     void *stream);
+
+/* ---- DCT-I and the SmoothedSVD noise filter --------------------------- */
+
+/* Batched unnormalised DCT-I (FFTW REDFT00) of nrow rows of length n >= 2:
+ * X_k = x_0 + (-1)^k x_{n-1} + 2 sum_{j=1}^{n-2} x_j cos(pi j k/(n-1)).
+ * Computed as a batched cuFFT real-to-complex transform of the even
+ * extension (length 2(n-1)); the real part of bins 0..n-1 is the DCT-I.
+ * `in` and `out` are (nrow, n) dtype-typed and may alias.  The plan holds a
+ * workspace of mk_dct1_workspace_bytes() bytes that the CALLER provides
+ * (device pointer, 256-byte aligned) and keeps alive while the plan is used.
+ * Replaces many_fft_r2r_1d / many_fftf_r2r_1d, minkasi/lib/mkfftw.c:174-254. */
+typedef struct mk_dct_plan mk_dct_plan;
+int mk_dct1_workspace_bytes(int64_t nrow, int64_t n, int dtype, size_t *bytes);
+int mk_dct1_plan_create(mk_dct_plan **plan, int64_t nrow, int64_t n, int dtype,
+                        void *workspace, size_t workspace_bytes);
+int mk_dct1_exec(mk_dct_plan *plan, const void *in, void *out, void *stream);
+int mk_dct1_plan_destroy(mk_dct_plan *plan);
+
+/* NoiseSmoothedSVD.apply_noise, minkasi/mapmaking/noise.py:680-714:
+ *   out = halve_ends( vT . DCT1( mywt[:, :ndata] * DCT1( v . dat ) ) )
+ * where halve_ends multiplies columns 0 and ndata-1 by 1/2.  v, vT are
+ * (ndet, ndet); mywt is (ndet, mywt_ld) with mywt_ld >= ndata (the reference
+ * slices mywt[:, :nn]); dat and out are (ndet, ndata); all dtype-typed.
+ * `out` may alias `dat`.  Prewhitening (noisevec) is folded into v and vT by
+ * the caller.  The plan shares the DCT workspace contract above and may be
+ * used for any TOD of the same (ndet, ndata).  rot_mode selects the
+ * detector-rotation GEMM: 0 = automatic, 1 = cuBLAS on the FP64 / FP32 units
+ * (DGEMM / SGEMM), 2 = this library's tensor-core kernel (FP32 only: 3xTF32
+ * split products, FP32 accumulate), 3 = cuBLAS tensor-core emulation (FP64:
+ * fixed-point slices; FP32: BF16x9). */
+typedef struct mk_noise_plan mk_noise_plan;
+int mk_noise_workspace_bytes(int64_t ndet, int64_t ndata, int dtype, size_t *bytes);
+int mk_noise_plan_create(mk_noise_plan **plan, int64_t ndet, int64_t ndata, int dtype,
+                         void *workspace, size_t workspace_bytes);
+int mk_apply_noise(mk_noise_plan *plan, const void *v, const void *vT, const void *mywt,
+                   int64_t mywt_ld, const void *dat, void *out, int rot_mode, void *stream);
+int mk_noise_plan_destroy(mk_noise_plan *plan);
+
+/* ---- map-space vector algebra and the PCG recurrence ------------------- */
+
+/* *result (DEVICE double) = sum_i a[i]*b[i], accumulated in FP64 with a
+ * fixed reduction tree (bitwise reproducible).  a, b dtype-typed.
+ * `scratch` is a device buffer of at least mk_reduce_scratch_bytes() bytes,
+ * zeroed once by the caller before first use (the kernel leaves it zeroed).
+ * Replaces SkyMap.dot (np.sum(a*b)), minkasi/maps/skymap.py:651-666. */
+size_t mk_reduce_scratch_bytes(void);
+int mk_dot(const void *a, const void *b, int64_t n, int dtype, double *result,
+           void *scratch, void *stream);
+
+/* y = y + alpha*x with host scalar alpha (SkyMap.axpy, skymap.py:428-440). */
+int mk_axpy(void *y, const void *x, double alpha, int64_t n, int dtype, void *stream);
+/* out = a * b elementwise (SkyMap.__mul__, skymap.py:724-740). */
+int mk_mul(void *out, const void *a, const void *b, int64_t n, int dtype, void *stream);
+
+/* One PCG update with every scalar kept on the device, so an iteration can
+ * be captured in a CUDA graph with no host round trip.  `s` is a device
+ * array of MK_PCG_NSCALAR doubles; on entry s[MK_S_ZR] holds z.r.
+ * Follows run_pcg_wprior, minkasi/mapmaking/pcg.py:137-171:
+ *   pAp = p.Ap; alpha = zr/pAp; x += alpha p; r += (-alpha) Ap;
+ *   z = precon*r (precon NULL: z = r); zr' = r.z; beta = zr'/zr;
+ *   p = z + beta p;  also s[MK_S_RR] = r.r.
+ * x, r, z, p, Ap, precon are dtype-typed maps of n pixels.  `scratch` as for
+ * mk_dot.  If pAp <= 0 or a scalar is non-finite, s[MK_S_FLAG] is set to 1
+ * and x, r, p are left unchanged from that point on. */
+enum { MK_S_ZR = 0, MK_S_PAP = 1, MK_S_ALPHA = 2, MK_S_ZRNEW = 3, MK_S_BETA = 4,
+       MK_S_RR = 5, MK_S_FLAG = 6, MK_S_ITER = 7, MK_PCG_NSCALAR = 8 };
+int mk_pcg_update(void *x, void *r, void *z, void *p, const void *Ap, const void *precon,
+                  int64_t n, int dtype, double *s, void *scratch, void *stream);
+
+/* PCG start: r = b - Ax; z = precon*r; p = z; s[MK_S_ZR] = r.z; s[MK_S_RR] = r.r;
+ * flag and iteration counter cleared.  pcg.py:101-121. */
+int mk_pcg_init(void *r, void *z, void *p, const void *b, const void *Ax,
+                const void *precon, int64_t n, int dtype, double *s, void *scratch,
+                void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MKGPU_H */

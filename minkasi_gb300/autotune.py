@@ -1,0 +1,134 @@
+"""Project autotuner: picks the tod2map kernel and the rotation GEMM per
+workload by timing the candidates on the actual device buffers, and caches
+the choice in a JSON file keyed on (GPU, dtype, detector counts, samples,
+map size, hit density).
+
+Cache file: $MINKASI_GB300_AUTOTUNE, else ~/.cache/minkasi_gb300/autotune.json.
+Set MINKASI_GB300_TOD2MAP=atomic|fixed|sorted (or ..._ROT=1|2|3) to force a choice.
+"""
+from __future__ import annotations
+
+import json
+import os
+from typing import Dict, Iterable, Optional
+
+import numpy as np
+import torch
+
+from . import kernels as K
+
+_MEM: Dict[str, object] = {}
+
+
+def cache_path() -> str:
+    p = os.environ.get("MINKASI_GB300_AUTOTUNE")
+    if p:
+        return p
+    return os.path.join(os.path.expanduser("~"), ".cache", "minkasi_gb300", "autotune.json")
+
+
+def _load() -> dict:
+    try:
+        with open(cache_path()) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store(key: str, value) -> None:
+    _MEM[key] = value
+    d = _load()
+    d[key] = value
+    try:
+        os.makedirs(os.path.dirname(cache_path()), exist_ok=True)
+        tmp = cache_path() + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(d, f, indent=1, sort_keys=True)
+        os.replace(tmp, cache_path())
+    except OSError:
+        pass
+
+
+def _lookup(key: str):
+    if key in _MEM:
+        return _MEM[key]
+    return _load().get(key)
+
+
+def workload_key(op, what: str) -> str:
+    ndets = sorted(set(d[0] for d in op.dims))
+    hits = op.hits()
+    density = float((hits > 0).double().mean().item())
+    gpu = torch.cuda.get_device_name(op.device)
+    return (f"{what}|{gpu}|{str(op.dtype).split('.')[-1]}|ndet={ndets}|S={op.S}|npix={op.npix}"
+            f"|density={density:.3f}")
+
+
+def time_ms(fn, reps: int = 3, warm: int = 1) -> float:
+    for _ in range(warm):
+        fn()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = float("inf")
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        e0.record()
+        fn()
+        e1.record()
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return best
+
+
+def choose_tod2map(op, candidates: Optional[Iterable[str]] = None) -> str:
+    forced = os.environ.get("MINKASI_GB300_TOD2MAP")
+    if forced:
+        return forced
+    if candidates is None:
+        candidates = ["atomic", "fixed"]
+        if op.S < (1 << 30) and max(op.sizes) < (1 << 31):
+            candidates.append("sorted")  # plan memory 4 B/sample
+    key = workload_key(op, "tod2map")
+    hit = _lookup(key)
+    if hit in candidates:
+        return hit
+    op.tmp.normal_()
+    out = torch.zeros(op.npix, dtype=op.dtype, device=op.device)
+    times = {m: time_ms(lambda m=m: op.project_out(out, m)) for m in candidates}
+    best = min(times, key=times.get)
+    if best != "sorted":
+        op._pixplans = None
+    _store(key, best)
+    return best
+
+
+def choose_rot_mode(op) -> int:
+    """Fastest rotation GEMM that agrees with the FP64/FP32 cuBLAS result
+    (rel. 1e-13 in FP64, 1e-6 in FP32) on the largest TOD shape."""
+    forced = os.environ.get("MINKASI_GB300_ROT")
+    if forced:
+        return int(forced)
+    key = workload_key(op, "rot")
+    hit = _lookup(key)
+    if hit is not None:
+        return int(hit)
+    i = int(np.argmax(op.sizes))
+    nd, n = op.dims[i]
+    v, vT, w = op.ops[i]
+    plan = op.plans[(nd, n)]
+    x = torch.randn((nd, n), dtype=op.dtype, device=op.device)
+    ref = plan.apply(v, vT, w, x, rot_mode=1)
+    tol = 1e-13 if op.dtype == torch.float64 else 1e-6
+    modes = [1, 3] + ([2] if op.dtype == torch.float32 else [])
+    times = {}
+    for m in modes:
+        try:
+            y = plan.apply(v, vT, w, x, rot_mode=m)
+        except K._lib.MkError:
+            continue
+        err = float((y - ref).abs().max() / ref.abs().max())
+        if err > tol:
+            continue
+        times[m] = time_ms(lambda m=m: plan.apply(v, vT, w, x, rot_mode=m))
+    best = min(times, key=times.get)
+    _store(key, best)
+    return best

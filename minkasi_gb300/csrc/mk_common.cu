@@ -1,0 +1,44 @@
+// Status strings, device properties and the library version.
+#include <stdarg.h>
+#include <string.h>
+
+#include "mk_common.cuh"
+
+namespace mk {
+
+static thread_local char g_err[512] = "no error";
+
+void set_error(const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+int sm_count() {
+  static int cached[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+  if (cached[dev] == 0) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+      n = 152;
+    cached[dev] = n;
+  }
+  return cached[dev];
+}
+
+int launch_status(const char *what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("%s: kernel launch failed: %s", what, cudaGetErrorString(e));
+    return MK_ERR_CUDA;
+  }
+  return MK_OK;
+}
+
+}  // namespace mk
+
+extern "C" const char *mk_last_error(void) { return mk::g_err; }
+
+extern "C" int mk_version(void) { return 1; }

@@ -1,0 +1,395 @@
+// DCT-I (FFTW REDFT00) and the NoiseSmoothedSVD filter on the GPU.
+//
+// DCT-I of a row x of length n equals the real part of the DFT of its even
+// extension y (length N = 2(n-1)):  y_j = x_j (0 <= j < n),
+// y_{N-j} = x_j (1 <= j <= n-2);  X_k = Re Y_k, k = 0..n-1.
+// So every DCT here is: hand-written extension kernel -> batched cuFFT
+// real-to-complex transform of length N -> hand-written kernel that takes the
+// real part and applies whatever comes next (the inverse-spectrum weights
+// and the next extension, or the endpoint halving).
+//
+// apply_noise (minkasi/mapmaking/noise.py:680-714) for one TOD:
+//   E[:, :n]  = v . dat                         (GEMM, written with ld N)
+//   E[:, n:]  = mirror                          (k_mirror)
+//   F         = R2C(E)                          (cuFFT)
+//   E         = extend(Re F * mywt)             (k_filter_extend)
+//   F         = R2C(E)                          (cuFFT)
+//   G         = Re F, columns 0 and n-1 halved  (k_real_halve; G aliases E)
+//   out       = vT . G                          (GEMM)
+// Halving before the second rotation equals halving after it (a column
+// scale commutes with a left multiplication).
+#include <cublas_v2.h>
+#include <cufft.h>
+
+#include <mutex>
+#include <new>
+
+#include "mk_common.cuh"
+#include "mk_rot.cuh"
+
+namespace {
+
+constexpr size_t ALIGN = 256;
+inline size_t align_up(size_t x) { return (x + ALIGN - 1) / ALIGN * ALIGN; }
+
+const char *cufft_str(cufftResult r) {
+  switch (r) {
+    case CUFFT_SUCCESS: return "CUFFT_SUCCESS";
+    case CUFFT_INVALID_PLAN: return "CUFFT_INVALID_PLAN";
+    case CUFFT_ALLOC_FAILED: return "CUFFT_ALLOC_FAILED";
+    case CUFFT_INVALID_VALUE: return "CUFFT_INVALID_VALUE";
+    case CUFFT_INTERNAL_ERROR: return "CUFFT_INTERNAL_ERROR";
+    case CUFFT_EXEC_FAILED: return "CUFFT_EXEC_FAILED";
+    case CUFFT_SETUP_FAILED: return "CUFFT_SETUP_FAILED";
+    case CUFFT_INVALID_SIZE: return "CUFFT_INVALID_SIZE";
+    default: return "cuFFT error";
+  }
+}
+
+#define MK_CUFFT(call)                                                              \
+  do {                                                                              \
+    cufftResult _r = (call);                                                        \
+    if (_r != CUFFT_SUCCESS) {                                                      \
+      mk::set_error("%s failed: %s (%d)", #call, cufft_str(_r), (int)_r);          \
+      return MK_ERR_CUFFT;                                                          \
+    }                                                                               \
+  } while (0)
+
+// ---- elementwise kernels (grid: x over columns, y over rows) --------------
+template <typename T>
+__global__ void k_extend(const T *__restrict__ in, int64_t ld_in, T *__restrict__ E, int64_t n,
+                         int64_t N, int64_t nrow) {
+  for (int64_t r = blockIdx.y; r < nrow; r += gridDim.y) {
+    const T *src = in + r * ld_in;
+    T *dst = E + r * N;
+    for (int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j < n;
+         j += (int64_t)gridDim.x * blockDim.x) {
+      T v = src[j];
+      dst[j] = v;
+      if (j >= 1 && j <= n - 2) dst[N - j] = v;
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_mirror(T *__restrict__ E, int64_t n, int64_t N, int64_t nrow) {
+  for (int64_t r = blockIdx.y; r < nrow; r += gridDim.y) {
+    T *row = E + r * N;
+    for (int64_t j = 1 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j <= n - 2;
+         j += (int64_t)gridDim.x * blockDim.x)
+      row[N - j] = row[j];
+  }
+}
+
+template <typename T, typename C>
+__global__ void k_real(const C *__restrict__ F, T *__restrict__ out, int64_t n, int64_t nrow) {
+  for (int64_t r = blockIdx.y; r < nrow; r += gridDim.y)
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x)
+      out[r * n + k] = F[r * n + k].x;
+}
+
+template <typename T, typename C>
+__global__ void k_filter_extend(const C *__restrict__ F, const T *__restrict__ w, int64_t ldw,
+                                T *__restrict__ E, int64_t n, int64_t N, int64_t nrow) {
+  for (int64_t r = blockIdx.y; r < nrow; r += gridDim.y) {
+    const C *f = F + r * n;
+    const T *wr = w + r * ldw;
+    T *dst = E + r * N;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+      T v = f[k].x * __ldcs(wr + k);
+      dst[k] = v;
+      if (k >= 1 && k <= n - 2) dst[N - k] = v;
+    }
+  }
+}
+
+template <typename T, typename C>
+__global__ void k_real_halve(const C *__restrict__ F, T *__restrict__ G, int64_t n, int64_t nrow) {
+  for (int64_t r = blockIdx.y; r < nrow; r += gridDim.y)
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
+      T v = F[r * n + k].x;
+      if (k == 0 || k == n - 1) v *= T(0.5);
+      G[r * n + k] = v;
+    }
+}
+
+dim3 rows_grid(int64_t n, int64_t nrow) {
+  // enough CTAs along the row to fill the GPU several times over
+  int64_t total = (int64_t)mk::sm_count() * 16;
+  int64_t gy = nrow < 65535 ? nrow : 65535;
+  int64_t gx = (total + gy - 1) / gy;
+  int64_t need = (n + 255) / 256;
+  if (gx > need) gx = need;
+  if (gx < 1) gx = 1;
+  return dim3((unsigned)gx, (unsigned)gy, 1);
+}
+
+// ---- plan object -----------------------------------------------------------
+struct DctCore {
+  cufftHandle fft = 0;
+  bool have_fft = false;
+  int64_t nrow = 0, n = 0, N = 0;
+  int dtype = MK_F64;
+  void *E = nullptr, *F = nullptr, *work = nullptr;
+  size_t work_bytes = 0;
+};
+
+size_t elt(int dtype) { return dtype == MK_F64 ? 8 : 4; }
+
+int make_fft(cufftHandle *h, int64_t nrow, int64_t N, int dtype, size_t *work) {
+  MK_CUFFT(cufftCreate(h));
+  cufftResult r = cufftSetAutoAllocation(*h, 0);
+  long long nn[1] = {(long long)N};
+  long long inembed[1] = {(long long)N};
+  long long onembed[1] = {(long long)(N / 2 + 1)};
+  if (r == CUFFT_SUCCESS)
+    r = cufftMakePlanMany64(*h, 1, nn, inembed, 1, (long long)N, onembed, 1, (long long)(N / 2 + 1),
+                            dtype == MK_F64 ? CUFFT_D2Z : CUFFT_R2C, (long long)nrow, work);
+  if (r != CUFFT_SUCCESS) {
+    cufftDestroy(*h);
+    mk::set_error("cufftMakePlanMany64(N=%lld, batch=%lld) failed: %s", (long long)N,
+                  (long long)nrow, cufft_str(r));
+    return MK_ERR_CUFFT;
+  }
+  return MK_OK;
+}
+
+int core_bytes(int64_t nrow, int64_t n, int dtype, size_t *bytes) {
+  MK_CHECK_ARG(bytes, "workspace size: null output");
+  MK_CHECK_ARG(MK_DTYPE_OK(dtype), "workspace size: bad dtype %d", dtype);
+  MK_CHECK_ARG(nrow >= 1 && n >= 2, "DCT-I needs nrow >= 1 and n >= 2 (got %lld, %lld)",
+               (long long)nrow, (long long)n);
+  int64_t N = 2 * (n - 1);
+  cufftHandle h;
+  size_t work = 0;
+  int rc = make_fft(&h, nrow, N, dtype, &work);
+  if (rc) return rc;
+  cufftDestroy(h);
+  *bytes = align_up((size_t)nrow * N * elt(dtype)) + align_up((size_t)nrow * n * 2 * elt(dtype)) +
+           align_up(work);
+  return MK_OK;
+}
+
+int core_create(DctCore *c, int64_t nrow, int64_t n, int dtype, void *ws, size_t ws_bytes) {
+  size_t need = 0;
+  int rc = core_bytes(nrow, n, dtype, &need);
+  if (rc) return rc;
+  MK_CHECK_ARG(ws && ((uintptr_t)ws % ALIGN) == 0, "workspace must be a 256-byte aligned device pointer");
+  MK_CHECK_ARG(ws_bytes >= need, "workspace too small: %zu < %zu bytes", ws_bytes, need);
+  c->nrow = nrow;
+  c->n = n;
+  c->N = 2 * (n - 1);
+  c->dtype = dtype;
+  char *p = (char *)ws;
+  c->E = p;
+  p += align_up((size_t)nrow * c->N * elt(dtype));
+  c->F = p;
+  p += align_up((size_t)nrow * n * 2 * elt(dtype));
+  c->work = p;
+  rc = make_fft(&c->fft, nrow, c->N, dtype, &c->work_bytes);
+  if (rc) return rc;
+  c->have_fft = true;
+  cufftResult r = cufftSetWorkArea(c->fft, c->work);
+  if (r != CUFFT_SUCCESS) {
+    cufftDestroy(c->fft);
+    c->have_fft = false;
+    mk::set_error("cufftSetWorkArea failed: %s", cufft_str(r));
+    return MK_ERR_CUFFT;
+  }
+  return MK_OK;
+}
+
+int core_fft(DctCore *c, cudaStream_t st) {
+  MK_CUFFT(cufftSetStream(c->fft, st));
+  if (c->dtype == MK_F64)
+    MK_CUFFT(cufftExecD2Z(c->fft, (cufftDoubleReal *)c->E, (cufftDoubleComplex *)c->F));
+  else
+    MK_CUFFT(cufftExecR2C(c->fft, (cufftReal *)c->E, (cufftComplex *)c->F));
+  return MK_OK;
+}
+
+template <typename T, typename C>
+int dct_exec_t(DctCore *c, const void *in, void *out, cudaStream_t st) {
+  dim3 g = rows_grid(c->n, c->nrow);
+  k_extend<T><<<g, 256, 0, st>>>((const T *)in, c->n, (T *)c->E, c->n, c->N, c->nrow);
+  int rc = mk::launch_status("mk_dct1_exec/extend");
+  if (rc) return rc;
+  if ((rc = core_fft(c, st))) return rc;
+  k_real<T, C><<<g, 256, 0, st>>>((const C *)c->F, (T *)out, c->n, c->nrow);
+  return mk::launch_status("mk_dct1_exec/real");
+}
+
+// ---- cuBLAS handle (one per device, shared; calls serialised) -------------
+std::mutex g_blas_mu;
+cublasHandle_t g_blas[64] = {};
+void *g_blas_ws[64] = {};
+
+int blas_handle(cublasHandle_t *out) {
+  int dev = 0;
+  MK_CUDA(cudaGetDevice(&dev));
+  MK_CHECK_ARG(dev >= 0 && dev < 64, "device ordinal %d out of range", dev);
+  if (!g_blas[dev]) {
+    cublasHandle_t h;
+    if (cublasCreate(&h) != CUBLAS_STATUS_SUCCESS) {
+      mk::set_error("cublasCreate failed");
+      return MK_ERR_CUBLAS;
+    }
+    // fixed workspace, so GEMMs inside a captured CUDA graph allocate nothing
+    const size_t ws = 32u << 20;
+    MK_CUDA(cudaMalloc(&g_blas_ws[dev], ws));
+    cublasSetWorkspace(h, g_blas_ws[dev], ws);
+    cublasSetMathMode(h, CUBLAS_DEFAULT_MATH);
+    g_blas[dev] = h;
+  }
+  *out = g_blas[dev];
+  return MK_OK;
+}
+
+// R (nrow x ncol, ld ldr) = A (nrow x nrow) . X (nrow x ncol, ld ldx), all row-major.
+// Column-major view: R^T = X^T A^T, i.e. gemm(N, N, m=ncol, n=nrow, k=nrow).
+// emulate: 0 = native FP64 / FP32 units; 1 = cuBLAS tensor-core emulation
+// (FP64: fixed-point slices, FP32: BF16x9).
+int blas_rotate(int dtype, const void *A, const void *X, int64_t ldx, void *R, int64_t ldr,
+                int64_t nrow, int64_t ncol, int emulate, cudaStream_t st) {
+  std::lock_guard<std::mutex> lk(g_blas_mu);
+  cublasHandle_t h;
+  int rc = blas_handle(&h);
+  if (rc) return rc;
+  cublasSetStream(h, st);
+  cublasMath_t mode = CUBLAS_DEFAULT_MATH;
+  if (emulate) mode = dtype == MK_F64 ? CUBLAS_FP64_EMULATED_FIXEDPOINT_MATH : CUBLAS_FP32_EMULATED_BF16X9_MATH;
+  cublasSetMathMode(h, mode);
+  cublasSetEmulationStrategy(h, emulate ? CUBLAS_EMULATION_STRATEGY_EAGER : CUBLAS_EMULATION_STRATEGY_DEFAULT);
+  cublasStatus_t s;
+  if (dtype == MK_F64) {
+    const double one = 1.0, zero = 0.0;
+    s = cublasDgemm_64(h, CUBLAS_OP_N, CUBLAS_OP_N, ncol, nrow, nrow, &one, (const double *)X, ldx,
+                       (const double *)A, nrow, &zero, (double *)R, ldr);
+  } else {
+    const float one = 1.f, zero = 0.f;
+    s = cublasSgemm_64(h, CUBLAS_OP_N, CUBLAS_OP_N, ncol, nrow, nrow, &one, (const float *)X, ldx,
+                       (const float *)A, nrow, &zero, (float *)R, ldr);
+  }
+  if (s != CUBLAS_STATUS_SUCCESS) {
+    mk::set_error("cuBLAS gemm failed (status %d)", (int)s);
+    return MK_ERR_CUBLAS;
+  }
+  return MK_OK;
+}
+
+int rotate(int dtype, int mode, const void *A, const void *X, int64_t ldx, void *R, int64_t ldr,
+           int64_t nrow, int64_t ncol, cudaStream_t st) {
+  if (mode == 0) mode = (dtype == MK_F32 && mk::rot_tc_supported(nrow)) ? 2 : 1;
+  if (mode == 2) {
+    MK_CHECK_ARG(dtype == MK_F32, "tensor-core rotation (rot_mode 2) is FP32 only");
+    return mk::rot_tc_f32((const float *)A, (const float *)X, ldx, (float *)R, ldr, nrow, ncol, st);
+  }
+  MK_CHECK_ARG(mode == 1 || mode == 3, "bad rot_mode %d", mode);
+  return blas_rotate(dtype, A, X, ldx, R, ldr, nrow, ncol, mode == 3, st);
+}
+
+template <typename T, typename C>
+int apply_noise_t(DctCore *c, const T *v, const T *vT, const T *w, int64_t ldw, const T *dat,
+                  T *out, int rot_mode, cudaStream_t st) {
+  const int64_t n = c->n, N = c->N, nd = c->nrow;
+  dim3 g = rows_grid(n, nd);
+  int rc = rotate(c->dtype, rot_mode, v, dat, n, c->E, N, nd, n, st);
+  if (rc) return rc;
+  k_mirror<T><<<g, 256, 0, st>>>((T *)c->E, n, N, nd);
+  if ((rc = mk::launch_status("apply_noise/mirror"))) return rc;
+  if ((rc = core_fft(c, st))) return rc;
+  k_filter_extend<T, C><<<g, 256, 0, st>>>((const C *)c->F, w, ldw, (T *)c->E, n, N, nd);
+  if ((rc = mk::launch_status("apply_noise/filter"))) return rc;
+  if ((rc = core_fft(c, st))) return rc;
+  k_real_halve<T, C><<<g, 256, 0, st>>>((const C *)c->F, (T *)c->E, n, nd);
+  if ((rc = mk::launch_status("apply_noise/halve"))) return rc;
+  return rotate(c->dtype, rot_mode, vT, c->E, n, out, n, nd, n, st);
+}
+
+}  // namespace
+
+struct mk_dct_plan {
+  DctCore core;
+};
+struct mk_noise_plan {
+  DctCore core;
+};
+
+extern "C" int mk_dct1_workspace_bytes(int64_t nrow, int64_t n, int dtype, size_t *bytes) {
+  return core_bytes(nrow, n, dtype, bytes);
+}
+
+extern "C" int mk_dct1_plan_create(mk_dct_plan **plan, int64_t nrow, int64_t n, int dtype,
+                                   void *workspace, size_t workspace_bytes) {
+  MK_CHECK_ARG(plan, "mk_dct1_plan_create: null plan pointer");
+  *plan = nullptr;
+  mk_dct_plan *p = new (std::nothrow) mk_dct_plan;
+  if (!p) return MK_ERR_NOMEM;
+  int rc = core_create(&p->core, nrow, n, dtype, workspace, workspace_bytes);
+  if (rc) {
+    delete p;
+    return rc;
+  }
+  *plan = p;
+  return MK_OK;
+}
+
+extern "C" int mk_dct1_exec(mk_dct_plan *plan, const void *in, void *out, void *stream) {
+  MK_CHECK_ARG(plan && in && out, "mk_dct1_exec: null pointer");
+  cudaStream_t st = mk::as_stream(stream);
+  return plan->core.dtype == MK_F64 ? dct_exec_t<double, cufftDoubleComplex>(&plan->core, in, out, st)
+                                    : dct_exec_t<float, cufftComplex>(&plan->core, in, out, st);
+}
+
+extern "C" int mk_dct1_plan_destroy(mk_dct_plan *plan) {
+  if (!plan) return MK_OK;
+  if (plan->core.have_fft) cufftDestroy(plan->core.fft);
+  delete plan;
+  return MK_OK;
+}
+
+extern "C" int mk_noise_workspace_bytes(int64_t ndet, int64_t ndata, int dtype, size_t *bytes) {
+  return core_bytes(ndet, ndata, dtype, bytes);
+}
+
+extern "C" int mk_noise_plan_create(mk_noise_plan **plan, int64_t ndet, int64_t ndata, int dtype,
+                                    void *workspace, size_t workspace_bytes) {
+  MK_CHECK_ARG(plan, "mk_noise_plan_create: null plan pointer");
+  *plan = nullptr;
+  mk_noise_plan *p = new (std::nothrow) mk_noise_plan;
+  if (!p) return MK_ERR_NOMEM;
+  int rc = core_create(&p->core, ndet, ndata, dtype, workspace, workspace_bytes);
+  if (rc) {
+    delete p;
+    return rc;
+  }
+  *plan = p;
+  return MK_OK;
+}
+
+extern "C" int mk_apply_noise(mk_noise_plan *plan, const void *v, const void *vT, const void *mywt,
+                              int64_t mywt_ld, const void *dat, void *out, int rot_mode,
+                              void *stream) {
+  MK_CHECK_ARG(plan && v && vT && mywt && dat && out, "mk_apply_noise: null pointer");
+  MK_CHECK_ARG(mywt_ld >= plan->core.n, "mk_apply_noise: mywt_ld %lld < ndata %lld",
+               (long long)mywt_ld, (long long)plan->core.n);
+  cudaStream_t st = mk::as_stream(stream);
+  if (plan->core.dtype == MK_F64)
+    return apply_noise_t<double, cufftDoubleComplex>(&plan->core, (const double *)v,
+                                                     (const double *)vT, (const double *)mywt,
+                                                     mywt_ld, (const double *)dat, (double *)out,
+                                                     rot_mode, st);
+  return apply_noise_t<float, cufftComplex>(&plan->core, (const float *)v, (const float *)vT,
+                                            (const float *)mywt, mywt_ld, (const float *)dat,
+                                            (float *)out, rot_mode, st);
+}
+
+extern "C" int mk_noise_plan_destroy(mk_noise_plan *plan) {
+  if (!plan) return MK_OK;
+  if (plan->core.have_fft) cufftDestroy(plan->core.fft);
+  delete plan;
+  return MK_OK;
+}

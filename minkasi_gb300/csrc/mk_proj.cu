@@ -1,0 +1,511 @@
+// Pointing projections: map2tod (gather) and tod2map (scatter-add).
+//
+//   map2tod  dat[i] (+)= map[ipix[i]]  -- minkasi/lib/minkasi.c:116-144
+//   tod2map  map[ipix[i]] += dat[i]    -- minkasi/lib/minkasi.c:50-112
+//
+// Both are HBM-bound streams over the TOD: per sample 4 B of ipix plus one
+// dat element read or written.  The map (<= 2048^2 doubles = 32 MB) stays
+// resident in the 129 MB L2, so the map side costs L2 bandwidth, not HBM.
+// Streams are read and written with evict-first hints (ld.global.cs /
+// st.global.cs) so they do not push the map out of L2.
+#include <cub/device/device_radix_sort.cuh>
+
+#include "mk_common.cuh"
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+template <typename T>
+__device__ __forceinline__ T gather(const T *__restrict__ map, int32_t p, int64_t npix) {
+  return ((uint32_t)p < (uint64_t)npix) ? __ldg(map + p) : T(0);
+}
+
+// ---- map2tod --------------------------------------------------------------
+// Vector body: each thread moves 4 consecutive samples (one 16-byte ipix
+// load, 16/32-byte dat accesses).  Requires ipix and dat 16-byte aligned;
+// the host peels nothing -- it falls back to the scalar kernel otherwise.
+template <typename T, bool ADD>
+__global__ void __launch_bounds__(256) k_map2tod_vec(T *__restrict__ dat, const T *__restrict__ map,
+                                                     const int32_t *__restrict__ ipix, int64_t n,
+                                                     int64_t npix) {
+  const int64_t n4 = n >> 2;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int4 *ip4 = reinterpret_cast<const int4 *>(ipix);
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n4; g += stride) {
+    int4 p = __ldcs(ip4 + g);
+    T v0 = gather(map, p.x, npix), v1 = gather(map, p.y, npix);
+    T v2 = gather(map, p.z, npix), v3 = gather(map, p.w, npix);
+    if constexpr (sizeof(T) == 8) {
+      double2 *d2 = reinterpret_cast<double2 *>(dat) + 2 * g;
+      if (ADD) {
+        double2 a = __ldcs(d2), b = __ldcs(d2 + 1);
+        v0 += a.x; v1 += a.y; v2 += b.x; v3 += b.y;
+      }
+      __stcs(d2, make_double2(v0, v1));
+      __stcs(d2 + 1, make_double2(v2, v3));
+    } else {
+      float4 *d4 = reinterpret_cast<float4 *>(dat) + g;
+      if (ADD) {
+        float4 a = __ldcs(d4);
+        v0 += a.x; v1 += a.y; v2 += a.z; v3 += a.w;
+      }
+      __stcs(d4, make_float4(v0, v1, v2, v3));
+    }
+  }
+  // tail (n % 4 samples), handled by the first threads of block 0
+  if (blockIdx.x == 0 && threadIdx.x < (n & 3)) {
+    int64_t i = (n4 << 2) + threadIdx.x;
+    T v = gather(map, ipix[i], npix);
+    dat[i] = ADD ? dat[i] + v : v;
+  }
+}
+
+template <typename T, bool ADD>
+__global__ void __launch_bounds__(256) k_map2tod_scalar(T *__restrict__ dat, const T *__restrict__ map,
+                                                        const int32_t *__restrict__ ipix, int64_t n,
+                                                        int64_t npix) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    T v = gather(map, ipix[i], npix);
+    dat[i] = ADD ? dat[i] + v : v;
+  }
+}
+
+// ---- tod2map: warp-aggregated atomics -------------------------------------
+// A warp reads 32 consecutive samples (coalesced).  Consecutive samples of a
+// scanning detector often fall in the same pixel, so runs of equal pixel
+// index are summed with a segmented shuffle scan and only the last lane of
+// each run issues the (L2) atomic add.
+template <typename T>
+__device__ __forceinline__ void warp_run_add(T *__restrict__ map, int32_t key, T val, int lane,
+                                             int64_t npix) {
+  int32_t prev = __shfl_up_sync(FULL, key, 1);
+  bool head = (lane == 0) || (prev != key);
+  unsigned heads = __ballot_sync(FULL, head);
+  unsigned upto = heads & (FULL >> (31 - lane));  // run heads at lanes <= mine
+  int start = 31 - __clz(upto);
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    T up = __shfl_up_sync(FULL, val, off);
+    if (lane - off >= start) val += up;
+  }
+  bool tail = (lane == 31) ? true : (((heads >> (lane + 1)) & 1u) != 0u);
+  if (tail && (uint32_t)key < (uint64_t)npix) atomicAdd(map + key, val);
+}
+
+// ROWS: the value of sample i is rowval[i / ndata] (1 if rowval is NULL);
+// used for hit maps, where no TOD-sized array of ones is materialised.
+template <typename T, bool ROWS, int U>
+__global__ void __launch_bounds__(256) k_tod2map_atomic(T *__restrict__ map, const T *__restrict__ dat,
+                                                        const int32_t *__restrict__ ipix, int64_t n,
+                                                        int64_t npix, const T *__restrict__ rowval,
+                                                        int64_t ndata) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t base = warp * (32 * U); base < n; base += nwarp * (32 * U)) {
+    int32_t p[U];
+    T v[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      int64_t i = base + u * 32 + lane;
+      if (i < n) {
+        p[u] = __ldcs(ipix + i);
+        if (ROWS)
+          v[u] = rowval ? rowval[i / ndata] : T(1);
+        else
+          v[u] = __ldcs(dat + i);
+      } else {
+        p[u] = -1;
+        v[u] = T(0);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) warp_run_add(map, p[u], v[u], lane, npix);
+  }
+}
+
+__global__ void k_count_bad(const int32_t *__restrict__ ipix, int64_t n, int64_t npix,
+                            unsigned long long *nbad) {
+  unsigned long long mine = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+    mine += ((uint32_t)ipix[i] >= (uint64_t)npix) ? 1ull : 0ull;
+  for (int off = 16; off > 0; off >>= 1) mine += __shfl_xor_sync(FULL, mine, off);
+  if ((threadIdx.x & 31) == 0 && mine) atomicAdd(nbad, mine);
+}
+
+// ---- deterministic tod2map via a pixel plan --------------------------------
+__global__ void k_iota(int32_t *v, int64_t n) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) v[i] = (int32_t)i;
+}
+
+// offsets[p] = first position in the sorted key list with key >= p, p in [0, npix]
+__global__ void k_pix_offsets(const int32_t *__restrict__ keys, int64_t n, int32_t *__restrict__ off,
+                              int64_t npix) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p <= npix; p += stride) {
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+      int64_t mid = (lo + hi) >> 1;
+      if ((int64_t)keys[mid] < p) lo = mid + 1; else hi = mid;
+    }
+    off[p] = (int32_t)lo;
+  }
+}
+
+// One warp per pixel: lane l sums the pixel's samples l, l+32, ... in sample
+// order, then a fixed xor tree combines the lanes -> reproducible bits.
+template <typename T>
+__global__ void __launch_bounds__(256) k_tod2map_sorted(T *__restrict__ map, const T *__restrict__ dat,
+                                                        const int32_t *__restrict__ perm,
+                                                        const int32_t *__restrict__ off, int64_t npix) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t p = warp; p < npix; p += nwarp) {
+    int32_t b = off[p], e = off[p + 1];
+    if (b == e) continue;
+    T acc = T(0);
+    for (int32_t j = b + lane; j < e; j += 32) acc += __ldg(dat + __ldg(perm + j));
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) acc += __shfl_xor_sync(FULL, acc, s);
+    if (lane == 0) map[p] += acc;
+  }
+}
+
+// ---- deterministic tod2map by 64-bit fixed-point accumulation ------------
+// Integer addition is associative, so the accumulated map is bitwise the
+// same whatever order the atomics land in.  Scale: with D = max|dat| < 2^(e+1)
+// and every pixel hit at most hmax <= 2^hbits times, each term
+// llrint(dat * 2^s) is below 2^(e+1+s) and a pixel's sum below
+// 2^(e+1+s+hbits) = 2^62 for s = 61 - e - hbits.
+// Header words of the scratch: [0] max|dat| as the bits of a non-negative
+// double (atomicMax on the bit pattern orders like the value; NaN sorts
+// above +inf), [1] the shift s chosen by the scatter pass.
+struct FixHdr {
+  unsigned long long dmax_bits;
+  long long shift;
+  unsigned long long pad[30];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_absmax(const T *__restrict__ dat, int64_t n, FixHdr *h) {
+  double m = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    double a = fabs((double)__ldcs(dat + i));
+    m = (a > m || a != a) ? a : m;
+  }
+  unsigned long long b = __double_as_longlong(m);
+  for (int off = 16; off > 0; off >>= 1) {
+    unsigned long long o = __shfl_xor_sync(FULL, b, off);
+    b = o > b ? o : b;
+  }
+  __shared__ unsigned long long sh[8];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = b;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) b = sh[w] > b ? sh[w] : b;
+    b = sh[0] > b ? sh[0] : b;
+    atomicMax(&h->dmax_bits, b);
+  }
+}
+
+__device__ __forceinline__ void warp_run_add_i64(unsigned long long *__restrict__ acc, int32_t key,
+                                                 long long val, int lane, int64_t npix) {
+  int32_t prev = __shfl_up_sync(FULL, key, 1);
+  bool head = (lane == 0) || (prev != key);
+  unsigned heads = __ballot_sync(FULL, head);
+  unsigned upto = heads & (FULL >> (31 - lane));
+  int start = 31 - __clz(upto);
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    long long up = __shfl_up_sync(FULL, val, off);
+    if (lane - off >= start) val += up;
+  }
+  bool tail = (lane == 31) ? true : (((heads >> (lane + 1)) & 1u) != 0u);
+  if (tail && val != 0 && (uint32_t)key < (uint64_t)npix) atomicAdd(acc + key, (unsigned long long)val);
+}
+
+template <typename T, int U>
+__global__ void __launch_bounds__(256) k_scatter_fixed(unsigned long long *__restrict__ acc, const T *__restrict__ dat,
+                                                       const int32_t *__restrict__ ipix, int64_t n,
+                                                       int64_t npix, int hbits, FixHdr *h) {
+  const double dmax = __longlong_as_double((long long)h->dmax_bits);
+  if (!(dmax > 0.0) || !isfinite(dmax)) return;  // nothing to add, or non-finite data
+  const int e = ilogb(dmax);
+  const int s = 61 - e - hbits;
+  const double scale = ldexp(1.0, s);
+  if (blockIdx.x == 0 && threadIdx.x == 0) h->shift = s;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t base = warp * (32 * U); base < n; base += nwarp * (32 * U)) {
+    int32_t p[U];
+    long long v[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      int64_t i = base + u * 32 + lane;
+      if (i < n) {
+        p[u] = __ldcs(ipix + i);
+        v[u] = __double2ll_rn((double)__ldcs(dat + i) * scale);
+      } else {
+        p[u] = -1;
+        v[u] = 0;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) warp_run_add_i64(acc, p[u], v[u], lane, npix);
+  }
+}
+
+// map += acc * 2^-s, acc cleared; non-finite data poisons the touched map with NaN.
+template <typename T>
+__global__ void k_fixed_finalize(T *__restrict__ map, unsigned long long *__restrict__ acc, int64_t npix,
+                                 FixHdr *h, int64_t nsamp) {
+  const double dmax = __longlong_as_double((long long)h->dmax_bits);
+  const bool bad = !isfinite(dmax);
+  const double inv = ldexp(1.0, -(int)h->shift);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += stride) {
+    long long a = (long long)acc[p];
+    if (a != 0) {
+      map[p] = (T)((double)map[p] + (double)a * inv);
+      acc[p] = 0ull;
+    }
+    if (bad && p == 0) map[0] = (T)NAN;
+  }
+}
+
+template <typename T>
+__global__ void k_fixed_reset(FixHdr *h) {
+  h->dmax_bits = 0ull;
+}
+
+template <typename T>
+int map2tod_t(void *dat, const void *map, const int32_t *ipix, int64_t n, int64_t npix, int do_add,
+              cudaStream_t st) {
+  bool vec = ((uintptr_t)dat % 16 == 0) && ((uintptr_t)ipix % 16 == 0) && n >= 4;
+  const int B = 256;
+  if (vec) {
+    unsigned g = mk_grid((n >> 2), B, 8);
+    if (do_add)
+      k_map2tod_vec<T, true><<<g, B, 0, st>>>((T *)dat, (const T *)map, ipix, n, npix);
+    else
+      k_map2tod_vec<T, false><<<g, B, 0, st>>>((T *)dat, (const T *)map, ipix, n, npix);
+  } else {
+    unsigned g = mk_grid(n, B, 8);
+    if (do_add)
+      k_map2tod_scalar<T, true><<<g, B, 0, st>>>((T *)dat, (const T *)map, ipix, n, npix);
+    else
+      k_map2tod_scalar<T, false><<<g, B, 0, st>>>((T *)dat, (const T *)map, ipix, n, npix);
+  }
+  return mk::launch_status("mk_map2tod");
+}
+
+template <typename T, bool ROWS>
+int tod2map_t(void *map, const void *dat, const int32_t *ipix, int64_t n, int64_t npix,
+              const void *rowval, int64_t ndata, cudaStream_t st) {
+  constexpr int U = 4;
+  const int B = 256;
+  unsigned g = mk_grid((n + U - 1) / U, B, 8);
+  k_tod2map_atomic<T, ROWS, U><<<g, B, 0, st>>>((T *)map, (const T *)dat, ipix, n, npix,
+                                                 (const T *)rowval, ndata);
+  return mk::launch_status("mk_tod2map");
+}
+
+template <typename T>
+int tod2map_fixed_t(void *map, const void *dat, const int32_t *ipix, int64_t n, int64_t npix,
+                    int hbits, void *scratch, cudaStream_t st) {
+  FixHdr *h = (FixHdr *)scratch;
+  unsigned long long *acc = (unsigned long long *)((char *)scratch + sizeof(FixHdr));
+  k_absmax<T><<<mk_grid(n, 256, 4), 256, 0, st>>>((const T *)dat, n, h);
+  constexpr int U = 4;
+  k_scatter_fixed<T, U><<<mk_grid((n + U - 1) / U, 256, 8), 256, 0, st>>>(acc, (const T *)dat, ipix, n,
+                                                                          npix, hbits, h);
+  k_fixed_finalize<T><<<mk_grid(npix, 256, 8), 256, 0, st>>>((T *)map, acc, npix, h, n);
+  k_fixed_reset<T><<<1, 1, 0, st>>>(h);
+  return mk::launch_status("mk_tod2map_fixed");
+}
+
+}  // namespace
+
+struct mk_pixplan {
+  int32_t *perm = nullptr;   // sample indices sorted by pixel (stable)
+  int32_t *off = nullptr;    // npix+1 offsets into perm
+  int64_t n = 0, npix = 0;
+};
+
+extern "C" int mk_map2tod(void *dat, const void *map, const int32_t *ipix, int64_t ndet,
+                          int64_t ndata, int64_t npix, int dtype, int do_add, void *stream) {
+  MK_CHECK_ARG(ndet >= 0 && ndata >= 0 && npix >= 0, "mk_map2tod: negative size");
+  MK_CHECK_ARG(MK_DTYPE_OK(dtype), "mk_map2tod: bad dtype %d", dtype);
+  int64_t n = ndet * ndata;
+  if (n == 0) return MK_OK;
+  MK_CHECK_ARG(dat && map && ipix, "mk_map2tod: null pointer");
+  cudaStream_t st = mk::as_stream(stream);
+  return dtype == MK_F64 ? map2tod_t<double>(dat, map, ipix, n, npix, do_add, st)
+                         : map2tod_t<float>(dat, map, ipix, n, npix, do_add, st);
+}
+
+extern "C" int mk_tod2map(void *map, const void *dat, const int32_t *ipix, int64_t ndet,
+                          int64_t ndata, int64_t npix, int dtype, void *stream) {
+  MK_CHECK_ARG(ndet >= 0 && ndata >= 0 && npix >= 0, "mk_tod2map: negative size");
+  MK_CHECK_ARG(MK_DTYPE_OK(dtype), "mk_tod2map: bad dtype %d", dtype);
+  int64_t n = ndet * ndata;
+  if (n == 0) return MK_OK;
+  MK_CHECK_ARG(dat && map && ipix, "mk_tod2map: null pointer");
+  cudaStream_t st = mk::as_stream(stream);
+  return dtype == MK_F64 ? tod2map_t<double, false>(map, dat, ipix, n, npix, nullptr, 1, st)
+                         : tod2map_t<float, false>(map, dat, ipix, n, npix, nullptr, 1, st);
+}
+
+extern "C" int mk_tod2map_rows(void *map, const void *w, const int32_t *ipix, int64_t ndet,
+                               int64_t ndata, int64_t npix, int dtype, void *stream) {
+  MK_CHECK_ARG(ndet >= 0 && ndata >= 0 && npix >= 0, "mk_tod2map_rows: negative size");
+  MK_CHECK_ARG(MK_DTYPE_OK(dtype), "mk_tod2map_rows: bad dtype %d", dtype);
+  int64_t n = ndet * ndata;
+  if (n == 0) return MK_OK;
+  MK_CHECK_ARG(map && ipix, "mk_tod2map_rows: null pointer");
+  cudaStream_t st = mk::as_stream(stream);
+  return dtype == MK_F64 ? tod2map_t<double, true>(map, nullptr, ipix, n, npix, w, ndata, st)
+                         : tod2map_t<float, true>(map, nullptr, ipix, n, npix, w, ndata, st);
+}
+
+extern "C" int mk_check_pix(const int32_t *ipix, int64_t n, int64_t npix, int64_t *nbad,
+                            void *stream) {
+  MK_CHECK_ARG(nbad, "mk_check_pix: null result pointer");
+  *nbad = 0;
+  if (n <= 0) return MK_OK;
+  MK_CHECK_ARG(ipix, "mk_check_pix: null ipix");
+  cudaStream_t st = mk::as_stream(stream);
+  unsigned long long *d = nullptr;
+  MK_CUDA(cudaMallocAsync((void **)&d, sizeof(*d), st));
+  MK_CUDA(cudaMemsetAsync(d, 0, sizeof(*d), st));
+  k_count_bad<<<mk_grid(n, 256, 8), 256, 0, st>>>(ipix, n, npix, d);
+  int rc = mk::launch_status("mk_check_pix");
+  unsigned long long h = 0;
+  cudaError_t e1 = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, st);
+  cudaError_t e2 = cudaFreeAsync(d, st);
+  cudaError_t e3 = cudaStreamSynchronize(st);
+  if (rc != MK_OK) return rc;
+  MK_CUDA(e1);
+  MK_CUDA(e2);
+  MK_CUDA(e3);
+  *nbad = (int64_t)h;
+  return MK_OK;
+}
+
+extern "C" int mk_pixplan_create(mk_pixplan **plan, const int32_t *ipix, int64_t n, int64_t npix,
+                                 void *stream) {
+  MK_CHECK_ARG(plan, "mk_pixplan_create: null plan pointer");
+  *plan = nullptr;
+  MK_CHECK_ARG(n >= 0 && n < (int64_t)INT32_MAX, "mk_pixplan_create: n=%lld must be < 2^31",
+               (long long)n);
+  MK_CHECK_ARG(npix > 0 && npix < (int64_t)INT32_MAX, "mk_pixplan_create: bad npix");
+  MK_CHECK_ARG(n == 0 || ipix, "mk_pixplan_create: null ipix");
+  int64_t nbad = 0;
+  int rc = mk_check_pix(ipix, n, npix, &nbad, stream);
+  if (rc) return rc;
+  if (nbad) {
+    mk::set_error("mk_pixplan_create: %lld pixel indices outside [0, %lld)", (long long)nbad,
+                  (long long)npix);
+    return MK_ERR_RANGE;
+  }
+  cudaStream_t st = mk::as_stream(stream);
+  mk_pixplan *pl = new (std::nothrow) mk_pixplan;
+  if (!pl) return MK_ERR_NOMEM;
+  pl->n = n;
+  pl->npix = npix;
+  int32_t *keys_out = nullptr, *idx_in = nullptr;
+  void *tmp = nullptr;
+  size_t tmp_bytes = 0;
+  int end_bit = 1;
+  while (end_bit < 31 && (int64_t(1) << end_bit) < npix) end_bit++;
+  cudaError_t e = cudaSuccess;
+  auto fail = [&](const char *what, cudaError_t err) {
+    mk::set_error("mk_pixplan_create: %s: %s", what, cudaGetErrorString(err));
+    cudaFree(keys_out);
+    cudaFree(idx_in);
+    cudaFree(tmp);
+    cudaFree(pl->perm);
+    cudaFree(pl->off);
+    delete pl;
+    return MK_ERR_CUDA;
+  };
+  size_t nb = (size_t)(n > 0 ? n : 1) * sizeof(int32_t);
+  if ((e = cudaMalloc(&pl->perm, nb)) != cudaSuccess) return fail("cudaMalloc", e);
+  if ((e = cudaMalloc(&pl->off, (size_t)(npix + 1) * sizeof(int32_t))) != cudaSuccess)
+    return fail("cudaMalloc", e);
+  if ((e = cudaMalloc(&keys_out, nb)) != cudaSuccess) return fail("cudaMalloc", e);
+  if ((e = cudaMalloc(&idx_in, nb)) != cudaSuccess) return fail("cudaMalloc", e);
+  if (n > 0) {
+    k_iota<<<mk_grid(n, 256, 8), 256, 0, st>>>(idx_in, n);
+    if ((e = cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, ipix, keys_out, idx_in, pl->perm,
+                                             (int)n, 0, end_bit, st)) != cudaSuccess)
+      return fail("sort sizing", e);
+    if ((e = cudaMalloc(&tmp, tmp_bytes)) != cudaSuccess) return fail("cudaMalloc", e);
+    if ((e = cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, ipix, keys_out, idx_in, pl->perm,
+                                             (int)n, 0, end_bit, st)) != cudaSuccess)
+      return fail("sort", e);
+  }
+  k_pix_offsets<<<mk_grid(npix + 1, 256, 8), 256, 0, st>>>(keys_out, n, pl->off, npix);
+  if ((e = cudaGetLastError()) != cudaSuccess) return fail("offsets", e);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail("sync", e);
+  cudaFree(keys_out);
+  cudaFree(idx_in);
+  cudaFree(tmp);
+  *plan = pl;
+  return MK_OK;
+}
+
+extern "C" int mk_tod2map_sorted(void *map, const void *dat, const mk_pixplan *plan, int dtype,
+                                 void *stream) {
+  MK_CHECK_ARG(plan && map, "mk_tod2map_sorted: null pointer");
+  MK_CHECK_ARG(MK_DTYPE_OK(dtype), "mk_tod2map_sorted: bad dtype %d", dtype);
+  if (plan->n == 0) return MK_OK;
+  MK_CHECK_ARG(dat, "mk_tod2map_sorted: null dat");
+  cudaStream_t st = mk::as_stream(stream);
+  unsigned g = mk_grid(plan->npix * 32, 256, 8);
+  if (dtype == MK_F64)
+    k_tod2map_sorted<double><<<g, 256, 0, st>>>((double *)map, (const double *)dat, plan->perm,
+                                                 plan->off, plan->npix);
+  else
+    k_tod2map_sorted<float><<<g, 256, 0, st>>>((float *)map, (const float *)dat, plan->perm,
+                                                plan->off, plan->npix);
+  return mk::launch_status("mk_tod2map_sorted");
+}
+
+extern "C" int mk_pixplan_destroy(mk_pixplan *plan) {
+  if (!plan) return MK_OK;
+  cudaFree(plan->perm);
+  cudaFree(plan->off);
+  delete plan;
+  return MK_OK;
+}
+
+extern "C" size_t mk_tod2map_fixed_scratch_bytes(int64_t npix) {
+  return sizeof(FixHdr) + (size_t)(npix > 0 ? npix : 0) * sizeof(unsigned long long);
+}
+
+extern "C" int mk_tod2map_fixed(void *map, const void *dat, const int32_t *ipix, int64_t ndet,
+                                int64_t ndata, int64_t npix, int64_t hmax, int dtype, void *scratch,
+                                void *stream) {
+  MK_CHECK_ARG(ndet >= 0 && ndata >= 0 && npix >= 0, "mk_tod2map_fixed: negative size");
+  MK_CHECK_ARG(MK_DTYPE_OK(dtype), "mk_tod2map_fixed: bad dtype %d", dtype);
+  MK_CHECK_ARG(hmax >= 1, "mk_tod2map_fixed: hmax must be >= 1 (max hits of any pixel)");
+  int64_t n = ndet * ndata;
+  if (n == 0) return MK_OK;
+  MK_CHECK_ARG(map && dat && ipix && scratch, "mk_tod2map_fixed: null pointer");
+  MK_CHECK_ARG(((uintptr_t)scratch % 256) == 0, "mk_tod2map_fixed: scratch must be 256-byte aligned");
+  int hbits = 0;
+  while (hbits < 62 && (int64_t(1) << hbits) < hmax) hbits++;
+  MK_CHECK_ARG(hbits <= 40, "mk_tod2map_fixed: hmax=%lld too large for 64-bit accumulation",
+               (long long)hmax);
+  cudaStream_t st = mk::as_stream(stream);
+  return dtype == MK_F64 ? tod2map_fixed_t<double>(map, dat, ipix, n, npix, hbits, scratch, st)
+                         : tod2map_fixed_t<float>(map, dat, ipix, n, npix, hbits, scratch, st);
+}

@@ -1,0 +1,290 @@
+"""Tensor-level wrappers over the libmkgpu C ABI.
+
+Every function takes CUDA torch tensors (C-contiguous, float64 or float32 data,
+int32 pixel indices), launches on torch's current stream, and raises
+``MkError`` on a non-zero status.  There is no CPU path: a CPU tensor is an
+error, and so is a missing library.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Optional
+
+import torch
+
+from . import _lib
+from ._lib import MK_F32, MK_F64, check
+
+_DT = {torch.float64: MK_F64, torch.float32: MK_F32}
+
+
+def lib():
+    return _lib.load()
+
+
+def _stream() -> ctypes.c_void_p:
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _p(t: Optional[torch.Tensor]):
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def _dev(t: torch.Tensor, name: str) -> None:
+    if not t.is_cuda:
+        raise ValueError(f"{name} must be a CUDA tensor (no CPU fallback)")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be C-contiguous")
+
+
+def dtype_code(t: torch.Tensor) -> int:
+    try:
+        return _DT[t.dtype]
+    except KeyError:
+        raise TypeError(f"unsupported dtype {t.dtype}; use float64 or float32") from None
+
+
+def _ipix(ipix: torch.Tensor, shape) -> None:
+    _dev(ipix, "ipix")
+    if ipix.dtype != torch.int32:
+        raise TypeError("ipix must be int32 (the reference's pixel index type)")
+    if ipix.numel() != int(torch.Size(shape).numel()):
+        raise ValueError(f"ipix has {ipix.numel()} entries, data has {torch.Size(shape).numel()}")
+
+
+def _nd(t: torch.Tensor):
+    if t.dim() == 2:
+        return t.shape[0], t.shape[1]
+    return 1, t.numel()
+
+
+# ---------------------------------------------------------------------------
+# projections
+# ---------------------------------------------------------------------------
+def map2tod(dat: torch.Tensor, map: torch.Tensor, ipix: torch.Tensor, do_add: bool = True) -> None:
+    """dat (+)= map.flat[ipix]  (mk_map2tod; minkasi.c:131-144)."""
+    _dev(dat, "dat"), _dev(map, "map"), _ipix(ipix, dat.shape)
+    if map.dtype != dat.dtype:
+        raise TypeError("map and dat must have the same dtype")
+    ndet, ndata = _nd(dat)
+    check(lib().mk_map2tod(_p(dat), _p(map), _p(ipix), ndet, ndata, map.numel(), dtype_code(dat),
+                           int(bool(do_add)), _stream()), "map2tod")
+
+
+def tod2map(map: torch.Tensor, dat: torch.Tensor, ipix: torch.Tensor) -> None:
+    """map.flat[ipix] += dat with warp-aggregated atomics (mk_tod2map)."""
+    _dev(dat, "dat"), _dev(map, "map"), _ipix(ipix, dat.shape)
+    if map.dtype != dat.dtype:
+        raise TypeError("map and dat must have the same dtype")
+    ndet, ndata = _nd(dat)
+    check(lib().mk_tod2map(_p(map), _p(dat), _p(ipix), ndet, ndata, map.numel(), dtype_code(dat),
+                           _stream()), "tod2map")
+
+
+def tod2map_rows(map: torch.Tensor, ipix: torch.Tensor, w: Optional[torch.Tensor] = None) -> None:
+    """map.flat[ipix[d, t]] += w[d] (1 when w is None) -- hit / weight maps."""
+    _dev(map, "map"), _dev(ipix, "ipix")
+    if ipix.dtype != torch.int32:
+        raise TypeError("ipix must be int32")
+    ndet, ndata = _nd(ipix)
+    if w is not None:
+        _dev(w, "w")
+        if w.dtype != map.dtype or w.numel() != ndet:
+            raise ValueError("w must have one entry per detector and the map's dtype")
+    check(lib().mk_tod2map_rows(_p(map), _p(w), _p(ipix), ndet, ndata, map.numel(),
+                                dtype_code(map), _stream()), "tod2map_rows")
+
+
+class FixedScratch:
+    """Accumulator scratch for the deterministic fixed-point tod2map."""
+
+    def __init__(self, npix: int, device=None):
+        device = device or torch.device("cuda", torch.cuda.current_device())
+        self.npix = int(npix)
+        nb = int(lib().mk_tod2map_fixed_scratch_bytes(self.npix))
+        self.buf = torch.zeros(nb, dtype=torch.uint8, device=device)
+
+
+def tod2map_fixed(map: torch.Tensor, dat: torch.Tensor, ipix: torch.Tensor, hmax: int,
+                  scratch: FixedScratch) -> None:
+    """Bitwise-reproducible map.flat[ipix] += dat (mk_tod2map_fixed); hmax
+    bounds the number of samples that hit any one pixel."""
+    _dev(dat, "dat"), _dev(map, "map"), _ipix(ipix, dat.shape)
+    if map.dtype != dat.dtype or scratch.npix != map.numel():
+        raise ValueError("tod2map_fixed: dtype or scratch size mismatch")
+    ndet, ndata = _nd(dat)
+    check(lib().mk_tod2map_fixed(_p(map), _p(dat), _p(ipix), ndet, ndata, map.numel(), int(hmax),
+                                 dtype_code(dat), _p(scratch.buf), _stream()), "tod2map_fixed")
+
+
+def check_pix(ipix: torch.Tensor, npix: int) -> int:
+    """Number of pixel indices outside [0, npix) (synchronises the stream)."""
+    _dev(ipix, "ipix")
+    nbad = ctypes.c_int64(0)
+    check(lib().mk_check_pix(_p(ipix), ipix.numel(), int(npix), ctypes.byref(nbad), _stream()),
+          "check_pix")
+    return int(nbad.value)
+
+
+class PixPlan:
+    """Sorted pixel plan for the deterministic tod2map (mk_pixplan_*)."""
+
+    def __init__(self, ipix: torch.Tensor, npix: int):
+        _dev(ipix, "ipix")
+        self.npix, self.n = int(npix), ipix.numel()
+        h = ctypes.c_void_p()
+        check(lib().mk_pixplan_create(ctypes.byref(h), _p(ipix), self.n, self.npix, _stream()),
+              "pixplan_create")
+        self._h = h
+
+    def tod2map(self, map: torch.Tensor, dat: torch.Tensor) -> None:
+        _dev(map, "map"), _dev(dat, "dat")
+        if dat.numel() != self.n or map.numel() != self.npix or map.dtype != dat.dtype:
+            raise ValueError("dat / map do not match the plan")
+        check(lib().mk_tod2map_sorted(_p(map), _p(dat), self._h, dtype_code(dat), _stream()),
+              "tod2map_sorted")
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().mk_pixplan_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+
+# ---------------------------------------------------------------------------
+# DCT-I and apply_noise
+# ---------------------------------------------------------------------------
+def _workspace(nbytes: int, device) -> torch.Tensor:
+    # torch's caching allocator returns 512-byte aligned blocks
+    return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
+
+
+class DCT1:
+    """Batched unnormalised DCT-I (REDFT00) of (nrow, n) arrays."""
+
+    def __init__(self, nrow: int, n: int, dtype=torch.float64, device=None,
+                 workspace: Optional[torch.Tensor] = None):
+        self.nrow, self.n, self.dtype = int(nrow), int(n), dtype
+        code = _DT[dtype]
+        nb = ctypes.c_size_t(0)
+        check(lib().mk_dct1_workspace_bytes(self.nrow, self.n, code, ctypes.byref(nb)), "dct1 size")
+        self.workspace_bytes = int(nb.value)
+        device = device or torch.device("cuda", torch.cuda.current_device())
+        self.ws = workspace if workspace is not None else _workspace(self.workspace_bytes, device)
+        h = ctypes.c_void_p()
+        check(lib().mk_dct1_plan_create(ctypes.byref(h), self.nrow, self.n, code, _p(self.ws),
+                                        self.ws.numel()), "dct1 plan")
+        self._h = h
+
+    def __call__(self, x: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        _dev(x, "x")
+        if x.dtype != self.dtype or _nd(x) != (self.nrow, self.n):
+            raise ValueError(f"x must be {self.dtype} of shape ({self.nrow}, {self.n})")
+        if out is None:
+            out = torch.empty_like(x)
+        check(lib().mk_dct1_exec(self._h, _p(x), _p(out), _stream()), "dct1")
+        return out
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().mk_dct1_plan_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+
+def noise_workspace_bytes(ndet: int, ndata: int, dtype=torch.float64) -> int:
+    nb = ctypes.c_size_t(0)
+    check(lib().mk_noise_workspace_bytes(int(ndet), int(ndata), _DT[dtype], ctypes.byref(nb)),
+          "noise workspace size")
+    return int(nb.value)
+
+
+class NoisePlan:
+    """apply_noise for TODs of one (ndet, ndata) shape; the workspace may be
+    shared between plans that run on the same stream."""
+
+    def __init__(self, ndet: int, ndata: int, dtype=torch.float64, device=None,
+                 workspace: Optional[torch.Tensor] = None):
+        self.ndet, self.ndata, self.dtype = int(ndet), int(ndata), dtype
+        self.workspace_bytes = noise_workspace_bytes(ndet, ndata, dtype)
+        device = device or torch.device("cuda", torch.cuda.current_device())
+        self.ws = workspace if workspace is not None else _workspace(self.workspace_bytes, device)
+        if self.ws.numel() < self.workspace_bytes:
+            raise ValueError("shared workspace too small for this TOD shape")
+        h = ctypes.c_void_p()
+        check(lib().mk_noise_plan_create(ctypes.byref(h), self.ndet, self.ndata, _DT[dtype],
+                                         _p(self.ws), self.ws.numel()), "noise plan")
+        self._h = h
+
+    def apply(self, v: torch.Tensor, vT: torch.Tensor, mywt: torch.Tensor, dat: torch.Tensor,
+              out: Optional[torch.Tensor] = None, rot_mode: int = 0) -> torch.Tensor:
+        for t, nm in ((v, "v"), (vT, "vT"), (mywt, "mywt"), (dat, "dat")):
+            _dev(t, nm)
+            if t.dtype != self.dtype:
+                raise TypeError(f"{nm} must be {self.dtype}")
+        if tuple(dat.shape) != (self.ndet, self.ndata):
+            raise ValueError(f"dat shape {tuple(dat.shape)} != plan ({self.ndet}, {self.ndata})")
+        if mywt.dim() != 2 or mywt.shape[0] != self.ndet or mywt.shape[1] < self.ndata:
+            raise ValueError("mywt must be (ndet, >= ndata)")
+        if out is None:
+            out = torch.empty_like(dat)
+        check(lib().mk_apply_noise(self._h, _p(v), _p(vT), _p(mywt), mywt.shape[1], _p(dat),
+                                   _p(out), int(rot_mode), _stream()), "apply_noise")
+        return out
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().mk_noise_plan_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+
+# ---------------------------------------------------------------------------
+# map algebra and the PCG recurrence
+# ---------------------------------------------------------------------------
+class Reducer:
+    """Owns the FP64 reduction scratch used by dot / pcg kernels."""
+
+    def __init__(self, device=None):
+        device = device or torch.device("cuda", torch.cuda.current_device())
+        self.scratch = torch.zeros(int(lib().mk_reduce_scratch_bytes()), dtype=torch.uint8,
+                                   device=device)
+
+    def dot(self, a: torch.Tensor, b: torch.Tensor, out: Optional[torch.Tensor] = None) -> torch.Tensor:
+        _dev(a, "a"), _dev(b, "b")
+        if a.dtype != b.dtype or a.numel() != b.numel():
+            raise ValueError("dot: operands differ in dtype or size")
+        if out is None:
+            out = torch.empty((), dtype=torch.float64, device=a.device)
+        check(lib().mk_dot(_p(a), _p(b), a.numel(), dtype_code(a), _p(out), _p(self.scratch),
+                           _stream()), "dot")
+        return out
+
+
+def axpy(y: torch.Tensor, x: torch.Tensor, alpha: float) -> None:
+    _dev(y, "y"), _dev(x, "x")
+    check(lib().mk_axpy(_p(y), _p(x), float(alpha), y.numel(), dtype_code(y), _stream()), "axpy")
+
+
+def mul(out: torch.Tensor, a: torch.Tensor, b: torch.Tensor) -> None:
+    _dev(out, "out"), _dev(a, "a"), _dev(b, "b")
+    check(lib().mk_mul(_p(out), _p(a), _p(b), out.numel(), dtype_code(out), _stream()), "mul")
+
+
+def pcg_init(r, z, p, b, Ax, precon, s, reducer: Reducer) -> None:
+    check(lib().mk_pcg_init(_p(r), _p(z), _p(p), _p(b), _p(Ax), _p(precon), r.numel(),
+                            dtype_code(r), _p(s), _p(reducer.scratch), _stream()), "pcg_init")
+
+
+def pcg_update(x, r, z, p, Ap, precon, s, reducer: Reducer) -> None:
+    check(lib().mk_pcg_update(_p(x), _p(r), _p(z), _p(p), _p(Ap), _p(precon), x.numel(),
+                              dtype_code(x), _p(s), _p(reducer.scratch), _stream()), "pcg_update")

@@ -1,0 +1,258 @@
+"""Preconditioned conjugate gradients (minkasi/mapmaking/pcg.py:22-255).
+
+``run_pcg`` / ``run_pcg_wprior`` keep the reference's signatures and
+recurrence (same order of updates, fixed ``maxiter`` unless the new ``tol``
+keyword is given).  On the fast path (one SkyMap, SmoothedSVD noise, no
+prior) an iteration is: one batched A-apply (map2tod, per-TOD noise filter,
+tod2map) + three fused update kernels with every scalar on the device, and
+from the second iteration on the whole iteration is replayed as one CUDA
+graph -- no host round trip per iteration.
+
+``run_pcg_mixed`` is the mixed-precision solver: an FP64 outer iterative
+refinement (true FP64 residual b - A x each outer step) around FP32 inner
+PCG solves (FP32 projections, filter and map vectors; FP64 dot products).
+It stops when the FP64 true residual ||b - A x|| / ||b|| reaches ``tol``.
+"""
+from __future__ import annotations
+
+import math
+import sys
+import time
+from typing import List, Optional
+
+import numpy as np
+import torch
+
+from . import kernels as K
+from ._lib import MK_S_FLAG, MK_S_ITER, MK_S_RR, MK_S_ZR
+from .maps import Mapset, SkyMap, _reducer
+from .tods import TodVec
+
+
+class HasPrior:
+    """Protocol of a prior: apply_prior(x, Ax) adds Q^-1 x to Ax (pcg.py:17-19)."""
+
+    def apply_prior(self, x, Ax):  # pragma: no cover - protocol
+        raise NotImplementedError
+
+
+class null_precon:
+    """A preconditioner that does nothing (pcg.py:241-255)."""
+
+    def __init__(self):
+        self.isnull = True
+
+    def __add__(self, val):
+        return val
+
+    def __mul__(self, val):
+        return val
+
+
+def _is_map_precon(precon) -> bool:
+    return isinstance(precon, Mapset) and precon.nmap == 1 and isinstance(precon.maps[0], SkyMap)
+
+
+class DevicePCG:
+    """Device-resident PCG state for one operator (flat maps of its dtype)."""
+
+    def __init__(self, op, b: torch.Tensor, x: torch.Tensor, M: Optional[torch.Tensor],
+                 graph: bool = True):
+        self.op = op
+        self.n = b.numel()
+        dt, dev = b.dtype, b.device
+        self.b = b.reshape(-1)
+        self.x = x.reshape(-1)
+        self.M = None if M is None else M.reshape(-1).to(dt).contiguous()
+        self.r = torch.empty(self.n, dtype=dt, device=dev)
+        self.z = torch.empty_like(self.r)
+        self.p = torch.empty_like(self.r)
+        self.Ap = torch.empty_like(self.r)
+        self.s = torch.zeros(8, dtype=torch.float64, device=dev)
+        self.red = _reducer(dev)
+        self.graph_enabled = graph
+        self._graph = None
+        self.iters = 0
+
+    def start(self, Ax: Optional[torch.Tensor] = None) -> None:
+        if Ax is None:
+            self.op.apply(self.x, self.Ap)
+            Ax = self.Ap
+        K.pcg_init(self.r, self.z, self.p, self.b, Ax.reshape(-1), self.M, self.s, self.red)
+        self.iters = 0
+
+    def _step(self) -> None:
+        self.op.apply(self.p, self.Ap)
+        K.pcg_update(self.x, self.r, self.z, self.p, self.Ap, self.M, self.s, self.red)
+
+    def step(self) -> None:
+        if self.graph_enabled and self.iters >= 1:
+            if self._graph is None:
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g):
+                    self._step()
+                self._graph = g
+            self._graph.replay()
+        else:
+            self._step()
+        self.iters += 1
+
+    def scalars(self) -> np.ndarray:
+        return self.s.cpu().numpy()
+
+
+def _true_residual(op, b: torch.Tensor, x: torch.Tensor) -> float:
+    ax = torch.empty_like(b)
+    op.apply(x, ax)
+    r = b.reshape(-1) - ax.reshape(-1)
+    red = _reducer(b.device)
+    return math.sqrt(red.dot(r, r).item()) / math.sqrt(red.dot(b.reshape(-1), b.reshape(-1)).item())
+
+
+def run_pcg_wprior(b: Mapset, x0: Mapset, tods: TodVec, prior=None, precon=None,
+                   mask: Optional[Mapset] = None, maxiter: int = 25, outroot: str = "map",
+                   save_iters: List[int] = [-1], save_ind: int = 0, save_tail: str = ".fits",
+                   plot_iters: List[int] = [], plot_info=None, plot_ind: int = 0, *,
+                   tol: Optional[float] = None, check_every: int = 10, graph: bool = True,
+                   verbose: bool = True, history: Optional[list] = None) -> Mapset:
+    """PCG on A x = b (pcg.py:22-200).  With ``tol`` set, stops once the
+    FP64 true residual ||b - A x||/||b|| <= tol (checked when the recursive
+    residual says so, every ``check_every`` iterations)."""
+    fast = (prior is None and mask is None and isinstance(tods, TodVec) and tods._fast(b)
+            and (precon is None or _is_map_precon(precon)))
+    if not fast:
+        return _run_pcg_generic(b, x0, tods, prior, precon, mask, maxiter, outroot, save_iters,
+                                save_ind, save_tail, verbose, history)
+    t0 = time.time()
+    op = tods.engine(b.maps[0])
+    x = x0.copy()
+    M = precon.maps[0].map if precon is not None else None
+    st = DevicePCG(op, b.maps[0].map, x.maps[0].map, M, graph=graph)
+    st.start()
+    bnorm = math.sqrt(b.dot(b)) if tol is not None else None
+    nsamp = tods.get_nsamp()
+    torch.cuda.synchronize()
+    tloop = time.time()
+    i = -1
+    for i in range(maxiter):
+        st.step()
+        need_check = tol is not None and ((i + 1) % check_every == 0 or i == maxiter - 1)
+        if i in save_iters:
+            x.maps[save_ind].write(outroot + "_" + str(i) + save_tail)
+        if need_check or history is not None:
+            s = st.scalars()
+            if s[MK_S_FLAG]:
+                raise FloatingPointError(f"PCG breakdown at iteration {i} (p.Ap <= 0 or non-finite)")
+            rec = math.sqrt(max(s[MK_S_RR], 0.0)) / bnorm if bnorm else float("nan")
+            if history is not None:
+                history.append({"iter": i, "zr": float(s[MK_S_ZR]), "rel_rr": rec})
+            if need_check and rec <= tol:
+                tr = _true_residual(op, b.maps[0].map, x.maps[0].map)
+                if history is not None:
+                    history[-1]["true_rel_residual"] = tr
+                if tr <= tol:
+                    break
+    torch.cuda.synchronize()
+    niter = i + 1
+    tave = (time.time() - tloop) / max(niter, 1)
+    if verbose:
+        print("average time per iteration was ", tave, " with effective throughput ",
+              nsamp / tave / 1e6, " Msamp/s")
+        sys.stdout.flush()
+    x.niter = niter
+    x.setup_s = tloop - t0
+    return x
+
+
+def run_pcg(b: Mapset, x0: Mapset, tods: TodVec, precon=None, mask: Optional[Mapset] = None,
+            maxiter: int = 25, outroot: str = "map", save_iters: List[int] = [-1],
+            save_ind: int = 0, save_tail: str = ".fits", plot_iters: List[int] = [],
+            plot_info=None, plot_ind: int = 0, **kw) -> Mapset:
+    """run_pcg_wprior without a prior (pcg.py:203-238)."""
+    return run_pcg_wprior(b, x0, tods, None, precon, mask, maxiter, outroot, save_iters, save_ind,
+                          save_tail, plot_iters, plot_info, plot_ind, **kw)
+
+
+def _run_pcg_generic(b, x0, tods, prior, precon, mask, maxiter, outroot, save_iters, save_ind,
+                     save_tail, verbose, history):
+    """The reference recurrence on Mapset algebra (still GPU kernels): for
+    priors, masks and multi-map Mapsets."""
+    Ax = tods.dot(x0, mask=mask)
+    r = b.copy()
+    r.axpy(Ax, -1)
+    z = precon * r if precon is not None else r.copy()
+    p = z.copy()
+    zr = r.dot(z)
+    x = x0.copy()
+    for i in range(maxiter):
+        Ap = tods.dot(p, mask=mask)
+        if prior is not None:
+            prior.apply_prior(p, Ap)
+        pAp = p.dot(Ap)
+        alpha = zr / pAp
+        x_new = x.copy()
+        x_new.axpy(p, alpha)
+        r_new = r.copy()
+        r_new.axpy(Ap, -alpha)
+        z_new = precon * r_new if precon is not None else r_new.copy()
+        zr_new = r_new.dot(z_new)
+        beta = zr_new / zr
+        p_new = z_new.copy()
+        p_new.axpy(p, beta)
+        p, z, r, zr, x = p_new, z_new, r_new, zr_new, x_new
+        if history is not None:
+            history.append({"iter": i, "zr": zr, "alpha": alpha, "beta": beta})
+        if i in save_iters:
+            x.maps[save_ind].write(outroot + "_" + str(i) + save_tail)
+    x.niter = maxiter
+    return x
+
+
+def run_pcg_mixed(b: Mapset, x0: Mapset, tods: TodVec, precon=None, tol: float = 1e-6,
+                  inner_iters: int = 20, max_outer: int = 200, graph: bool = True,
+                  verbose: bool = False, history: Optional[list] = None,
+                  inner_precon=None) -> Mapset:
+    """Mixed precision: FP64 outer iterative refinement, FP32 inner PCG.
+
+    Each outer step computes the FP64 true residual r = b - A64 x (FP64
+    projections and filter), stops if ||r||/||b|| <= tol, else solves
+    A32 e = r approximately with ``inner_iters`` FP32 PCG iterations (FP64
+    dot products) and updates x += e in FP64.  ``inner_precon`` replaces the
+    Jacobi precon in the inner solve (any object with apply(r32, z32))."""
+    m64 = b.maps[0]
+    op64 = tods.engine(m64, torch.float64)
+    op32 = tods.engine(m64, torch.float32)
+    x = x0.copy()
+    xf = x.maps[0].map.reshape(-1)
+    bf = m64.map.reshape(-1)
+    red = _reducer(bf.device)
+    bnorm = math.sqrt(red.dot(bf, bf).item())
+    M32 = precon.maps[0].map.reshape(-1).float().contiguous() if precon is not None else None
+    r32 = torch.empty(bf.numel(), dtype=torch.float32, device=bf.device)
+    e32 = torch.zeros_like(r32)
+    zero32 = torch.zeros_like(r32)
+    inner = DevicePCG(op32, r32, e32, M32, graph=graph)
+    ax = torch.empty_like(bf)
+    total_inner = 0
+    rel = float("inf")
+    for outer in range(max_outer):
+        op64.apply(xf, ax)
+        r64 = bf - ax
+        rel = math.sqrt(red.dot(r64, r64).item()) / bnorm
+        if history is not None:
+            history.append({"outer": outer, "inner_total": total_inner, "true_rel_residual": rel})
+        if verbose:
+            print(f"outer {outer}: true FP64 residual {rel:.3e} after {total_inner} inner iterations")
+        if rel <= tol:
+            break
+        r32.copy_(r64)
+        e32.zero_()
+        inner.start(zero32)
+        for _ in range(inner_iters):
+            inner.step()
+        total_inner += inner_iters
+        xf.add_(e32.to(torch.float64))
+    x.niter = total_inner
+    x.outer = outer
+    x.rel_residual = rel
+    return x

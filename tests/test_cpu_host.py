@@ -1,0 +1,82 @@
+"""Host-side checks that need no GPU: the C-ABI library loads and exports
+every entry point include/mkgpu.h declares, truncation and synthetic-shape
+logic, TOD partitioning."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_library_exports_every_header_symbol():
+    from minkasi_gb300 import _lib
+    h = _lib.load()
+    declared = _lib.header_symbols()
+    assert len(declared) >= 20
+    for name in declared:
+        assert hasattr(h, name), name           # dlsym succeeds
+        assert name in _lib.SIGNATURES, name     # and the binding covers it
+    assert h.mk_version() >= 1
+    assert h.mk_reduce_scratch_bytes() > 0       # pure host query, no device work
+
+
+def test_library_is_built_for_sm103a():
+    # the build passes one -gencode for compute_103a/sm_103a
+    from minkasi_gb300 import build
+    assert build.ARCH == ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def test_argument_errors_need_no_gpu():
+    from minkasi_gb300 import _lib
+    h = _lib.load()
+    assert h.mk_map2tod(None, None, None, 1, 1, 1, 7, 0, None) == _lib.MK_ERR_ARG
+    assert b"dtype" in h.mk_last_error()
+    nb = ctypes.c_size_t(0)
+    assert h.mk_dct1_workspace_bytes(4, 1, 0, ctypes.byref(nb)) == _lib.MK_ERR_ARG
+    assert h.mk_tod2map_fixed(None, None, None, 1, 1, 1, 0, 0, None, None) == _lib.MK_ERR_ARG
+
+
+def test_truncation_matches_reference(gold):
+    from minkasi_gb300 import truncate
+    g = gold("lens.npz")
+    for n, t in zip(g["ndata"], g["truncated"]):
+        assert truncate.truncated_length(int(n)) == int(t)
+    info = {"dat_calib": np.zeros((3, 1025)), "ipix": np.zeros((3, 1025), np.int32), "x": 5}
+    truncate.truncate_tod(info)
+    assert info["dat_calib"].shape == (3, g["truncated"][list(g["ndata"]).index(1025)])
+
+
+def test_synth_shapes_are_seeded_and_smooth():
+    from minkasi_gb300 import synth, truncate
+    a = synth.tod_shapes(synth.CONFIGS["c2"])
+    b = synth.tod_shapes(synth.CONFIGS["c2"])
+    assert a == b and len(a) == 32
+    for ndet, n in a:
+        assert ndet == 256 and (1 << 17) - 2000 <= n <= (1 << 19)
+        assert truncate.truncated_length(n) == n   # already FFT friendly
+    c4 = synth.tod_shapes(synth.CONFIGS["c4"])
+    assert len(c4) == 200 and set(d for d, _ in c4) <= {32, 64, 128, 256}
+
+
+def test_synth_pointing_in_range_on_cpu():
+    import torch
+    from minkasi_gb300 import synth
+    cfg = synth.CONFIGS["tiny"]
+    info = synth.make_tod_info(cfg, 0, 8, 3001, torch.device("cpu"))
+    ip = info["ipix"].numpy()
+    assert ip.dtype == np.int32 and ip.min() >= 0 and ip.max() < cfg.nx * cfg.ny
+    assert info["dat_calib"].shape == (8, 3001)
+
+
+def test_partition_balances_uneven_tods():
+    from minkasi_gb300 import parallel
+    costs = [parallel.tod_cost(nd, n) for nd, n in [(256, 500000), (32, 60000), (128, 300000),
+                                                    (64, 100000), (256, 200000), (32, 550000)]]
+    parts = parallel.partition(costs, 2)
+    assert sorted(sum(parts, [])) == list(range(6))
+    loads = [sum(costs[i] for i in p) for p in parts]
+    assert max(loads) / min(loads) < 1.6
+    assert parallel.partition(costs, 2) == parts  # deterministic

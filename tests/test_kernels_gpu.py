@@ -1,0 +1,220 @@
+"""Parity of each CUDA kernel (through the C ABI) with the oracle and with the
+reference-generated golden fixtures.  GPU only."""
+import numpy as np
+import pytest
+import torch
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+cuda = torch.device("cuda", 0)
+
+
+def dev(a, dtype=None):
+    t = torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+    return t.to(dtype) if dtype is not None else t
+
+
+def rel(a, b):
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def K():
+    from minkasi_gb300 import kernels
+    return kernels
+
+
+# ---------------------------------------------------------------- projections
+def test_map2tod_golden_bit_exact(K, gold):
+    g = gold("proj.npz")
+    for do_add, key in ((True, "map2tod_add"), (False, "map2tod_set")):
+        d = dev(g["dat"])
+        K.map2tod(d, dev(g["map"]), dev(g["ipix"]), do_add)
+        assert np.array_equal(d.cpu().numpy(), g[key])
+
+
+@pytest.mark.parametrize("n", [1, 3, 4, 5, 1000, 4099])
+def test_map2tod_ragged_lengths_f32_f64(K, n):
+    rng = np.random.default_rng(n)
+    npix = 97
+    ipix = rng.integers(0, npix, size=(1, n)).astype(np.int32)
+    for dt, tdt in ((np.float64, torch.float64), (np.float32, torch.float32)):
+        m = rng.standard_normal(npix).astype(dt)
+        d0 = rng.standard_normal((1, n)).astype(dt)
+        ref = d0.copy()
+        oracle.map2tod(ref, m, ipix, True)
+        d = dev(d0)
+        K.map2tod(d, dev(m), dev(ipix), True)
+        assert np.array_equal(d.cpu().numpy(), ref)
+
+
+def test_map2tod_unaligned_view(K):
+    # a view starting one element in: not 16-byte aligned -> scalar kernel
+    rng = np.random.default_rng(5)
+    ipix = rng.integers(0, 50, size=1001).astype(np.int32)
+    m = rng.standard_normal(50)
+    base = torch.zeros(1002, dtype=torch.float64, device=cuda)
+    d = base[1:]
+    ip = dev(np.concatenate([[0], ipix]).astype(np.int32))[1:]
+    K.map2tod(d, dev(m), ip, False)
+    assert np.array_equal(d.cpu().numpy(), m[ipix])
+
+
+def test_tod2map_golden(K, gold):
+    g = gold("proj.npz")
+    m = dev(g["map"])
+    K.tod2map(m, dev(g["dat"]), dev(g["ipix"]))
+    assert rel(m.cpu().numpy(), g["tod2map_omp"]) < 1e-13
+
+
+def test_tod2map_sorted_is_deterministic(K, gold):
+    g = gold("proj.npz")
+    ip = dev(g["ipix"])
+    plan = K.PixPlan(ip, g["map"].size)
+    outs = []
+    for _ in range(2):
+        m = dev(g["map"])
+        plan.tod2map(m, dev(g["dat"]))
+        outs.append(m.cpu().numpy())
+    assert np.array_equal(outs[0], outs[1])
+    assert rel(outs[0], g["tod2map_omp"]) < 1e-13
+
+
+def test_tod2map_large_runs_f64_f32(K):
+    rng = np.random.default_rng(2)
+    ndet, ndata, npix = 16, 200_003, 64 * 64
+    # slowly moving pointing -> long runs of equal pixels, plus jumps
+    walk = np.cumsum(rng.integers(-1, 2, size=(ndet, ndata)), axis=1) // 5
+    ipix = np.mod(walk + rng.integers(0, npix, size=(ndet, 1)), npix).astype(np.int32)
+    dat = rng.standard_normal((ndet, ndata))
+    ref = np.zeros(npix)
+    oracle.tod2map(ref, dat, ipix)
+    m = torch.zeros(npix, dtype=torch.float64, device=cuda)
+    K.tod2map(m, dev(dat), dev(ipix))
+    assert rel(m.cpu().numpy(), ref) < 1e-12
+    m32 = torch.zeros(npix, dtype=torch.float32, device=cuda)
+    K.tod2map(m32, dev(dat, torch.float32), dev(ipix))
+    assert rel(m32.cpu().numpy(), ref) < 2e-5
+    plan = K.PixPlan(dev(ipix), npix)
+    ms = torch.zeros(npix, dtype=torch.float64, device=cuda)
+    plan.tod2map(ms, dev(dat))
+    assert rel(ms.cpu().numpy(), ref) < 1e-12
+
+
+def test_tod2map_rows_hits(K, gold):
+    g = gold("solve.npz")
+    hits = torch.zeros(int(g["nx"]) * int(g["ny"]), dtype=torch.float64, device=cuda)
+    for k in range(int(g["ntod"])):
+        K.tod2map_rows(hits, dev(g[f"t{k}_ipix"]))
+    assert np.array_equal(hits.cpu().numpy().reshape(g["hits"].shape), g["hits"])
+
+
+def test_check_pix_counts_out_of_range(K):
+    ip = np.array([0, 5, -1, 9, 10, 3], dtype=np.int32)
+    assert K.check_pix(dev(ip), 10) == 2
+    with pytest.raises(Exception):
+        K.PixPlan(dev(ip), 10)
+
+
+# ---------------------------------------------------------------- DCT / noise
+def test_dct1_golden_f64(K, gold):
+    g = gold("dct.npz")
+    i = 0
+    while f"x{i}" in g:
+        x = g[f"x{i}"]
+        y = K.DCT1(x.shape[0], x.shape[1], torch.float64)(dev(x)).cpu().numpy()
+        assert rel(y, g[f"y{i}"]) < 1e-13, i
+        i += 1
+
+
+def test_dct1_f32_and_roundtrip(K):
+    x = np.random.default_rng(3).standard_normal((7, 4097))
+    d = K.DCT1(7, 4097, torch.float32)
+    y = d(dev(x, torch.float32))
+    assert rel(y.cpu().numpy(), oracle.dct1(x)) < 2e-6
+    back = d(y).cpu().numpy() / (2 * 4096)
+    assert rel(back, x) < 2e-6
+
+
+def test_apply_noise_golden_f64(K, gold):
+    g = gold("noise.npz")
+    v, vT, w = dev(g["v"]), dev(g["vT"]), dev(g["mywt"])
+    for key_x, key_dd in (("x", "dd"), ("x_short", "dd_short")):
+        x = g[key_x]
+        plan = K.NoisePlan(x.shape[0], x.shape[1], torch.float64)
+        dd = plan.apply(v, vT, w, dev(x)).cpu().numpy()
+        assert rel(dd, g[key_dd]) < 1e-12, key_x
+    # in place (out aliases dat)
+    x = dev(g["x"])
+    plan = K.NoisePlan(x.shape[0], x.shape[1], torch.float64)
+    plan.apply(v, vT, w, x, out=x)
+    assert rel(x.cpu().numpy(), g["dd"]) < 1e-12
+
+
+def test_apply_noise_prewhitened_by_folding(K, gold):
+    g = gold("noise.npz")
+    nv = g["pw_noisevec"]
+    v = g["pw_v"] / nv[None, :]
+    vT = g["pw_vT"] / nv[:, None]
+    x = g["x"]
+    plan = K.NoisePlan(x.shape[0], x.shape[1], torch.float64)
+    dd = plan.apply(dev(v), dev(vT), dev(g["pw_mywt"]), dev(x)).cpu().numpy()
+    assert rel(dd, g["pw_dd"]) < 1e-12
+
+
+def test_apply_noise_f32_close_to_f64(K, gold):
+    g = gold("noise.npz")
+    x = g["x"]
+    plan = K.NoisePlan(x.shape[0], x.shape[1], torch.float32)
+    dd = plan.apply(dev(g["v"], torch.float32), dev(g["vT"], torch.float32),
+                    dev(g["mywt"], torch.float32), dev(x, torch.float32), rot_mode=1).cpu().numpy()
+    assert rel(dd, g["dd"]) < 1e-5
+
+
+# ---------------------------------------------------------------- map algebra / PCG
+def test_dot_is_fp64_and_reproducible(K):
+    rng = np.random.default_rng(4)
+    a, b = rng.standard_normal(1_000_003), rng.standard_normal(1_000_003)
+    R = K.Reducer()
+    r1 = R.dot(dev(a), dev(b)).item()
+    r2 = R.dot(dev(a), dev(b)).item()
+    assert r1 == r2
+    assert abs(r1 - float(np.dot(a, b))) < 1e-10 * np.abs(a * b).sum()
+    r32 = R.dot(dev(a, torch.float32), dev(b, torch.float32)).item()
+    exact32 = float(np.dot(a.astype(np.float32).astype(np.float64), b.astype(np.float32).astype(np.float64)))
+    assert abs(r32 - exact32) < 1e-10 * np.abs(a * b).sum()
+
+
+def test_pcg_recurrence_matches_reference(K, gold):
+    g = gold("solve.npz")
+    tods = [oracle.OracleTod(ipix=g[f"t{k}_ipix"], v=g[f"t{k}_v"], vT=g[f"t{k}_vT"],
+                             mywt=g[f"t{k}_mywt"], dat=g[f"t{k}_dat"]) for k in range(int(g["ntod"]))]
+    shape = (int(g["nx"]), int(g["ny"]))
+    plans = [K.NoisePlan(t.ipix.shape[0], t.ipix.shape[1], torch.float64) for t in tods]
+    dt = [(dev(t.ipix), dev(t.v), dev(t.vT), dev(t.mywt)) for t in tods]
+
+    def A(x):
+        out = torch.zeros_like(x)
+        for (ip, v, vT, w), pl in zip(dt, plans):
+            tmp = torch.empty(ip.shape, dtype=x.dtype, device=cuda)
+            K.map2tod(tmp, x, ip, False)
+            pl.apply(v, vT, w, tmp, out=tmp)
+            K.tod2map(out, tmp, ip)
+        return out
+
+    ax = A(dev(g["xr"])).cpu().numpy()
+    assert rel(ax, g["Axr"]) < 1e-12
+    b = dev(g["rhs"])
+    M = dev(g["precon"])
+    x = torch.zeros_like(b)
+    r, z, p = torch.empty_like(b), torch.empty_like(b), torch.empty_like(b)
+    s = torch.zeros(8, dtype=torch.float64, device=cuda)
+    R = K.Reducer()
+    K.pcg_init(r, z, p, b, A(x), M, s, R)
+    for _ in range(8):
+        K.pcg_update(x, r, z, p, A(p), M, s, R)
+    assert s[6].item() == 0.0 and s[7].item() == 8.0
+    assert rel(x.cpu().numpy(), g["pcg8"]) < 1e-9
