@@ -156,6 +156,19 @@ int mk_apply_noise(mk_noise_plan *plan, const void *v, const void *vT, const voi
                    int64_t mywt_ld, const void *dat, void *out, int rot_mode, void *stream);
 int mk_noise_plan_destroy(mk_noise_plan *plan);
 
+/* The detector rotation alone, R = A . X, for the plan's (ndet, ndata):
+ * A (ndet, ndet), X and R (ndet, ndata), dtype-typed, R must not alias X.
+ * rot_mode as for mk_apply_noise.  Same GEMM as np.dot(self.v, dat),
+ * minkasi/mapmaking/noise.py:704. */
+int mk_rotate(mk_noise_plan *plan, const void *A, const void *X, void *R, int rot_mode,
+              void *stream);
+
+/* Device status of the plan's tensor-core kernels: *code = 1 if one of
+ * their bounded waits timed out since the last call (the kernel then stops,
+ * frees its tensor memory and leaves its output incomplete), else 0.  Reads
+ * and clears the word; synchronises `stream`. */
+int mk_noise_status(mk_noise_plan *plan, int *code, void *stream);
+
 /* ---- map-space vector algebra and the PCG recurrence ------------------- */
 
 /* *result (DEVICE double) = sum_i a[i]*b[i], accumulated in FP64 with a
@@ -192,6 +205,37 @@ int mk_pcg_update(void *x, void *r, void *z, void *p, const void *Ap, const void
 int mk_pcg_init(void *r, void *z, void *p, const void *b, const void *Ax,
                 const void *precon, int64_t n, int dtype, double *s, void *scratch,
                 void *stream);
+
+/* Split form of mk_pcg_update for an operator preconditioner z = M(r)
+ * (e.g. the learned SPD convolutional preconditioner) computed between the
+ * two calls:  mk_pcg_step_xr: pAp, alpha, x += alpha p, r += (-alpha) Ap,
+ * s[MK_S_RR] = r.r;  then the caller computes z = M(r);  mk_pcg_step_zp:
+ * zr' = r.z, beta = zr'/zr, p = z + beta p.  Same recurrence as
+ * minkasi/mapmaking/pcg.py:137-171 with `precon * r` generalised to M(r). */
+int mk_pcg_step_xr(void *x, void *r, const void *p, const void *Ap, int64_t n, int dtype,
+                   double *s, void *scratch, void *stream);
+int mk_pcg_step_zp(const void *z, const void *r, void *p, int64_t n, int dtype, double *s,
+                   void *scratch, void *stream);
+
+/* out = d * (a + b) elementwise (b may be NULL); dtype-typed maps. */
+int mk_scale_add(void *out, const void *d, const void *a, const void *b, int64_t n, int dtype,
+                 void *stream);
+
+/* ---- learned preconditioner: 3x3 convolutions (no reference counterpart;
+ * they implement the SPD map-space preconditioner M = D^-1/2 (I + K^T K) D^-1/2
+ * that replaces the elementwise `precon * r` of minkasi/mapmaking/pcg.py:157-158)
+ * Layout [B][C][H][W] float32, 1 <= C <= 16, zero padding, w [Cout][Cin][3][3].
+ *   fwd : y[b,co,p] = sum_{ci,d} w[co,ci,d] x[b,ci,p+d]
+ *   adj : x[b,ci,q] = sum_{co,d} w[co,ci,d] y[b,co,q-d]   (exact adjoint of fwd)
+ *   wgrad: g[co,ci,d] = sum_{b,p} h[b,co,p] x[b,ci,p+d]   (reproducible order)
+ */
+int mk_conv3x3_fwd(const float *x, const float *w, float *y, int B, int Cin, int Cout, int H,
+                   int W, void *stream);
+int mk_conv3x3_adj(const float *y, const float *w, float *x, int B, int Cin, int Cout, int H,
+                   int W, void *stream);
+size_t mk_conv3x3_wgrad_scratch_bytes(int B, int Cin, int Cout, int H, int W);
+int mk_conv3x3_wgrad(const float *x, const float *h, float *g, int B, int Cin, int Cout, int H,
+                     int W, void *scratch, size_t scratch_bytes, void *stream);
 
 #ifdef __cplusplus
 }

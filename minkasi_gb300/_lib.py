@@ -51,12 +51,21 @@ SIGNATURES = {
     "mk_noise_plan_create": (_i32, [_pp, _i64, _i64, _i32, _vp, _sz]),
     "mk_apply_noise": (_i32, [_vp, _vp, _vp, _vp, _i64, _vp, _vp, _i32, _vp]),
     "mk_noise_plan_destroy": (_i32, [_vp]),
+    "mk_rotate": (_i32, [_vp, _vp, _vp, _vp, _i32, _vp]),
+    "mk_noise_status": (_i32, [_vp, ctypes.POINTER(ctypes.c_int), _vp]),
     "mk_reduce_scratch_bytes": (_sz, []),
     "mk_dot": (_i32, [_vp, _vp, _i64, _i32, _vp, _vp, _vp]),
     "mk_axpy": (_i32, [_vp, _vp, ctypes.c_double, _i64, _i32, _vp]),
     "mk_mul": (_i32, [_vp, _vp, _vp, _i64, _i32, _vp]),
     "mk_pcg_update": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp]),
     "mk_pcg_init": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp]),
+    "mk_pcg_step_xr": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp]),
+    "mk_pcg_step_zp": (_i32, [_vp, _vp, _vp, _i64, _i32, _vp, _vp, _vp]),
+    "mk_scale_add": (_i32, [_vp, _vp, _vp, _vp, _i64, _i32, _vp]),
+    "mk_conv3x3_fwd": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp]),
+    "mk_conv3x3_adj": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp]),
+    "mk_conv3x3_wgrad_scratch_bytes": (_sz, [_i32, _i32, _i32, _i32, _i32]),
+    "mk_conv3x3_wgrad": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp, _sz, _vp]),
 }
 
 _lib: Optional[ctypes.CDLL] = None
@@ -83,7 +92,7 @@ def load(path: Optional[str] = None) -> ctypes.CDLL:
         except OSError as e:  # pragma: no cover - depends on the machine
             errors.append(f"{cand}: {e}")
     if h is None:
-        raise OSError("libmkgpu.so not found; build it with `python -m minkasi_gb300.build` "
+        raise OSError("libmkgpu.so not found; build it with `python minkasi_gb300/build.py` "
                       "(or __graft_entry__.build()).\n" + "\n".join(errors))
     for name, (res, args) in SIGNATURES.items():
         fn = getattr(h, name)

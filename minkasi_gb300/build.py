@@ -1,7 +1,7 @@
 """Build libmkgpu.so in-tree for sm_103a (GB300).
 
-    python -m minkasi_gb300.build          # incremental
-    python -m minkasi_gb300.build --force
+    python minkasi_gb300/build.py          # incremental
+    python minkasi_gb300/build.py --force
 
 Each .cu under csrc/ is compiled by its own nvcc process (in parallel) into
 _build/, then linked with cuFFT and cuBLAS into minkasi_gb300/libmkgpu.so.

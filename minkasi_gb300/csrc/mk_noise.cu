@@ -135,7 +135,16 @@ struct DctCore {
   int dtype = MK_F64;
   void *E = nullptr, *F = nullptr, *work = nullptr;
   size_t work_bytes = 0;
+  // tensor-core rotation scratch (FP32 plans): status word, then operand image
+  int *tc_err = nullptr;
+  void *tc_bimg = nullptr;
 };
+
+// workspace bytes of the tensor-core rotation scratch: 256 B status + image
+size_t tc_bytes(int64_t nrow, int dtype) {
+  if (dtype != MK_F32 || !mk::rot_tc_supported(nrow)) return 0;
+  return 256 + ((mk::rot_tc_bimg_bytes(nrow) + 255) / 256) * 256;
+}
 
 size_t elt(int dtype) { return dtype == MK_F64 ? 8 : 4; }
 
@@ -169,7 +178,7 @@ int core_bytes(int64_t nrow, int64_t n, int dtype, size_t *bytes) {
   if (rc) return rc;
   cufftDestroy(h);
   *bytes = align_up((size_t)nrow * N * elt(dtype)) + align_up((size_t)nrow * n * 2 * elt(dtype)) +
-           align_up(work);
+           align_up(work) + tc_bytes(nrow, dtype);
   return MK_OK;
 }
 
@@ -191,6 +200,17 @@ int core_create(DctCore *c, int64_t nrow, int64_t n, int dtype, void *ws, size_t
   c->work = p;
   rc = make_fft(&c->fft, nrow, c->N, dtype, &c->work_bytes);
   if (rc) return rc;
+  if (tc_bytes(nrow, dtype)) {
+    char *q = (char *)c->work + align_up(c->work_bytes);
+    c->tc_err = (int *)q;
+    c->tc_bimg = q + 256;
+    cudaError_t e = cudaMemset(c->tc_err, 0, sizeof(int));
+    if (e != cudaSuccess) {
+      cufftDestroy(c->fft);
+      mk::set_error("workspace status init failed: %s", cudaGetErrorString(e));
+      return MK_ERR_CUDA;
+    }
+  }
   c->have_fft = true;
   cufftResult r = cufftSetWorkArea(c->fft, c->work);
   if (r != CUFFT_SUCCESS) {
@@ -280,12 +300,17 @@ int blas_rotate(int dtype, const void *A, const void *X, int64_t ldx, void *R, i
   return MK_OK;
 }
 
-int rotate(int dtype, int mode, const void *A, const void *X, int64_t ldx, void *R, int64_t ldr,
+// mode 0 (automatic) means cuBLAS here; the host autotuner picks 2 or 3 per
+// workload after checking their accuracy against it.
+int rotate(DctCore *c, int mode, const void *A, const void *X, int64_t ldx, void *R, int64_t ldr,
            int64_t nrow, int64_t ncol, cudaStream_t st) {
-  if (mode == 0) mode = (dtype == MK_F32 && mk::rot_tc_supported(nrow)) ? 2 : 1;
+  const int dtype = c->dtype;
+  if (mode == 0) mode = 1;
   if (mode == 2) {
     MK_CHECK_ARG(dtype == MK_F32, "tensor-core rotation (rot_mode 2) is FP32 only");
-    return mk::rot_tc_f32((const float *)A, (const float *)X, ldx, (float *)R, ldr, nrow, ncol, st);
+    MK_CHECK_ARG(c->tc_bimg != nullptr, "tensor-core rotation needs ndet in {32,64,128,256}");
+    return mk::rot_tc_f32((const float *)A, (const float *)X, ldx, (float *)R, ldr, nrow, ncol,
+                          c->tc_bimg, c->tc_err, st);
   }
   MK_CHECK_ARG(mode == 1 || mode == 3, "bad rot_mode %d", mode);
   return blas_rotate(dtype, A, X, ldx, R, ldr, nrow, ncol, mode == 3, st);
@@ -296,7 +321,7 @@ int apply_noise_t(DctCore *c, const T *v, const T *vT, const T *w, int64_t ldw, 
                   T *out, int rot_mode, cudaStream_t st) {
   const int64_t n = c->n, N = c->N, nd = c->nrow;
   dim3 g = rows_grid(n, nd);
-  int rc = rotate(c->dtype, rot_mode, v, dat, n, c->E, N, nd, n, st);
+  int rc = rotate(c, rot_mode, v, dat, n, c->E, N, nd, n, st);
   if (rc) return rc;
   k_mirror<T><<<g, 256, 0, st>>>((T *)c->E, n, N, nd);
   if ((rc = mk::launch_status("apply_noise/mirror"))) return rc;
@@ -306,7 +331,7 @@ int apply_noise_t(DctCore *c, const T *v, const T *vT, const T *w, int64_t ldw, 
   if ((rc = core_fft(c, st))) return rc;
   k_real_halve<T, C><<<g, 256, 0, st>>>((const C *)c->F, (T *)c->E, n, nd);
   if ((rc = mk::launch_status("apply_noise/halve"))) return rc;
-  return rotate(c->dtype, rot_mode, vT, c->E, n, out, n, nd, n, st);
+  return rotate(c, rot_mode, vT, c->E, n, out, n, nd, n, st);
 }
 
 }  // namespace
@@ -391,5 +416,24 @@ extern "C" int mk_noise_plan_destroy(mk_noise_plan *plan) {
   if (!plan) return MK_OK;
   if (plan->core.have_fft) cufftDestroy(plan->core.fft);
   delete plan;
+  return MK_OK;
+}
+
+extern "C" int mk_rotate(mk_noise_plan *plan, const void *A, const void *X, void *R, int rot_mode,
+                         void *stream) {
+  MK_CHECK_ARG(plan && A && X && R, "mk_rotate: null pointer");
+  MK_CHECK_ARG(X != R, "mk_rotate: R must not alias X");
+  const int64_t nd = plan->core.nrow, n = plan->core.n;
+  return rotate(&plan->core, rot_mode, A, X, n, R, n, nd, n, mk::as_stream(stream));
+}
+
+extern "C" int mk_noise_status(mk_noise_plan *plan, int *code, void *stream) {
+  MK_CHECK_ARG(plan && code, "mk_noise_status: null pointer");
+  *code = 0;
+  if (!plan->core.tc_err) return MK_OK;
+  cudaStream_t st = mk::as_stream(stream);
+  MK_CUDA(cudaMemcpyAsync(code, plan->core.tc_err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  MK_CUDA(cudaMemsetAsync(plan->core.tc_err, 0, sizeof(int), st));
+  MK_CUDA(cudaStreamSynchronize(st));
   return MK_OK;
 }

@@ -180,6 +180,55 @@ __global__ void k_pcg_p(T *__restrict__ p, const T *__restrict__ z, int64_t n, c
     p[i] = (T)__dadd_rn((double)z[i], __dmul_rn(beta, (double)p[i]));
 }
 
+// Split update for an operator preconditioner z = M(r) computed between the
+// two halves:  (1) x += alpha p; r += (-alpha) Ap; rr = r.r
+template <typename T>
+__global__ void __launch_bounds__(RB) k_pcg_xr(T *__restrict__ x, T *__restrict__ r, const T *__restrict__ p,
+                                               const T *__restrict__ Ap, int64_t n, double *s, Scratch *sc) {
+  const bool stop = s[MK_S_FLAG] != 0.0;
+  const double alpha = s[MK_S_ALPHA];
+  double acc[1] = {0.0};
+  if (!stop) {
+    for (int64_t i = (int64_t)blockIdx.x * RB + threadIdx.x; i < n; i += (int64_t)gridDim.x * RB) {
+      x[i] = (T)__dadd_rn((double)x[i], __dmul_rn(alpha, (double)p[i]));
+      T ri = (T)__dadd_rn((double)r[i], __dmul_rn(-alpha, (double)Ap[i]));
+      r[i] = ri;
+      acc[0] = __dadd_rn(acc[0], __dmul_rn((double)ri, (double)ri));
+    }
+  }
+  double tot[1];
+  if (finish_reduce<1>(acc, sc, tot) && threadIdx.x == 0 && !stop) s[MK_S_RR] = tot[0];
+}
+
+// (2) zr' = r.z; beta = zr'/zr; zr = zr'; iteration count += 1
+template <typename T>
+__global__ void __launch_bounds__(RB) k_pcg_zr(const T *__restrict__ r, const T *__restrict__ z, int64_t n,
+                                               double *s, Scratch *sc) {
+  const bool stop = s[MK_S_FLAG] != 0.0;
+  double acc[1] = {0.0};
+  if (!stop)
+    for (int64_t i = (int64_t)blockIdx.x * RB + threadIdx.x; i < n; i += (int64_t)gridDim.x * RB)
+      acc[0] = __dadd_rn(acc[0], __dmul_rn((double)r[i], (double)z[i]));
+  double tot[1];
+  if (finish_reduce<1>(acc, sc, tot) && threadIdx.x == 0 && !stop) {
+    double beta = tot[0] / s[MK_S_ZR];
+    s[MK_S_ZRNEW] = tot[0];
+    s[MK_S_BETA] = beta;
+    s[MK_S_ZR] = tot[0];
+    s[MK_S_ITER] += 1.0;
+    if (!finite(beta) || !(tot[0] > 0.0)) s[MK_S_FLAG] = 1.0;
+  }
+}
+
+// out = d * (a + b)
+template <typename T>
+__global__ void k_scale_add(T *__restrict__ out, const T *__restrict__ d, const T *__restrict__ a,
+                            const T *__restrict__ b, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = d[i] * (a[i] + (b ? b[i] : T(0)));
+}
+
 template <typename T>
 int pcg_update_t(T *x, T *r, T *z, T *p, const T *Ap, const T *M, int64_t n, double *s,
                  Scratch *sc, cudaStream_t st) {
@@ -262,4 +311,53 @@ extern "C" int mk_pcg_update(void *x, void *r, void *z, void *p, const void *Ap,
                                 (Scratch *)scratch, st);
   return pcg_update_t<float>((float *)x, (float *)r, (float *)z, (float *)p, (const float *)Ap,
                              (const float *)precon, n, s, (Scratch *)scratch, st);
+}
+
+extern "C" int mk_pcg_step_xr(void *x, void *r, const void *p, const void *Ap, int64_t n, int dtype,
+                              double *s, void *scratch, void *stream) {
+  MK_CHECK_ARG(MK_DTYPE_OK(dtype), "mk_pcg_step_xr: bad dtype %d", dtype);
+  MK_CHECK_ARG(n >= 1 && x && r && p && Ap && s && scratch, "mk_pcg_step_xr: bad argument");
+  cudaStream_t st = mk::as_stream(stream);
+  unsigned g = red_grid(n);
+  if (dtype == MK_F64) {
+    k_pcg_pap<double><<<g, RB, 0, st>>>((const double *)p, (const double *)Ap, n, s, (Scratch *)scratch);
+    k_pcg_xr<double><<<g, RB, 0, st>>>((double *)x, (double *)r, (const double *)p, (const double *)Ap, n,
+                                       s, (Scratch *)scratch);
+  } else {
+    k_pcg_pap<float><<<g, RB, 0, st>>>((const float *)p, (const float *)Ap, n, s, (Scratch *)scratch);
+    k_pcg_xr<float><<<g, RB, 0, st>>>((float *)x, (float *)r, (const float *)p, (const float *)Ap, n, s,
+                                      (Scratch *)scratch);
+  }
+  return mk::launch_status("mk_pcg_step_xr");
+}
+
+extern "C" int mk_pcg_step_zp(const void *z, const void *r, void *p, int64_t n, int dtype, double *s,
+                              void *scratch, void *stream) {
+  MK_CHECK_ARG(MK_DTYPE_OK(dtype), "mk_pcg_step_zp: bad dtype %d", dtype);
+  MK_CHECK_ARG(n >= 1 && z && r && p && s && scratch, "mk_pcg_step_zp: bad argument");
+  cudaStream_t st = mk::as_stream(stream);
+  unsigned g = red_grid(n);
+  if (dtype == MK_F64) {
+    k_pcg_zr<double><<<g, RB, 0, st>>>((const double *)r, (const double *)z, n, s, (Scratch *)scratch);
+    k_pcg_p<double><<<mk_grid(n, 256, 8), 256, 0, st>>>((double *)p, (const double *)z, n, s);
+  } else {
+    k_pcg_zr<float><<<g, RB, 0, st>>>((const float *)r, (const float *)z, n, s, (Scratch *)scratch);
+    k_pcg_p<float><<<mk_grid(n, 256, 8), 256, 0, st>>>((float *)p, (const float *)z, n, s);
+  }
+  return mk::launch_status("mk_pcg_step_zp");
+}
+
+extern "C" int mk_scale_add(void *out, const void *d, const void *a, const void *b, int64_t n, int dtype,
+                            void *stream) {
+  MK_CHECK_ARG(MK_DTYPE_OK(dtype), "mk_scale_add: bad dtype %d", dtype);
+  if (n <= 0) return MK_OK;
+  MK_CHECK_ARG(out && d && a, "mk_scale_add: null pointer");
+  cudaStream_t st = mk::as_stream(stream);
+  if (dtype == MK_F64)
+    k_scale_add<double><<<mk_grid(n, 256, 8), 256, 0, st>>>((double *)out, (const double *)d,
+                                                            (const double *)a, (const double *)b, n);
+  else
+    k_scale_add<float><<<mk_grid(n, 256, 8), 256, 0, st>>>((float *)out, (const float *)d,
+                                                           (const float *)a, (const float *)b, n);
+  return mk::launch_status("mk_scale_add");
 }

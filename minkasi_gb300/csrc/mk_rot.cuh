@@ -4,11 +4,15 @@
 // row-major.  Used by apply_noise for the v / vT rotations.
 #pragma once
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 
 namespace mk {
 // true when the tensor-core kernel handles this detector count
 bool rot_tc_supported(int64_t nrow);
+// bytes of the operand image the kernel stages A from (16-byte aligned buffer)
+size_t rot_tc_bimg_bytes(int64_t nrow);
+// `err` is a device int set to 1 if a bounded wait inside the kernel timed out
 int rot_tc_f32(const float *A, const float *X, int64_t ldx, float *R, int64_t ldr, int64_t nrow,
-               int64_t ncol, cudaStream_t st);
+               int64_t ncol, void *bimg, int *err, cudaStream_t st);
 }  // namespace mk

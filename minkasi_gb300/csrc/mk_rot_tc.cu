@@ -1,12 +1,314 @@
-// Tensor-core rotation (placeholder until the tcgen05 kernel lands).
+// Detector rotation R = A . X on the 5th-generation tensor cores
+// (tcgen05.mma kind::tf32), FP32 in / FP32 out, 3xTF32 split precision:
+//   A = Ah + Al, X = Xh + Xl (h = round-to-TF32, l = remainder, also TF32)
+//   R ~= Xh.Ah + Xl.Ah + Xh.Al   accumulated in FP32 in tensor memory.
+// The dropped Xl.Al term is ~2^-22 relative, so the result carries FP32-level
+// accuracy (the apply_noise rotations np.dot(v, dat), np.dot(vT, .) of
+// minkasi/mapmaking/noise.py:704,709).
+//
+// Tile mapping (all operands K-major, 128-byte swizzle):
+//   D^T (128 samples x ndet) = X^T (128 samples x K=ndet) . A^T (K x N=ndet)
+//   MMA A-operand: the X^T tile.  Each thread owns one sample row; it loads
+//     its 32 detector values of a K-chunk (coalesced across the warp: 32
+//     consecutive samples of one detector row), splits them, and writes the
+//     hi and lo rows (128 B each) into shared memory.
+//   MMA B-operand: rows j = output detector, K contiguous = A[j][k0..k0+31],
+//     i.e. A row-major.  Its hi/lo split is built once per call by k_bprep
+//     in exactly the shared-memory image and bulk-copied (cp.async.bulk)
+//     per K-chunk, completing on an mbarrier.
+//   Accumulator: 128 TMEM lanes (= samples) x ndet columns (= detectors).
+//   Epilogue: each warp reads its 32 lanes with tcgen05.ld 32x32b and
+//     stores, per detector column, 32 consecutive samples (128 B, coalesced).
+// Pipeline: 2 shared-memory stages; the MMAs of chunk g run while the
+// threads split chunk g+1.  One elected thread issues the MMAs and the bulk
+// copies.  Every mbarrier wait is bounded: on timeout the CTA records an
+// error code, waits (bounded) for its outstanding MMAs, frees its tensor
+// memory and returns.
 #include "mk_common.cuh"
 #include "mk_rot.cuh"
 
-namespace mk {
-bool rot_tc_supported(int64_t) { return false; }
-int rot_tc_f32(const float *, const float *, int64_t, float *, int64_t, int64_t, int64_t,
-               cudaStream_t) {
-  set_error("tensor-core rotation is not available in this build");
-  return MK_ERR_ARG;
+namespace {
+
+constexpr int TILE_M = 128;      // samples per tile (MMA M)
+constexpr int KC = 32;           // K per chunk: one 128-byte swizzle row of tf32
+constexpr int NSTAGE = 2;
+constexpr int NTHREADS = 128;
+constexpr uint32_t SPIN_LIMIT = 1u << 24;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
 }
+
+__device__ __forceinline__ float tf32_round(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+// byte offset of element (row, k) in a K-major, 128B-swizzled tile whose
+// rows hold 32 fp32 (one swizzle row each); 8-row groups are 1024 B apart.
+__host__ __device__ __forceinline__ uint32_t sw128_off(uint32_t row, uint32_t k) {
+  return (row >> 3) * 1024u + (row & 7u) * 128u + ((((k >> 2) ^ (row & 7u)) & 7u) << 4) + (k & 3u) * 4u;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait; false on timeout
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  for (uint32_t i = 0; i < SPIN_LIMIT; i++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// shared-memory matrix descriptor: K-major, SWIZZLE_128B, 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);          // start address
+  d |= (uint64_t)1 << 16;                              // leading byte offset (unused for SW128 K-major)
+  d |= (uint64_t)(1024u >> 4) << 32;                   // stride byte offset
+  d |= (uint64_t)1 << 46;                              // descriptor version (tcgen05)
+  d |= (uint64_t)2 << 61;                              // swizzle: 128B
+  return d;
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+        "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+        "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// B-operand image in global memory: for each K-chunk c, the hi tile then the
+// lo tile, each ndet rows x 32 k in the swizzled layout above.
+__global__ void k_bprep(const float *__restrict__ A, int ndet, char *__restrict__ img) {
+  const int nchunk = ndet / KC;
+  const size_t tile = (size_t)ndet * 128;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < ndet * ndet; idx += gridDim.x * blockDim.x) {
+    int j = idx / ndet, k = idx % ndet;
+    int c = k / KC, kk = k % KC;
+    float a = A[(size_t)j * ndet + k];
+    float h = tf32_round(a);
+    float l = tf32_round(a - h);
+    char *base = img + (size_t)c * 2 * tile;
+    *(float *)(base + sw128_off(j, kk)) = h;
+    *(float *)(base + tile + sw128_off(j, kk)) = l;
+  }
+  (void)nchunk;
+}
+
+// shared memory: [stage][Ahi 16KB | Alo 16KB | Bhi ndet*128 | Blo ndet*128], 1024-aligned
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_rot_tc(const float *__restrict__ X, int64_t ldx, float *__restrict__ R, int64_t ldr, int ndet,
+             int64_t ncol, const char *__restrict__ bimg, int *__restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const uint32_t a_bytes = TILE_M * 128;          // 16 KB
+  const uint32_t b_bytes = (uint32_t)ndet * 128;  // per hi or lo tile
+  const uint32_t stage_bytes = 2 * a_bytes + 2 * b_bytes;
+  __shared__ uint64_t bar_b[NSTAGE], bar_mma[NSTAGE];
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ int abort_sh;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nchunk = ndet / KC;
+  const uint32_t ncols = ndet < 32 ? 32u : (uint32_t)ndet;  // power of two by construction
+  const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(ndet >> 3) << 17) |
+                         ((uint32_t)(TILE_M >> 4) << 24);
+
+  if (tid == 0) {
+    for (int s = 0; s < NSTAGE; s++) {
+      mbar_init(&bar_b[s], 1);
+      mbar_init(&bar_mma[s], 1);
+    }
+    abort_sh = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base_sh)),
+                 "r"(ncols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_base_sh;
+
+  // Control flow is CTA-uniform: only thread 0 waits on mbarriers; the
+  // outcome reaches the other threads through abort_sh and __syncthreads.
+  const int64_t ntile = (ncol + TILE_M - 1) / TILE_M;
+  uint32_t g = 0;  // chunks issued by this CTA so far
+  for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
+    const int64_t n0 = tile * TILE_M;
+    const int64_t my = n0 + tid;
+    for (int c = 0; c < nchunk; c++, g++) {
+      const uint32_t s = g % NSTAGE, use = g / NSTAGE;
+      unsigned char *st = smem + s * stage_bytes;
+      // this thread's sample row: 32 detectors of chunk c, split into hi / lo
+      // (global loads issued before the stage wait so their latency overlaps it)
+      float h[KC], l[KC];
+#pragma unroll
+      for (int kk = 0; kk < KC; kk++) {
+        float x = (my < ncol) ? __ldcs(X + (int64_t)(c * KC + kk) * ldx + my) : 0.f;
+        h[kk] = tf32_round(x);
+        l[kk] = tf32_round(x - h[kk]);
+      }
+      if (tid == 0) {
+        // stage s is free once the MMAs of chunk g-2 have completed
+        if (g >= NSTAGE && !mbar_wait(&bar_mma[s], (use - 1) & 1)) {
+          abort_sh = 1;
+        } else {
+          mbar_expect_tx(&bar_b[s], 2 * b_bytes);
+          bulk_g2s(st + 2 * a_bytes, bimg + (size_t)c * 2 * b_bytes, 2 * b_bytes, &bar_b[s]);
+        }
+      }
+      __syncthreads();
+      if (abort_sh) break;
+      unsigned char *ah = st, *al = st + a_bytes;
+#pragma unroll
+      for (int q = 0; q < KC / 4; q++) {
+        uint32_t off = sw128_off(tid, 4 * q);
+        *(float4 *)(ah + off) = make_float4(h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
+        *(float4 *)(al + off) = make_float4(l[4 * q], l[4 * q + 1], l[4 * q + 2], l[4 * q + 3]);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncthreads();
+      if (tid == 0) {
+        if (!mbar_wait(&bar_b[s], use & 1)) {
+          abort_sh = 1;  // seen by everyone at the next __syncthreads
+        } else {
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const uint32_t sa_h = smem_u32(ah), sa_l = smem_u32(al);
+          const uint32_t sb_h = smem_u32(st + 2 * a_bytes), sb_l = sb_h + b_bytes;
+#pragma unroll
+          for (int k8 = 0; k8 < KC / 8; k8++) {
+            const uint32_t ko = k8 * 32;  // 8 tf32 = 32 bytes along K
+            const uint32_t acc0 = (c == 0 && k8 == 0) ? 0u : 1u;
+            mma_tf32(tmem, sdesc(sa_h + ko), sdesc(sb_h + ko), idesc, acc0);
+            mma_tf32(tmem, sdesc(sa_l + ko), sdesc(sb_h + ko), idesc, 1u);
+            mma_tf32(tmem, sdesc(sa_h + ko), sdesc(sb_l + ko), idesc, 1u);
+          }
+          mma_commit(&bar_mma[s]);
+        }
+      }
+    }
+    // epilogue: wait for the tile's last chunk, TMEM -> registers -> R
+    if (tid == 0 && !abort_sh) {
+      const uint32_t sl = (g - 1) % NSTAGE, ul = (g - 1) / NSTAGE;
+      if (!mbar_wait(&bar_mma[sl], ul & 1)) abort_sh = 1;
+    }
+    __syncthreads();
+    if (abort_sh) break;
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+    for (int c0 = 0; c0 < ndet; c0 += 32) {
+      float v[32];
+      tmem_ld32(tmem + lane_base + (uint32_t)c0, v);
+      if (my < ncol) {
+#pragma unroll
+        for (int j = 0; j < 32; j++) __stcs(R + (int64_t)(c0 + j) * ldr + my, v[j]);
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+  }
+  if (abort_sh && tid == 0) {
+    atomicExch(err, 1);
+    // bounded drain of MMAs possibly still in flight before freeing tensor memory
+    for (uint32_t q = (g > NSTAGE ? g - NSTAGE : 0); q < g; q++)
+      (void)mbar_wait(&bar_mma[q % NSTAGE], (q / NSTAGE) & 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+}
+
+}  // namespace
+
+namespace mk {
+
+bool rot_tc_supported(int64_t nrow) {
+  return nrow == 32 || nrow == 64 || nrow == 128 || nrow == 256;
+}
+
+size_t rot_tc_bimg_bytes(int64_t nrow) { return (size_t)nrow * (size_t)nrow * 8; }
+
+int rot_tc_f32(const float *A, const float *X, int64_t ldx, float *R, int64_t ldr, int64_t nrow,
+               int64_t ncol, void *bimg, int *err, cudaStream_t st) {
+  MK_CHECK_ARG(rot_tc_supported(nrow), "tensor-core rotation supports ndet in {32,64,128,256}, got %lld",
+               (long long)nrow);
+  MK_CHECK_ARG(bimg && err && ((uintptr_t)bimg % 16) == 0, "tensor-core rotation: bad scratch");
+  if (ncol <= 0) return MK_OK;
+  const int nd = (int)nrow;
+  k_bprep<<<(nd * nd + 255) / 256, 256, 0, st>>>(A, nd, (char *)bimg);
+  const size_t stage = 2 * (size_t)TILE_M * 128 + 2 * (size_t)nd * 128;
+  const size_t smem = NSTAGE * stage + 1024;
+  static int attr_set[64] = {0};
+  int dev = 0;
+  MK_CUDA(cudaGetDevice(&dev));
+  if (dev >= 0 && dev < 64 && attr_set[dev] < (int)smem) {
+    MK_CUDA(cudaFuncSetAttribute(k_rot_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set[dev] = (int)smem;
+  }
+  int per_sm = (int)(220 * 1024 / smem);
+  if (per_sm < 1) per_sm = 1;
+  if (per_sm > 2) per_sm = 2;  // tensor memory: <= 2 x 256 columns per SM
+  int64_t ntile = (ncol + TILE_M - 1) / TILE_M;
+  int64_t grid = (int64_t)sm_count() * per_sm;
+  if (grid > ntile) grid = ntile;
+  k_rot_tc<<<(unsigned)grid, NTHREADS, smem, st>>>(X, ldx, R, ldr, nd, ncol, (const char *)bimg, err);
+  return launch_status("rot_tc_f32");
+}
+
 }  // namespace mk

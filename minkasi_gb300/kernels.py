@@ -222,6 +222,26 @@ class NoisePlan:
                                          _p(self.ws), self.ws.numel()), "noise plan")
         self._h = h
 
+    def rotate(self, A: torch.Tensor, X: torch.Tensor, out: Optional[torch.Tensor] = None,
+               rot_mode: int = 0) -> torch.Tensor:
+        """R = A . X for this plan's shape (mk_rotate)."""
+        for t, nm in ((A, "A"), (X, "X")):
+            _dev(t, nm)
+            if t.dtype != self.dtype:
+                raise TypeError(f"{nm} must be {self.dtype}")
+        if tuple(X.shape) != (self.ndet, self.ndata) or tuple(A.shape) != (self.ndet, self.ndet):
+            raise ValueError("rotate: shapes do not match the plan")
+        if out is None:
+            out = torch.empty_like(X)
+        check(lib().mk_rotate(self._h, _p(A), _p(X), _p(out), int(rot_mode), _stream()), "rotate")
+        return out
+
+    def status(self) -> int:
+        """1 if a tensor-core kernel of this plan timed out since the last call."""
+        code = ctypes.c_int(0)
+        check(lib().mk_noise_status(self._h, ctypes.byref(code), _stream()), "noise_status")
+        return int(code.value)
+
     def apply(self, v: torch.Tensor, vT: torch.Tensor, mywt: torch.Tensor, dat: torch.Tensor,
               out: Optional[torch.Tensor] = None, rot_mode: int = 0) -> torch.Tensor:
         for t, nm in ((v, "v"), (vT, "vT"), (mywt, "mywt"), (dat, "dat")):
@@ -283,6 +303,16 @@ def mul(out: torch.Tensor, a: torch.Tensor, b: torch.Tensor) -> None:
 def pcg_init(r, z, p, b, Ax, precon, s, reducer: Reducer) -> None:
     check(lib().mk_pcg_init(_p(r), _p(z), _p(p), _p(b), _p(Ax), _p(precon), r.numel(),
                             dtype_code(r), _p(s), _p(reducer.scratch), _stream()), "pcg_init")
+
+
+def pcg_step_xr(x, r, p, Ap, s, reducer: Reducer) -> None:
+    check(lib().mk_pcg_step_xr(_p(x), _p(r), _p(p), _p(Ap), x.numel(), dtype_code(x), _p(s),
+                               _p(reducer.scratch), _stream()), "pcg_step_xr")
+
+
+def pcg_step_zp(z, r, p, s, reducer: Reducer) -> None:
+    check(lib().mk_pcg_step_zp(_p(z), _p(r), _p(p), z.numel(), dtype_code(z), _p(s),
+                               _p(reducer.scratch), _stream()), "pcg_step_zp")
 
 
 def pcg_update(x, r, z, p, Ap, precon, s, reducer: Reducer) -> None:

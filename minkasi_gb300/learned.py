@@ -1,0 +1,330 @@
+"""Learned SPD map-space preconditioner for the mapmaking PCG.
+
+    M = D^-1/2 (I + K^T K) D^-1/2,   K = L4 L3 L2 L1
+
+D is the hit map (D^-1/2 = 0 on unhit pixels), each L is a linear 3x3
+convolution (channels 1 -> 16 -> 16 -> 16 -> 16, FP32 weights).  M is
+symmetric positive definite on the hit pixels for any weights, so plain PCG
+stays valid; K = 0 gives exactly the Jacobi preconditioner 1/hits that the
+reference scripts use (examples/minkasi_mpi_example.py:99-105).  M replaces
+the elementwise ``precon * r`` of run_pcg (minkasi/mapmaking/pcg.py:157-158).
+
+Training data are (r_k, A^-1 r_k) pairs from the mapmaker's own converged
+solves on seeded synthetic skies: for each sky, Jacobi PCG runs to a tight
+FP64 tolerance, recording every iterate; once converged, x* - x_k = A^-1 r_k
+for every recorded residual r_k.  Skies are a Gaussian random field with
+C_l ~ l^-2.5 plus random beta-model clusters.
+
+Loss per pair: ||P(M r - e)||^2 / ||P e||^2, P removing the hit-region mean
+(A annihilates a constant map, so that component of e is undetermined).
+Forward (conv_fwd), adjoint (conv_adj) and weight-gradient (conv_wgrad)
+passes are the project's CUDA kernels (libmkgpu mk_conv3x3_*).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+import torch
+
+from . import kernels as K
+from ._lib import check
+from .kernels import _p, _stream, lib
+
+CHANNELS = (1, 16, 16, 16, 16)
+
+
+# ---------------------------------------------------------------- conv ops
+def conv_fwd(x: torch.Tensor, w: torch.Tensor) -> torch.Tensor:
+    B, Cin, H, W = x.shape
+    Cout = w.shape[0]
+    y = torch.empty((B, Cout, H, W), dtype=torch.float32, device=x.device)
+    check(lib().mk_conv3x3_fwd(_p(x), _p(w), _p(y), B, Cin, Cout, H, W, _stream()), "conv_fwd")
+    return y
+
+
+def conv_adj(y: torch.Tensor, w: torch.Tensor) -> torch.Tensor:
+    B, Cout, H, W = y.shape
+    Cin = w.shape[1]
+    x = torch.empty((B, Cin, H, W), dtype=torch.float32, device=y.device)
+    check(lib().mk_conv3x3_adj(_p(y), _p(w), _p(x), B, Cin, Cout, H, W, _stream()), "conv_adj")
+    return x
+
+
+_WG_SCRATCH = {}
+
+
+def conv_wgrad(x: torch.Tensor, h: torch.Tensor) -> torch.Tensor:
+    """g[co, ci, d] = sum_{b,p} h[b, co, p] x[b, ci, p + d]."""
+    B, Cin, H, W = x.shape
+    Cout = h.shape[1]
+    nb = int(lib().mk_conv3x3_wgrad_scratch_bytes(B, Cin, Cout, H, W))
+    key = (str(x.device),)
+    buf = _WG_SCRATCH.get(key)
+    if buf is None or buf.numel() < nb:
+        buf = torch.empty(max(nb, 256), dtype=torch.uint8, device=x.device)
+        _WG_SCRATCH[key] = buf
+    g = torch.empty((Cout, Cin, 3, 3), dtype=torch.float32, device=x.device)
+    check(lib().mk_conv3x3_wgrad(_p(x), _p(h), _p(g), B, Cin, Cout, H, W, _p(buf), buf.numel(),
+                                 _stream()), "conv_wgrad")
+    return g
+
+
+# ---------------------------------------------------------------- the network
+class ConvNet:
+    """K = L_n ... L_1 with 3x3 kernels; weights[l] has shape (Cout, Cin, 3, 3)."""
+
+    def __init__(self, weights: Sequence[torch.Tensor]):
+        self.weights = [w.contiguous().float() for w in weights]
+
+    @classmethod
+    def init(cls, channels=CHANNELS, scale: float = 0.05, seed: int = 0, device=None):
+        g = torch.Generator().manual_seed(seed)
+        ws = []
+        for cin, cout in zip(channels[:-1], channels[1:]):
+            w = torch.randn((cout, cin, 3, 3), generator=g) * (scale / math.sqrt(cin * 9))
+            ws.append(w.to(device or torch.device("cuda", torch.cuda.current_device())))
+        return cls(ws)
+
+    def forward(self, u: torch.Tensor) -> List[torch.Tensor]:
+        acts = [u]
+        for w in self.weights:
+            acts.append(conv_fwd(acts[-1], w))
+        return acts
+
+    def adjoint(self, y: torch.Tensor) -> List[torch.Tensor]:
+        """[b_n = y, b_{n-1}, ..., b_0] with b_{l-1} = L_l^T b_l."""
+        bs = [y]
+        for w in reversed(self.weights):
+            bs.append(conv_adj(bs[-1], w))
+        return bs
+
+    def ktk(self, u: torch.Tensor) -> torch.Tensor:
+        return self.adjoint(self.forward(u)[-1])[-1]
+
+    def grad(self, u: torch.Tensor, g0: torch.Tensor) -> List[torch.Tensor]:
+        """dL/dw for z = K^T K u given dL/dz = g0 (all [B, C, H, W])."""
+        n = len(self.weights)
+        a = self.forward(u)                       # a_0..a_n
+        b = self.adjoint(a[-1])                   # b_n..b_0 (b[i] = b_{n-i})
+        grads = [torch.zeros_like(w) for w in self.weights]
+        # back through the adjoint chain: g_l = L_l g_{l-1}, l = 1..n
+        g = g0
+        for l in range(1, n + 1):
+            w = self.weights[l - 1]
+            # b_{l-1} = L_l^T b_l  ->  dL/dw_l += wgrad(x = g_{l-1}, h = b_l)
+            grads[l - 1] += conv_wgrad(g, b[n - l])
+            g = conv_fwd(g, w)
+        # g is now dL/dy = dL/da_n; back through the forward chain
+        h = g
+        for l in range(n, 0, -1):
+            grads[l - 1] += conv_wgrad(a[l - 1], h)
+            if l > 1:
+                h = conv_adj(h, self.weights[l - 1])
+        return grads
+
+    def state(self) -> dict:
+        return {f"w{i}": w.detach().cpu().numpy() for i, w in enumerate(self.weights)}
+
+    @classmethod
+    def from_state(cls, st: dict, device=None):
+        ws = [torch.from_numpy(np.asarray(st[f"w{i}"], np.float32)).to(device or "cuda")
+              for i in range(len([k for k in st if k.startswith("w")]))]
+        return cls(ws)
+
+
+# ---------------------------------------------------------------- the preconditioner
+class LearnedPrecon:
+    """z = M r with M = D^-1/2 (I + K^T K) D^-1/2 on an (nx, ny) map."""
+
+    def __init__(self, hits: torch.Tensor, net: ConvNet, shape: Tuple[int, int]):
+        h = hits.reshape(-1).double()
+        dsq = torch.where(h > 0, 1.0 / torch.sqrt(torch.clamp(h, min=1e-300)), torch.zeros_like(h))
+        self.dsq64 = dsq.contiguous()
+        self.dsq32 = dsq.float().contiguous()
+        self.net = net
+        self.shape = tuple(shape)
+        self._u = None
+
+    def apply(self, r: torch.Tensor, z: torch.Tensor) -> torch.Tensor:
+        """z = M r for flat maps (float32 or float64)."""
+        dt = r.dtype
+        dsq = self.dsq64 if dt == torch.float64 else self.dsq32
+        u = torch.empty_like(r)
+        K.mul(u, dsq, r)
+        u32 = u if dt == torch.float32 else u.float()
+        kk = self.net.ktk(u32.view(1, 1, *self.shape)).reshape(-1)
+        kk = kk if dt == torch.float32 else kk.double()
+        check(lib().mk_scale_add(_p(z), _p(dsq), _p(u), _p(kk.contiguous()), z.numel(),
+                                 K.dtype_code(z), _stream()), "scale_add")
+        return z
+
+    def __mul__(self, mapset):
+        out = mapset.copy()
+        for m_in, m_out in zip(mapset.maps, out.maps):
+            self.apply(m_in.map.reshape(-1), m_out.map.reshape(-1))
+        return out
+
+
+# ---------------------------------------------------------------- synthetic skies
+def sky(nx: int, ny: int, pix_arcsec: float, seed: int, device, n_clusters: int = 3,
+        slope: float = -2.5, grf_rms: float = 1e-4) -> torch.Tensor:
+    """GRF with C_l ~ l^slope plus random beta-model clusters (float64, (nx, ny))."""
+    g = torch.Generator(device=device).manual_seed(seed)
+    kx = torch.fft.fftfreq(nx, device=device, dtype=torch.float64)[:, None]
+    ky = torch.fft.rfftfreq(ny, device=device, dtype=torch.float64)[None, :]
+    ell = torch.sqrt(kx ** 2 + ky ** 2)
+    amp = torch.where(ell > 0, ell.clamp(min=1e-12) ** (slope / 2), torch.zeros_like(ell))
+    wn = torch.randn((nx, ny), generator=g, dtype=torch.float64, device=device)
+    f = torch.fft.irfft2(torch.fft.rfft2(wn) * amp, s=(nx, ny))
+    f = f / f.std() * grf_rms
+    rng = np.random.default_rng(seed)
+    yy, xx = torch.meshgrid(torch.arange(nx, device=device, dtype=torch.float64),
+                            torch.arange(ny, device=device, dtype=torch.float64), indexing="ij")
+    for _ in range(n_clusters):
+        cx, cy = rng.uniform(0.2, 0.8) * nx, rng.uniform(0.2, 0.8) * ny
+        thc = rng.uniform(10, 40) / pix_arcsec
+        a = -rng.uniform(2e-4, 1e-3)
+        r2 = (xx - cx) ** 2 + (yy - cy) ** 2
+        f = f + a * (1 + r2 / thc ** 2) ** (0.5 - 1.5 * (2.0 / 3.0))
+    return f
+
+
+# ---------------------------------------------------------------- training data
+def sky_rhs(op64, m, seed: int, pix_arcsec: float) -> torch.Tensor:
+    """b = P^T N d for d = P sky + white noise (1 mK), on the operator's TODs."""
+    dev = op64.device
+    s = sky(m.nx, m.ny, pix_arcsec, seed, dev).reshape(-1)
+    K.map2tod(op64.tmp, s, op64.ipix, False)
+    g = torch.Generator(device=dev).manual_seed(10_000 + seed)
+    op64.tmp.add_(torch.randn(op64.S, generator=g, dtype=torch.float64, device=dev) * 1e-3)
+    op64.noise_all()
+    b = torch.zeros(op64.npix, dtype=torch.float64, device=dev)
+    op64.project_out(b)
+    return b
+
+
+def solve_pairs(op64, m, hits: torch.Tensor, skies: Sequence[int], pix_arcsec: float,
+                max_iter: int = 600, tol: float = 1e-10, keep_above: float = 1e-7):
+    """(r_k, x* - x_k) pairs from converged Jacobi FP64 solves, one solve per
+    sky seed.  Each solve runs until ||r||/||b|| <= tol; iterates whose
+    residual is above ``keep_above`` (so x* - x_k is accurate to ~tol/keep_above
+    relative) become pairs."""
+    from ._lib import MK_S_RR
+    from .pcg import DevicePCG
+
+    M = torch.where(hits > 0, 1.0 / hits.clamp(min=1), torch.zeros_like(hits)).reshape(-1)
+    R, E, iters = [], [], []
+    for seed in skies:
+        b = sky_rhs(op64, m, seed, pix_arcsec)
+        bn2 = float((b * b).sum())
+        x = torch.zeros_like(b)
+        st = DevicePCG(op64, b, x, M, graph=True)
+        st.start()
+        xs, rs = [], []
+        for k in range(max_iter):
+            rel = math.sqrt(max(float(st.s[MK_S_RR]), 0.0) / bn2)
+            if rel <= tol:
+                break
+            if rel > keep_above:
+                xs.append(st.x.clone())
+                rs.append(st.r.clone())
+            st.step()
+        iters.append(k)
+        xstar = st.x.clone()
+        for xk, rk in zip(xs, rs):
+            R.append(rk.float())
+            E.append((xstar - xk).float())
+    return torch.stack(R), torch.stack(E), iters
+
+
+def iterations_to(op64, b: torch.Tensor, precon, tol: float = 1e-6, max_iter: int = 2000):
+    """PCG iterations until the recursive residual reaches tol, then the FP64
+    true residual; ``precon`` is a diagonal map or an object with apply()."""
+    from ._lib import MK_S_RR
+    from .pcg import DevicePCG, _true_residual
+
+    x = torch.zeros_like(b)
+    st = DevicePCG(op64, b, x, precon, graph=True)
+    st.start()
+    bn2 = float((b * b).sum())
+    k = 0
+    for k in range(1, max_iter + 1):
+        st.step()
+        if k % 5 == 0 and math.sqrt(max(float(st.s[MK_S_RR]), 0.0) / bn2) <= tol:
+            tr = _true_residual(op64, b, st.x)
+            if tr <= tol:
+                return k, tr
+    return k, _true_residual(op64, b, st.x)
+
+
+# ---------------------------------------------------------------- training
+def _project(v: torch.Tensor, mask: torch.Tensor, nhit: float) -> torch.Tensor:
+    mean = (v * mask).sum(dim=1, keepdim=True) / nhit
+    return (v - mean) * mask
+
+
+def loss_and_grad(net: ConvNet, dsq: torch.Tensor, mask: torch.Tensor, R: torch.Tensor,
+                  E: torch.Tensor, shape, need_grad: bool = True):
+    """Mean over the batch of ||P(M r - e)||^2 / ||P e||^2 and its weight gradient."""
+    B = R.shape[0]
+    nhit = float(mask.sum())
+    u = (R * dsq[None, :])
+    kk = net.ktk(u.view(B, 1, *shape).contiguous()).reshape(B, -1)
+    mr = dsq[None, :] * (u + kk)
+    pe = _project(E, mask, nhit)
+    den = (pe * pe).sum(dim=1).clamp(min=1e-30)
+    res = _project(mr, mask, nhit) - pe
+    loss = float(((res * res).sum(dim=1) / den).mean())
+    if not need_grad:
+        return loss, None
+    # dL/d(mr) = 2 P res / den / B ; mr = dsq*(u + z) -> dL/dz = dsq * dL/dmr
+    gmr = 2.0 * _project(res, mask, nhit) / den[:, None] / B
+    gz = (dsq[None, :] * gmr).view(B, 1, *shape).contiguous()
+    return loss, net.grad(u.view(B, 1, *shape).contiguous(), gz)
+
+
+def train(net: ConvNet, hits: torch.Tensor, shape, R: torch.Tensor, E: torch.Tensor,
+          epochs: int = 30, batch: int = 64, lr: float = 3e-3, seed: int = 0, log=None) -> List[float]:
+    """Adam on the relative error loss; returns the per-epoch mean loss."""
+    dev = R.device
+    h = hits.reshape(-1).float()
+    dsq = torch.where(h > 0, 1.0 / torch.sqrt(h.clamp(min=1e-30)), torch.zeros_like(h))
+    mask = (h > 0).float()
+    m = [torch.zeros_like(w) for w in net.weights]
+    v = [torch.zeros_like(w) for w in net.weights]
+    b1, b2, eps = 0.9, 0.999, 1e-8
+    t = 0
+    gen = torch.Generator(device="cpu").manual_seed(seed)
+    hist = []
+    n = R.shape[0]
+    for ep in range(epochs):
+        perm = torch.randperm(n, generator=gen)
+        tot, cnt = 0.0, 0
+        for i in range(0, n - batch + 1, batch):
+            idx = perm[i:i + batch].to(dev)
+            loss, grads = loss_and_grad(net, dsq, mask, R[idx], E[idx], shape)
+            t += 1
+            for j, (w, g) in enumerate(zip(net.weights, grads)):
+                m[j].mul_(b1).add_(g, alpha=1 - b1)
+                v[j].mul_(b2).addcmul_(g, g, value=1 - b2)
+                mh = m[j] / (1 - b1 ** t)
+                vh = v[j] / (1 - b2 ** t)
+                w.sub_(lr * mh / (vh.sqrt() + eps))
+            tot += loss
+            cnt += 1
+        hist.append(tot / max(cnt, 1))
+        if log:
+            log(f"epoch {ep}: loss {hist[-1]:.4e}")
+    return hist
+
+
+def save(net: ConvNet, path: str) -> None:
+    np.savez(path, **net.state())
+
+
+def load(path: str, device=None) -> ConvNet:
+    return ConvNet.from_state(dict(np.load(path)), device)

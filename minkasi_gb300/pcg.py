@@ -50,7 +50,14 @@ class null_precon:
 
 
 def _is_map_precon(precon) -> bool:
-    return isinstance(precon, Mapset) and precon.nmap == 1 and isinstance(precon.maps[0], SkyMap)
+    return (isinstance(precon, Mapset) and precon.nmap == 1 and isinstance(precon.maps[0], SkyMap)) \
+        or hasattr(precon, "apply")
+
+
+def _precon_arg(precon):
+    if precon is None:
+        return None
+    return precon if hasattr(precon, "apply") else precon.maps[0].map
 
 
 class DevicePCG:
@@ -63,7 +70,11 @@ class DevicePCG:
         dt, dev = b.dtype, b.device
         self.b = b.reshape(-1)
         self.x = x.reshape(-1)
-        self.M = None if M is None else M.reshape(-1).to(dt).contiguous()
+        # a diagonal preconditioner (map) is fused into the update kernels; an
+        # operator (anything with apply(r, z), e.g. LearnedPrecon) runs between
+        # the two halves of the split update
+        self.Mop = M if hasattr(M, "apply") else None
+        self.M = None if (M is None or self.Mop is not None) else M.reshape(-1).to(dt).contiguous()
         self.r = torch.empty(self.n, dtype=dt, device=dev)
         self.z = torch.empty_like(self.r)
         self.p = torch.empty_like(self.r)
@@ -79,11 +90,20 @@ class DevicePCG:
             self.op.apply(self.x, self.Ap)
             Ax = self.Ap
         K.pcg_init(self.r, self.z, self.p, self.b, Ax.reshape(-1), self.M, self.s, self.red)
+        if self.Mop is not None:
+            self.Mop.apply(self.r, self.z)
+            self.p.copy_(self.z)
+            self.red.dot(self.r, self.z, out=self.s[MK_S_ZR])
         self.iters = 0
 
     def _step(self) -> None:
         self.op.apply(self.p, self.Ap)
-        K.pcg_update(self.x, self.r, self.z, self.p, self.Ap, self.M, self.s, self.red)
+        if self.Mop is None:
+            K.pcg_update(self.x, self.r, self.z, self.p, self.Ap, self.M, self.s, self.red)
+        else:
+            K.pcg_step_xr(self.x, self.r, self.p, self.Ap, self.s, self.red)
+            self.Mop.apply(self.r, self.z)
+            K.pcg_step_zp(self.z, self.r, self.p, self.s, self.red)
 
     def step(self) -> None:
         if self.graph_enabled and self.iters >= 1:
@@ -126,8 +146,7 @@ def run_pcg_wprior(b: Mapset, x0: Mapset, tods: TodVec, prior=None, precon=None,
     t0 = time.time()
     op = tods.engine(b.maps[0])
     x = x0.copy()
-    M = precon.maps[0].map if precon is not None else None
-    st = DevicePCG(op, b.maps[0].map, x.maps[0].map, M, graph=graph)
+    st = DevicePCG(op, b.maps[0].map, x.maps[0].map, _precon_arg(precon), graph=graph)
     st.start()
     bnorm = math.sqrt(b.dot(b)) if tol is not None else None
     nsamp = tods.get_nsamp()
@@ -227,7 +246,12 @@ def run_pcg_mixed(b: Mapset, x0: Mapset, tods: TodVec, precon=None, tol: float =
     bf = m64.map.reshape(-1)
     red = _reducer(bf.device)
     bnorm = math.sqrt(red.dot(bf, bf).item())
-    M32 = precon.maps[0].map.reshape(-1).float().contiguous() if precon is not None else None
+    if inner_precon is not None:
+        M32 = inner_precon
+    elif precon is not None and hasattr(precon, "apply"):
+        M32 = precon
+    else:
+        M32 = precon.maps[0].map.reshape(-1).float().contiguous() if precon is not None else None
     r32 = torch.empty(bf.numel(), dtype=torch.float32, device=bf.device)
     e32 = torch.zeros_like(r32)
     zero32 = torch.zeros_like(r32)
