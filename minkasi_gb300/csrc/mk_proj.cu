@@ -262,6 +262,114 @@ __global__ void __launch_bounds__(256) k_scatter_fixed(unsigned long long *__res
   }
 }
 
+// ---- vectorised forms (ipix and dat 16-byte aligned) -----------------------
+// Each thread owns 8 consecutive samples: two 16-byte ipix loads and 16/32
+// bytes of dat per load instruction (a warp covers 256 consecutive samples,
+// fully coalesced).  Runs of equal pixels inside the 8 are summed in a
+// register; one integer atomic per run.  This trades the warp-wide scan
+// (~25 instructions per sample) for ~6, which matters because the scan
+// version is issue-bound.
+template <typename T>
+__device__ __forceinline__ void load8(const T *__restrict__ p, T (&v)[8]) {
+  if constexpr (sizeof(T) == 8) {
+    const double2 *q = reinterpret_cast<const double2 *>(p);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      double2 a = __ldcs(q + k);
+      v[2 * k] = a.x;
+      v[2 * k + 1] = a.y;
+    }
+  } else {
+    const float4 *q = reinterpret_cast<const float4 *>(p);
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      float4 a = __ldcs(q + k);
+      v[4 * k] = a.x;
+      v[4 * k + 1] = a.y;
+      v[4 * k + 2] = a.z;
+      v[4 * k + 3] = a.w;
+    }
+  }
+}
+
+__device__ __forceinline__ void load8i(const int32_t *__restrict__ p, int32_t (&k)[8]) {
+  const int4 *q = reinterpret_cast<const int4 *>(p);
+  int4 a = __ldcs(q), b = __ldcs(q + 1);
+  k[0] = a.x; k[1] = a.y; k[2] = a.z; k[3] = a.w;
+  k[4] = b.x; k[5] = b.y; k[6] = b.z; k[7] = b.w;
+}
+
+__device__ __forceinline__ double fmax_nan(double m, double a) { return (a > m || a != a) ? a : m; }
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_absmax8(const T *__restrict__ dat, int64_t n, FixHdr *h) {
+  double m = 0.0;
+  const int64_t n8 = n >> 3;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n8; g += stride) {
+    T v[8];
+    load8(dat + 8 * g, v);
+#pragma unroll
+    for (int k = 0; k < 8; k++) m = fmax_nan(m, fabs((double)v[k]));
+  }
+  if (blockIdx.x == 0 && threadIdx.x < (n & 7)) m = fmax_nan(m, fabs((double)dat[(n8 << 3) + threadIdx.x]));
+  unsigned long long b = __double_as_longlong(m);
+  for (int off = 16; off > 0; off >>= 1) {
+    unsigned long long o = __shfl_xor_sync(FULL, b, off);
+    b = o > b ? o : b;
+  }
+  __shared__ unsigned long long sh[8];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = b;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) b = sh[w] > b ? sh[w] : b;
+    atomicMax(&h->dmax_bits, b);
+  }
+}
+
+__device__ __forceinline__ void flush_i64(unsigned long long *__restrict__ acc, int32_t key, long long v,
+                                          int64_t npix) {
+  if (v != 0 && (uint32_t)key < (uint64_t)npix) atomicAdd(acc + key, (unsigned long long)v);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_scatter_fixed8(unsigned long long *__restrict__ acc,
+                                                        const T *__restrict__ dat,
+                                                        const int32_t *__restrict__ ipix, int64_t n,
+                                                        int64_t npix, int hbits, FixHdr *h) {
+  const double dmax = __longlong_as_double((long long)h->dmax_bits);
+  if (!(dmax > 0.0) || !isfinite(dmax)) return;
+  const int s = 61 - ilogb(dmax) - hbits;
+  const double scale = ldexp(1.0, s);
+  if (blockIdx.x == 0 && threadIdx.x == 0) h->shift = s;
+  const int64_t n8 = n >> 3;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n8; g += stride) {
+    int32_t p[8];
+    T v[8];
+    load8i(ipix + 8 * g, p);
+    load8(dat + 8 * g, v);
+    int32_t key = p[0];
+    long long cur = __double2ll_rn((double)v[0] * scale);
+#pragma unroll
+    for (int k = 1; k < 8; k++) {
+      long long t = __double2ll_rn((double)v[k] * scale);
+      if (p[k] == key) {
+        cur += t;
+      } else {
+        flush_i64(acc, key, cur, npix);
+        key = p[k];
+        cur = t;
+      }
+    }
+    flush_i64(acc, key, cur, npix);
+  }
+  if (blockIdx.x == 0 && threadIdx.x < (n & 7)) {
+    int64_t i = (n8 << 3) + threadIdx.x;
+    flush_i64(acc, ipix[i], __double2ll_rn((double)dat[i] * scale), npix);
+  }
+}
+
 // map += acc * 2^-s, acc cleared; non-finite data poisons the touched map with NaN.
 template <typename T>
 __global__ void k_fixed_finalize(T *__restrict__ map, unsigned long long *__restrict__ acc, int64_t npix,
@@ -322,10 +430,17 @@ int tod2map_fixed_t(void *map, const void *dat, const int32_t *ipix, int64_t n, 
                     int hbits, void *scratch, cudaStream_t st) {
   FixHdr *h = (FixHdr *)scratch;
   unsigned long long *acc = (unsigned long long *)((char *)scratch + sizeof(FixHdr));
-  k_absmax<T><<<mk_grid(n, 256, 4), 256, 0, st>>>((const T *)dat, n, h);
-  constexpr int U = 4;
-  k_scatter_fixed<T, U><<<mk_grid((n + U - 1) / U, 256, 8), 256, 0, st>>>(acc, (const T *)dat, ipix, n,
-                                                                          npix, hbits, h);
+  const bool vec = ((uintptr_t)dat % 16 == 0) && ((uintptr_t)ipix % 16 == 0);
+  if (vec) {
+    k_absmax8<T><<<mk_grid((n + 7) / 8, 256, 8), 256, 0, st>>>((const T *)dat, n, h);
+    k_scatter_fixed8<T><<<mk_grid((n + 7) / 8, 256, 8), 256, 0, st>>>(acc, (const T *)dat, ipix, n, npix,
+                                                                      hbits, h);
+  } else {
+    k_absmax<T><<<mk_grid(n, 256, 8), 256, 0, st>>>((const T *)dat, n, h);
+    constexpr int U = 4;
+    k_scatter_fixed<T, U><<<mk_grid((n + U - 1) / U, 256, 8), 256, 0, st>>>(acc, (const T *)dat, ipix, n,
+                                                                            npix, hbits, h);
+  }
   k_fixed_finalize<T><<<mk_grid(npix, 256, 8), 256, 0, st>>>((T *)map, acc, npix, h, n);
   k_fixed_reset<T><<<1, 1, 0, st>>>(h);
   return mk::launch_status("mk_tod2map_fixed");

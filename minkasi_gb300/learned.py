@@ -269,20 +269,25 @@ def _project(v: torch.Tensor, mask: torch.Tensor, nhit: float) -> torch.Tensor:
 
 def loss_and_grad(net: ConvNet, dsq: torch.Tensor, mask: torch.Tensor, R: torch.Tensor,
                   E: torch.Tensor, shape, need_grad: bool = True):
-    """Mean over the batch of ||P(M r - e)||^2 / ||P e||^2 and its weight gradient."""
+    """Mean over the batch of min_c ||c P(M r) - P e||^2 / ||P e||^2 and its
+    weight gradient.  CG is invariant to a scalar scale of M, so each pair's
+    best scale c is taken in closed form; by the envelope theorem the
+    gradient is the partial derivative at that c."""
     B = R.shape[0]
     nhit = float(mask.sum())
     u = (R * dsq[None, :])
     kk = net.ktk(u.view(B, 1, *shape).contiguous()).reshape(B, -1)
     mr = dsq[None, :] * (u + kk)
     pe = _project(E, mask, nhit)
+    a = _project(mr, mask, nhit)
     den = (pe * pe).sum(dim=1).clamp(min=1e-30)
-    res = _project(mr, mask, nhit) - pe
+    c = (a * pe).sum(dim=1) / (a * a).sum(dim=1).clamp(min=1e-30)
+    res = c[:, None] * a - pe
     loss = float(((res * res).sum(dim=1) / den).mean())
     if not need_grad:
         return loss, None
-    # dL/d(mr) = 2 P res / den / B ; mr = dsq*(u + z) -> dL/dz = dsq * dL/dmr
-    gmr = 2.0 * _project(res, mask, nhit) / den[:, None] / B
+    # dL/d(mr) = 2 c P res / den / B ; mr = dsq*(u + z) -> dL/dz = dsq * dL/dmr
+    gmr = 2.0 * c[:, None] * _project(res, mask, nhit) / den[:, None] / B
     gz = (dsq[None, :] * gmr).view(B, 1, *shape).contiguous()
     return loss, net.grad(u.view(B, 1, *shape).contiguous(), gz)
 

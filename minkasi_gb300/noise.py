@@ -55,11 +55,31 @@ def smooth_many_vecs(vecs: torch.Tensor, fwhm: float = 20.0) -> torch.Tensor:
     return back / (2 * (n - 1))
 
 
+def row_median(a: torch.Tensor) -> torch.Tensor:
+    """numpy.median along the last axis: the mean of the two middle values
+    for an even count (torch.median would return the lower one)."""
+    s = torch.sort(a, dim=-1).values
+    n = s.shape[-1]
+    if n % 2:
+        return s[..., n // 2].clone()
+    return (s[..., n // 2 - 1] + s[..., n // 2]) / 2
+
+
+def _eig_desc(c: np.ndarray) -> np.ndarray:
+    w, u = np.linalg.eigh(c)
+    return u[:, np.argsort(w)[::-1]]
+
+
 def left_singular_vectors(dat: torch.Tensor) -> torch.Tensor:
-    """u of the thin SVD of dat (ndet x ndata), columns by descending singular value."""
-    r = torch.linalg.qr(dat.T, mode="r")[1]
-    _, _, vh = torch.linalg.svd(r)
-    return vh.T.contiguous()
+    """u of the thin SVD of dat (ndet x ndata), columns by descending singular
+    value: eigenvectors of the Gram matrix d d^T (an FP64 GEMM on the GPU),
+    decomposed on the host (ndet x ndet), then refined once by
+    re-diagonalising the Gram matrix of the rotated data."""
+    u = _eig_desc((dat @ dat.T).cpu().numpy())
+    ut = torch.from_numpy(np.ascontiguousarray(u)).to(dat.device)
+    d2 = ut.T @ dat
+    u = u @ _eig_desc((d2 @ d2.T).cpu().numpy())
+    return torch.from_numpy(np.ascontiguousarray(u)).to(dat.device)
 
 
 class NoiseSmoothedSVD:
@@ -72,7 +92,7 @@ class NoiseSmoothedSVD:
         dat = as_device(dat_use, torch.float64)
         self.noisevec: Optional[torch.Tensor] = None
         if prewhiten:
-            noisevec = torch.median(torch.abs(torch.diff(dat, dim=1)), dim=1).values
+            noisevec = row_median(torch.abs(torch.diff(dat, dim=1)))
             dat = dat / noisevec[:, None]
             self.noisevec = noisevec.clone()
         if u_in is None:
@@ -83,7 +103,7 @@ class NoiseSmoothedSVD:
             u = as_device(u_in, torch.float64)
             assert u.shape[0] == u.shape[1]
             self.v = u.T.contiguous()
-            self.vT = torch.linalg.inv(self.v).contiguous()
+            self.vT = torch.from_numpy(np.linalg.inv(self.v.cpu().numpy())).to(self.v.device).contiguous()
         dat_rot = self.v @ dat
         dat_trans = dct1(dat_rot)
         spec = smooth_many_vecs(dat_trans ** 2, fwhm)

@@ -8,10 +8,9 @@ tod2map) + three fused update kernels with every scalar on the device, and
 from the second iteration on the whole iteration is replayed as one CUDA
 graph -- no host round trip per iteration.
 
-``run_pcg_mixed`` is the mixed-precision solver: an FP64 outer iterative
-refinement (true FP64 residual b - A x each outer step) around FP32 inner
-PCG solves (FP32 projections, filter and map vectors; FP64 dot products).
-It stops when the FP64 true residual ||b - A x|| / ||b|| reaches ``tol``.
+``run_pcg_mixed`` is the mixed-precision solver: FP64 vectors, dot products
+and scalars around FP32 operator applications, refined by FP64 true
+residuals (residual replacement) until ||b - A x|| / ||b|| reaches ``tol``.
 """
 from __future__ import annotations
 
@@ -227,17 +226,109 @@ def _run_pcg_generic(b, x0, tods, prior, precon, mask, maxiter, outroot, save_it
     return x
 
 
-def run_pcg_mixed(b: Mapset, x0: Mapset, tods: TodVec, precon=None, tol: float = 1e-6,
-                  inner_iters: int = 20, max_outer: int = 200, graph: bool = True,
-                  verbose: bool = False, history: Optional[list] = None,
-                  inner_precon=None) -> Mapset:
-    """Mixed precision: FP64 outer iterative refinement, FP32 inner PCG.
+class MixedOp:
+    """A in FP32 seen from FP64 vectors: p64 -> p32 -> A32 p32 -> Ap64."""
 
-    Each outer step computes the FP64 true residual r = b - A64 x (FP64
-    projections and filter), stops if ||r||/||b|| <= tol, else solves
-    A32 e = r approximately with ``inner_iters`` FP32 PCG iterations (FP64
-    dot products) and updates x += e in FP64.  ``inner_precon`` replaces the
-    Jacobi precon in the inner solve (any object with apply(r32, z32))."""
+    def __init__(self, op32, n: int, device):
+        self.op32 = op32
+        self.p32 = torch.empty(n, dtype=torch.float32, device=device)
+        self.a32 = torch.empty(n, dtype=torch.float32, device=device)
+
+    def apply(self, x: torch.Tensor, out: torch.Tensor, accumulate: bool = False):
+        self.p32.copy_(x.reshape(-1))
+        self.op32.apply(self.p32, self.a32)
+        if accumulate:
+            out.reshape(-1).add_(self.a32)
+        else:
+            out.reshape(-1).copy_(self.a32)
+        return out
+
+
+def run_pcg_mixed(b: Mapset, x0: Mapset, tods: TodVec, precon=None, tol: float = 1e-6,
+                  max_iter: int = 5000, replace_every: int = 50, graph: bool = True,
+                  verbose: bool = False, history: Optional[list] = None,
+                  inner_precon=None, on_outer=None, mode: str = "reliable",
+                  inner_iters: int = 20, max_outer: int = 500) -> Mapset:
+    """Mixed-precision PCG to an FP64 true residual ||b - A x||/||b|| <= tol.
+
+    mode="reliable" (default): PCG whose vectors, dot products and scalars are
+    FP64 but whose operator applications run in FP32 (FP32 projections, FP32
+    DCT/filter, 3xTF32 tensor-core rotations); every ``replace_every``
+    iterations, and whenever the recursive residual claims convergence, the
+    residual is replaced by the FP64 true residual b - A64 x (an FP64
+    operator application).  Those replacements are the iterative-refinement
+    steps: the FP64 residual corrects the drift of the FP32 operator while the
+    Krylov space is kept.
+
+    mode="refine": classic iterative refinement -- each outer step solves
+    A32 e = r64 with ``inner_iters`` FP32 PCG iterations from zero and updates
+    x += e in FP64.  Restarting the Krylov space every ``inner_iters`` makes
+    it stall on ill-conditioned maps; kept for comparison.
+
+    ``inner_precon``/``precon`` may be a Mapset (diagonal) or any object with
+    apply(r, z) (e.g. LearnedPrecon).  ``on_outer(k, x, rel)`` is called at
+    every FP64 residual evaluation."""
+    if mode == "refine":
+        return _run_refine(b, x0, tods, precon, tol, inner_iters, max_outer, graph, verbose,
+                           history, inner_precon, on_outer)
+    m64 = b.maps[0]
+    op64 = tods.engine(m64, torch.float64)
+    op32 = tods.engine(m64, torch.float32)
+    x = x0.copy()
+    xf = x.maps[0].map.reshape(-1)
+    bf = m64.map.reshape(-1)
+    red = _reducer(bf.device)
+    bnorm = math.sqrt(red.dot(bf, bf).item())
+    M = inner_precon if inner_precon is not None else _precon_arg(precon)
+    st = DevicePCG(MixedOp(op32, bf.numel(), bf.device), bf, xf, M, graph=graph)
+    ax = torch.empty_like(bf)
+    ptmp = torch.empty_like(bf)
+
+    def replace() -> float:
+        # r = b - A64 x; z = M r; zr = r.z  (p kept)
+        op64.apply(xf, ax)
+        K.pcg_init(st.r, st.z, ptmp, bf, ax, st.M, st.s, st.red)
+        if st.Mop is not None:
+            st.Mop.apply(st.r, st.z)
+            st.red.dot(st.r, st.z, out=st.s[MK_S_ZR])
+        return math.sqrt(max(float(st.s[MK_S_RR]), 0.0)) / bnorm
+
+    st.start()
+    rel = math.sqrt(max(float(st.s[MK_S_RR]), 0.0)) / bnorm
+    k = 0
+    outer = 0
+    since = 0
+    while k < max_iter:
+        st.step()
+        k += 1
+        since += 1
+        check = since >= replace_every or k % 5 == 0
+        if not check:
+            continue
+        s = st.scalars()
+        if s[MK_S_FLAG]:
+            raise FloatingPointError(f"mixed PCG breakdown at iteration {k}")
+        rec = math.sqrt(max(s[MK_S_RR], 0.0)) / bnorm
+        if since >= replace_every or rec <= tol:
+            rel = replace()
+            outer += 1
+            since = 0
+            if history is not None:
+                history.append({"iter": k, "recursive_rel": rec, "true_rel_residual": rel})
+            if verbose:
+                print(f"iter {k}: true FP64 residual {rel:.3e} (recursive {rec:.3e})")
+            if on_outer is not None:
+                on_outer(outer, xf, rel)
+            if rel <= tol:
+                break
+    x.niter = k
+    x.outer = outer
+    x.rel_residual = rel
+    return x
+
+
+def _run_refine(b, x0, tods, precon, tol, inner_iters, max_outer, graph, verbose, history,
+                inner_precon, on_outer) -> Mapset:
     m64 = b.maps[0]
     op64 = tods.engine(m64, torch.float64)
     op32 = tods.engine(m64, torch.float32)
@@ -267,6 +358,8 @@ def run_pcg_mixed(b: Mapset, x0: Mapset, tods: TodVec, precon=None, tol: float =
             history.append({"outer": outer, "inner_total": total_inner, "true_rel_residual": rel})
         if verbose:
             print(f"outer {outer}: true FP64 residual {rel:.3e} after {total_inner} inner iterations")
+        if on_outer is not None:
+            on_outer(outer, xf, rel)
         if rel <= tol:
             break
         r32.copy_(r64)

@@ -68,12 +68,15 @@ def _proj(v, mask):
 
 
 def loss(ws, dsq, mask, R, E, shape) -> float:
+    """mean_b min_c ||c P(M r_b) - P e_b||^2 / ||P e_b||^2."""
     B = R.shape[0]
     u = R * dsq[None, :]
     z = ktk(ws, u.reshape(B, 1, *shape)).reshape(B, -1)
     mr = dsq[None, :] * (u + z)
     pe = _proj(E, mask)
-    res = _proj(mr, mask) - pe
+    a = _proj(mr, mask)
+    c = (a * pe).sum(axis=1) / (a * a).sum(axis=1)
+    res = c[:, None] * a - pe
     return float(((res ** 2).sum(axis=1) / (pe ** 2).sum(axis=1)).mean())
 
 
@@ -91,10 +94,13 @@ def loss_grad(ws, dsq, mask, R, E, shape) -> Tuple[float, List[np.ndarray]]:
     z = bs[-1].reshape(B, -1)
     mr = dsq[None, :] * (u.reshape(B, -1) + z)
     pe = _proj(E, mask)
+    a = _proj(mr, mask)
     den = (pe ** 2).sum(axis=1)
-    res = _proj(mr, mask) - pe
+    c = (a * pe).sum(axis=1) / (a * a).sum(axis=1)
+    res = c[:, None] * a - pe
     L = float(((res ** 2).sum(axis=1) / den).mean())
-    gmr = 2.0 * _proj(res, mask) / den[:, None] / B
+    # envelope theorem: at the optimal c the gradient is the partial at fixed c
+    gmr = 2.0 * c[:, None] * _proj(res, mask) / den[:, None] / B
     g = (dsq[None, :] * gmr).reshape(B, 1, *shape)
     grads = [np.zeros_like(w) for w in ws]
     for l in range(1, n + 1):
