@@ -119,6 +119,25 @@ int mk_tod2map_fixed(void *map, const void *dat, const int32_t *ipix, int64_t nd
                      int64_t ndata, int64_t npix, int64_t hmax, int dtype, void *scratch,
                      void *stream);
 
+/* mk_tod2map_fixed without a scratch argument.  This entry point has no
+ * counterpart in the reference.  It exists for callers that cannot allocate
+ * device memory: a host binding that only forwards pointers it was handed,
+ * or a process whose memory pool owns the GPU and must not be bypassed by a
+ * cudaMalloc.  It allocates nothing.  Its accumulator is a device array
+ * built into the library (a 256-byte header plus 8 bytes per pixel for up to
+ * MK_NOALLOC_MAX_NPIX pixels, 32 MiB), which every GPU that loads the
+ * library holds until the process exits.  npix above the limit is rejected
+ * with MK_ERR_ARG.  The first call on a device looks up that array's device
+ * address (cudaGetSymbolAddress, with that device current); make this first
+ * call before any stream capture.  All calls share the one array, which
+ * every complete call leaves zeroed: calls that overlap on the GPU (on
+ * different streams, or from different host threads without ordering) race
+ * and give wrong maps.  Inputs, outputs and results are as mk_tod2map_fixed. */
+#define MK_NOALLOC_MAX_NPIX (4194304LL)
+int mk_tod2map_fixed_noalloc(void *map, const void *dat, const int32_t *ipix, int64_t ndet,
+                             int64_t ndata, int64_t npix, int64_t hmax, int dtype,
+                             void *stream);
+
 /* ---- DCT-I and the SmoothedSVD noise filter --------------------------- */
 
 /* Batched unnormalised DCT-I (FFTW REDFT00) of nrow rows of length n >= 2:

@@ -40,6 +40,7 @@ SIGNATURES = {
     "mk_check_pix": (_i32, [_vp, _i64, _i64, ctypes.POINTER(ctypes.c_int64), _vp]),
     "mk_tod2map_fixed_scratch_bytes": (_sz, [_i64]),
     "mk_tod2map_fixed": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _i64, _i32, _vp, _vp]),
+    "mk_tod2map_fixed_noalloc": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _i64, _i32, _vp]),
     "mk_pixplan_create": (_i32, [_pp, _vp, _i64, _i64, _vp]),
     "mk_tod2map_sorted": (_i32, [_vp, _vp, _vp, _i32, _vp]),
     "mk_pixplan_destroy": (_i32, [_vp]),

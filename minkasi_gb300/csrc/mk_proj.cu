@@ -10,6 +10,8 @@
 // st.global.cs) so they do not push the map out of L2.
 #include <cub/device/device_radix_sort.cuh>
 
+#include <mutex>
+
 #include "mk_common.cuh"
 
 namespace {
@@ -623,4 +625,52 @@ extern "C" int mk_tod2map_fixed(void *map, const void *dat, const int32_t *ipix,
   cudaStream_t st = mk::as_stream(stream);
   return dtype == MK_F64 ? tod2map_fixed_t<double>(map, dat, ipix, n, npix, hbits, scratch, st)
                          : tod2map_fixed_t<float>(map, dat, ipix, n, npix, hbits, scratch, st);
+}
+
+// ---- the same scatter with library-owned scratch, for callers that cannot
+// allocate device memory ----------------------------------------------------
+// The accumulator lives in a file-scope device array that every GPU loading
+// this library holds until the process exits: a 256-byte header plus one
+// int64 per pixel for up to MK_NOALLOC_MAX_NPIX pixels (32 MiB).  It is
+// zero when the module loads, and every complete call leaves it zero again.
+namespace {
+constexpr int64_t NOALLOC_MAX_NPIX = MK_NOALLOC_MAX_NPIX;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(FixHdr) +
+                                                                 NOALLOC_MAX_NPIX * sizeof(unsigned long long)];
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[64] = {};
+
+// Device address of g_noalloc_scratch on the current device.  The name is a
+// host-side stand-in for the array, not a device address, so it is resolved
+// once per device with cudaGetSymbolAddress (this device must be current).
+int noalloc_scratch(void **out) {
+  int dev = 0;
+  MK_CUDA(cudaGetDevice(&dev));
+  MK_CHECK_ARG(dev >= 0 && dev < 64, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      mk::set_error("mk_tod2map_fixed_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+      return MK_ERR_CUDA;
+    }
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return MK_OK;
+}
+}  // namespace
+
+extern "C" int mk_tod2map_fixed_noalloc(void *map, const void *dat, const int32_t *ipix,
+                                        int64_t ndet, int64_t ndata, int64_t npix, int64_t hmax,
+                                        int dtype, void *stream) {
+  MK_CHECK_ARG(npix >= 0 && npix <= NOALLOC_MAX_NPIX,
+               "mk_tod2map_fixed_noalloc: npix=%lld exceeds the built-in scratch limit of %lld pixels "
+               "(use mk_tod2map_fixed with caller scratch for larger maps)",
+               (long long)npix, (long long)NOALLOC_MAX_NPIX);
+  void *scratch = nullptr;
+  int rc = noalloc_scratch(&scratch);
+  if (rc) return rc;
+  return mk_tod2map_fixed(map, dat, ipix, ndet, ndata, npix, hmax, dtype, scratch, stream);
 }

@@ -1,0 +1,64 @@
+"""mk_tod2map_fixed_noalloc: the tod2map for callers that cannot allocate
+device memory (its accumulator is a device array built into the library).
+
+Called through the C ABI and checked against mk_tod2map_fixed with caller
+scratch, on two calls in a row: the second call must see the built-in
+scratch left clean by the first.  Same tolerance as the other tod2map parity
+tests (1e-13 relative), though the two paths run the same arithmetic.
+Collected last on purpose.  GPU only.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+cuda = torch.device("cuda", 0)
+
+
+def _case(seed, ndet, ndata, npix):
+    rng = np.random.default_rng(seed)
+    walk = np.cumsum(rng.integers(-1, 2, size=(ndet, ndata)), axis=1) // 3
+    ipix = np.mod(walk + rng.integers(0, npix, size=(ndet, 1)), npix).astype(np.int32)
+    dat = rng.standard_normal((ndet, ndata))
+    return ipix, dat
+
+
+def test_noalloc_matches_scratch_variant_twice():
+    from minkasi_gb300 import _lib, kernels as K
+
+    h = _lib.load()
+    vp = ctypes.c_void_p
+    stream = vp(torch.cuda.current_stream().cuda_stream)
+    npix = 1 << 16
+    outs = []
+    for call, seed in enumerate((11, 12)):
+        ipix, dat = _case(seed, 12, 30_001, npix)
+        gi = torch.from_numpy(ipix).to(cuda)
+        gd = torch.from_numpy(dat).to(cuda)
+        hmax = int(np.bincount(ipix.ravel(), minlength=npix).max())
+        base = torch.from_numpy(np.random.default_rng(seed + 100).standard_normal(npix)).to(cuda)
+        ref = base.clone()
+        scratch = K.FixedScratch(npix)
+        assert h.mk_tod2map_fixed(vp(ref.data_ptr()), vp(gd.data_ptr()), vp(gi.data_ptr()), 12, 30_001,
+                                  npix, hmax, _lib.MK_F64, vp(scratch.buf.data_ptr()), stream) == 0
+        got = base.clone()
+        rc = h.mk_tod2map_fixed_noalloc(vp(got.data_ptr()), vp(gd.data_ptr()), vp(gi.data_ptr()), 12,
+                                        30_001, npix, hmax, _lib.MK_F64, stream)
+        assert rc == 0, h.mk_last_error()
+        torch.cuda.synchronize()
+        r, g = ref.cpu().numpy(), got.cpu().numpy()
+        assert np.abs(g - r).max() <= 1e-13 * np.abs(r).max()
+        outs.append(g)
+    assert not np.array_equal(outs[0], outs[1])
+
+
+def test_noalloc_rejects_maps_above_the_limit():
+    from minkasi_gb300 import _lib
+
+    h = _lib.load()
+    too_big = 4194304 + 1
+    rc = h.mk_tod2map_fixed_noalloc(None, None, None, 1, 1, too_big, 1, _lib.MK_F64, None)
+    assert rc == _lib.MK_ERR_ARG
+    assert b"limit" in h.mk_last_error()
