@@ -284,7 +284,14 @@ int blas_rotate(int dtype, const void *A, const void *X, int64_t ldx, void *R, i
   cublasSetMathMode(h, mode);
   cublasSetEmulationStrategy(h, emulate ? CUBLAS_EMULATION_STRATEGY_EAGER : CUBLAS_EMULATION_STRATEGY_DEFAULT);
   cublasStatus_t s;
-  if (dtype == MK_F64) {
+  if (dtype == MK_F64 && emulate) {
+    // explicit emulated compute type: FP64 operands sliced into fixed-point
+    // pieces on the integer tensor cores
+    const double one = 1.0, zero = 0.0;
+    s = cublasGemmEx_64(h, CUBLAS_OP_N, CUBLAS_OP_N, ncol, nrow, nrow, &one, X, CUDA_R_64F, ldx, A,
+                        CUDA_R_64F, nrow, &zero, R, CUDA_R_64F, ldr,
+                        CUBLAS_COMPUTE_64F_EMULATED_FIXEDPOINT, CUBLAS_GEMM_DEFAULT);
+  } else if (dtype == MK_F64) {
     const double one = 1.0, zero = 0.0;
     s = cublasDgemm_64(h, CUBLAS_OP_N, CUBLAS_OP_N, ncol, nrow, nrow, &one, (const double *)X, ldx,
                        (const double *)A, nrow, &zero, (double *)R, ldr);
@@ -302,15 +309,17 @@ int blas_rotate(int dtype, const void *A, const void *X, int64_t ldx, void *R, i
 
 // mode 0 (automatic) means cuBLAS here; the host autotuner picks 2 or 3 per
 // workload after checking their accuracy against it.
+// mirror_n: see rot_tc_f32 (only the tensor-core kernel fuses the extension;
+// the caller runs k_mirror otherwise).
 int rotate(DctCore *c, int mode, const void *A, const void *X, int64_t ldx, void *R, int64_t ldr,
-           int64_t nrow, int64_t ncol, cudaStream_t st) {
+           int64_t nrow, int64_t ncol, cudaStream_t st, int64_t mirror_n = 0) {
   const int dtype = c->dtype;
   if (mode == 0) mode = 1;
   if (mode == 2) {
     MK_CHECK_ARG(dtype == MK_F32, "tensor-core rotation (rot_mode 2) is FP32 only");
     MK_CHECK_ARG(c->tc_bimg != nullptr, "tensor-core rotation needs ndet in {32,64,128,256}");
     return mk::rot_tc_f32((const float *)A, (const float *)X, ldx, (float *)R, ldr, nrow, ncol,
-                          c->tc_bimg, c->tc_err, st);
+                          c->tc_bimg, c->tc_err, st, mirror_n);
   }
   MK_CHECK_ARG(mode == 1 || mode == 3, "bad rot_mode %d", mode);
   return blas_rotate(dtype, A, X, ldx, R, ldr, nrow, ncol, mode == 3, st);
@@ -321,10 +330,13 @@ int apply_noise_t(DctCore *c, const T *v, const T *vT, const T *w, int64_t ldw, 
                   T *out, int rot_mode, cudaStream_t st) {
   const int64_t n = c->n, N = c->N, nd = c->nrow;
   dim3 g = rows_grid(n, nd);
-  int rc = rotate(c, rot_mode, v, dat, n, c->E, N, nd, n, st);
+  const bool fused_mirror = (rot_mode == 2);  // the tensor-core epilogue writes the extension
+  int rc = rotate(c, rot_mode, v, dat, n, c->E, N, nd, n, st, fused_mirror ? N : 0);
   if (rc) return rc;
-  k_mirror<T><<<g, 256, 0, st>>>((T *)c->E, n, N, nd);
-  if ((rc = mk::launch_status("apply_noise/mirror"))) return rc;
+  if (!fused_mirror) {
+    k_mirror<T><<<g, 256, 0, st>>>((T *)c->E, n, N, nd);
+    if ((rc = mk::launch_status("apply_noise/mirror"))) return rc;
+  }
   if ((rc = core_fft(c, st))) return rc;
   k_filter_extend<T, C><<<g, 256, 0, st>>>((const C *)c->F, w, ldw, (T *)c->E, n, N, nd);
   if ((rc = mk::launch_status("apply_noise/filter"))) return rc;

@@ -193,27 +193,100 @@ struct FixHdr {
   unsigned long long pad[30];
 };
 
+// Integer-only fixed-point conversion.  GB300's FP64 units are a small
+// fraction of its integer throughput, so the per-sample path touches no FP64
+// arithmetic: |x| is compared as a bit pattern, and x * 2^s is formed by
+// shifting the mantissa (round half away from zero).  The same helpers serve
+// the aligned and unaligned kernels, so both give identical bits.
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+__device__ __forceinline__ unsigned int abs_bits(float x) { return __float_as_uint(x) & 0x7FFFFFFFu; }
+
+__device__ __forceinline__ long long shift_round(unsigned long long m, int sh, bool neg) {
+  unsigned long long r;
+  if (sh >= 0)
+    r = m << sh;  // sh <= 9 (double) / 38 (float) by the choice of s: no overflow
+  else if (sh > -64)
+    r = (m + (1ull << (-sh - 1))) >> (-sh);
+  else
+    r = 0;
+  return neg ? -(long long)r : (long long)r;
+}
+
+// round(x * 2^s) for a finite double
+__device__ __forceinline__ long long to_fixed(double x, int s) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int ef = (int)((b >> 52) & 0x7FF);
+  unsigned long long m = b & 0x000FFFFFFFFFFFFFull;
+  if (ef) m |= 0x0010000000000000ull;
+  return shift_round(m, (ef ? ef : 1) - 1075 + s, (b >> 63) != 0);
+}
+
+// round(x * 2^s) for a finite float
+__device__ __forceinline__ long long to_fixed(float x, int s) {
+  const unsigned int b = __float_as_uint(x);
+  const int ef = (int)((b >> 23) & 0xFF);
+  unsigned long long m = b & 0x7FFFFFu;
+  if (ef) m |= 0x800000u;
+  return shift_round(m, (ef ? ef : 1) - 150 + s, (b >> 31) != 0);
+}
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_absmax(const T *__restrict__ dat, int64_t n, FixHdr *h) {
-  double m = 0.0;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-    double a = fabs((double)__ldcs(dat + i));
-    m = (a > m || a != a) ? a : m;
+struct AbsBits;
+template <>
+struct AbsBits<double> {
+  using U = unsigned long long;
+  static __device__ __forceinline__ unsigned long long as_double_bits(U u) { return u; }
+};
+template <>
+struct AbsBits<float> {
+  using U = unsigned int;
+  static __device__ __forceinline__ unsigned long long as_double_bits(U u) {
+    return (unsigned long long)__double_as_longlong((double)__uint_as_float(u));
   }
-  unsigned long long b = __double_as_longlong(m);
+};
+
+// block max of bit patterns -> one atomicMax into the header (as double bits)
+template <typename T>
+__device__ __forceinline__ void absmax_finish(typename AbsBits<T>::U m, FixHdr *h) {
+  unsigned long long b = AbsBits<T>::as_double_bits(m);
   for (int off = 16; off > 0; off >>= 1) {
     unsigned long long o = __shfl_xor_sync(FULL, b, off);
     b = o > b ? o : b;
   }
-  __shared__ unsigned long long sh[8];
+  __shared__ unsigned long long sh[32];
   if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = b;
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int w = 1; w < (int)(blockDim.x >> 5); w++) b = sh[w] > b ? sh[w] : b;
-    b = sh[0] > b ? sh[0] : b;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) b = sh[w] > b ? sh[w] : b;
     atomicMax(&h->dmax_bits, b);
   }
+}
+
+__device__ __forceinline__ void flush_i64(unsigned long long *__restrict__ acc, int32_t key, long long v,
+                                          int64_t npix) {
+  if (v != 0 && (uint32_t)key < (uint64_t)npix) atomicAdd(acc + key, (unsigned long long)v);
+}
+
+// shift s from the header, or INT_MIN if there is nothing (or nothing finite) to add
+__device__ __forceinline__ int fixed_shift(const FixHdr *h, int hbits) {
+  const double dmax = __longlong_as_double((long long)h->dmax_bits);
+  if (!(dmax > 0.0) || !isfinite(dmax)) return INT_MIN;
+  return 61 - ilogb(dmax) - hbits;
+}
+
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_absmax(const T *__restrict__ dat, int64_t n, FixHdr *h) {
+  using U = typename AbsBits<T>::U;
+  U m = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    U a = abs_bits(__ldcs(dat + i));
+    m = a > m ? a : m;
+  }
+  absmax_finish<T>(m, h);
 }
 
 __device__ __forceinline__ void warp_run_add_i64(unsigned long long *__restrict__ acc, int32_t key,
@@ -236,11 +309,8 @@ template <typename T, int U>
 __global__ void __launch_bounds__(256) k_scatter_fixed(unsigned long long *__restrict__ acc, const T *__restrict__ dat,
                                                        const int32_t *__restrict__ ipix, int64_t n,
                                                        int64_t npix, int hbits, FixHdr *h) {
-  const double dmax = __longlong_as_double((long long)h->dmax_bits);
-  if (!(dmax > 0.0) || !isfinite(dmax)) return;  // nothing to add, or non-finite data
-  const int e = ilogb(dmax);
-  const int s = 61 - e - hbits;
-  const double scale = ldexp(1.0, s);
+  const int s = fixed_shift(h, hbits);
+  if (s == INT_MIN) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) h->shift = s;
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -253,7 +323,7 @@ __global__ void __launch_bounds__(256) k_scatter_fixed(unsigned long long *__res
       int64_t i = base + u * 32 + lane;
       if (i < n) {
         p[u] = __ldcs(ipix + i);
-        v[u] = __double2ll_rn((double)__ldcs(dat + i) * scale);
+        v[u] = to_fixed(__ldcs(dat + i), s);
       } else {
         p[u] = -1;
         v[u] = 0;
@@ -301,37 +371,26 @@ __device__ __forceinline__ void load8i(const int32_t *__restrict__ p, int32_t (&
   k[4] = b.x; k[5] = b.y; k[6] = b.z; k[7] = b.w;
 }
 
-__device__ __forceinline__ double fmax_nan(double m, double a) { return (a > m || a != a) ? a : m; }
-
 template <typename T>
 __global__ void __launch_bounds__(256) k_absmax8(const T *__restrict__ dat, int64_t n, FixHdr *h) {
-  double m = 0.0;
+  using U = typename AbsBits<T>::U;
+  U m = 0;
   const int64_t n8 = n >> 3;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n8; g += stride) {
     T v[8];
     load8(dat + 8 * g, v);
 #pragma unroll
-    for (int k = 0; k < 8; k++) m = fmax_nan(m, fabs((double)v[k]));
+    for (int k = 0; k < 8; k++) {
+      U a = abs_bits(v[k]);
+      m = a > m ? a : m;  // NaN patterns sort above +inf
+    }
   }
-  if (blockIdx.x == 0 && threadIdx.x < (n & 7)) m = fmax_nan(m, fabs((double)dat[(n8 << 3) + threadIdx.x]));
-  unsigned long long b = __double_as_longlong(m);
-  for (int off = 16; off > 0; off >>= 1) {
-    unsigned long long o = __shfl_xor_sync(FULL, b, off);
-    b = o > b ? o : b;
+  if (blockIdx.x == 0 && threadIdx.x < (n & 7)) {
+    U a = abs_bits(dat[(n8 << 3) + threadIdx.x]);
+    m = a > m ? a : m;
   }
-  __shared__ unsigned long long sh[8];
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = b;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int w = 0; w < (int)(blockDim.x >> 5); w++) b = sh[w] > b ? sh[w] : b;
-    atomicMax(&h->dmax_bits, b);
-  }
-}
-
-__device__ __forceinline__ void flush_i64(unsigned long long *__restrict__ acc, int32_t key, long long v,
-                                          int64_t npix) {
-  if (v != 0 && (uint32_t)key < (uint64_t)npix) atomicAdd(acc + key, (unsigned long long)v);
+  absmax_finish<T>(m, h);
 }
 
 template <typename T>
@@ -339,10 +398,8 @@ __global__ void __launch_bounds__(256) k_scatter_fixed8(unsigned long long *__re
                                                         const T *__restrict__ dat,
                                                         const int32_t *__restrict__ ipix, int64_t n,
                                                         int64_t npix, int hbits, FixHdr *h) {
-  const double dmax = __longlong_as_double((long long)h->dmax_bits);
-  if (!(dmax > 0.0) || !isfinite(dmax)) return;
-  const int s = 61 - ilogb(dmax) - hbits;
-  const double scale = ldexp(1.0, s);
+  const int s = fixed_shift(h, hbits);
+  if (s == INT_MIN) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) h->shift = s;
   const int64_t n8 = n >> 3;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -352,10 +409,10 @@ __global__ void __launch_bounds__(256) k_scatter_fixed8(unsigned long long *__re
     load8i(ipix + 8 * g, p);
     load8(dat + 8 * g, v);
     int32_t key = p[0];
-    long long cur = __double2ll_rn((double)v[0] * scale);
+    long long cur = to_fixed(v[0], s);
 #pragma unroll
     for (int k = 1; k < 8; k++) {
-      long long t = __double2ll_rn((double)v[k] * scale);
+      long long t = to_fixed(v[k], s);
       if (p[k] == key) {
         cur += t;
       } else {
@@ -368,7 +425,7 @@ __global__ void __launch_bounds__(256) k_scatter_fixed8(unsigned long long *__re
   }
   if (blockIdx.x == 0 && threadIdx.x < (n & 7)) {
     int64_t i = (n8 << 3) + threadIdx.x;
-    flush_i64(acc, ipix[i], __double2ll_rn((double)dat[i] * scale), npix);
+    flush_i64(acc, ipix[i], to_fixed(dat[i], s), npix);
   }
 }
 
@@ -416,11 +473,50 @@ int map2tod_t(void *dat, const void *map, const int32_t *ipix, int64_t n, int64_
   return mk::launch_status("mk_map2tod");
 }
 
+// Per-thread runs over 8 consecutive samples (vector loads), one atomic per
+// run: ~1 add per sample instead of the warp scan's ~5, which matters for
+// FP64 on GB300 where the scan's FP64 adds bound the kernel.
+template <typename T>
+__global__ void __launch_bounds__(256) k_tod2map_atomic8(T *__restrict__ map, const T *__restrict__ dat,
+                                                         const int32_t *__restrict__ ipix, int64_t n,
+                                                         int64_t npix) {
+  const int64_t n8 = n >> 3;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n8; g += stride) {
+    int32_t p[8];
+    T v[8];
+    load8i(ipix + 8 * g, p);
+    load8(dat + 8 * g, v);
+    int32_t key = p[0];
+    T cur = v[0];
+#pragma unroll
+    for (int k = 1; k < 8; k++) {
+      if (p[k] == key) {
+        cur += v[k];
+      } else {
+        if ((uint32_t)key < (uint64_t)npix) atomicAdd(map + key, cur);
+        key = p[k];
+        cur = v[k];
+      }
+    }
+    if ((uint32_t)key < (uint64_t)npix) atomicAdd(map + key, cur);
+  }
+  if (blockIdx.x == 0 && threadIdx.x < (n & 7)) {
+    int64_t i = (n8 << 3) + threadIdx.x;
+    int32_t key = ipix[i];
+    if ((uint32_t)key < (uint64_t)npix) atomicAdd(map + key, dat[i]);
+  }
+}
+
 template <typename T, bool ROWS>
 int tod2map_t(void *map, const void *dat, const int32_t *ipix, int64_t n, int64_t npix,
               const void *rowval, int64_t ndata, cudaStream_t st) {
-  constexpr int U = 4;
   const int B = 256;
+  if (!ROWS && sizeof(T) == 8 && (uintptr_t)dat % 16 == 0 && (uintptr_t)ipix % 16 == 0) {
+    k_tod2map_atomic8<T><<<mk_grid((n + 7) / 8, B, 8), B, 0, st>>>((T *)map, (const T *)dat, ipix, n, npix);
+    return mk::launch_status("mk_tod2map");
+  }
+  constexpr int U = 4;
   unsigned g = mk_grid((n + U - 1) / U, B, 8);
   k_tod2map_atomic<T, ROWS, U><<<g, B, 0, st>>>((T *)map, (const T *)dat, ipix, n, npix,
                                                  (const T *)rowval, ndata);

@@ -12,7 +12,9 @@ namespace mk {
 bool rot_tc_supported(int64_t nrow);
 // bytes of the operand image the kernel stages A from (16-byte aligned buffer)
 size_t rot_tc_bimg_bytes(int64_t nrow);
-// `err` is a device int set to 1 if a bounded wait inside the kernel timed out
+// `err` is a device int set to 1 if a bounded wait inside the kernel timed out.
+// mirror_n > 0 (= 2(ncol-1), with ldr >= mirror_n) also writes the even
+// extension R[., mirror_n - j] = R[., j], 1 <= j <= ncol-2, for a DCT-I.
 int rot_tc_f32(const float *A, const float *X, int64_t ldx, float *R, int64_t ldr, int64_t nrow,
-               int64_t ncol, void *bimg, int *err, cudaStream_t st);
+               int64_t ncol, void *bimg, int *err, cudaStream_t st, int64_t mirror_n = 0);
 }  // namespace mk

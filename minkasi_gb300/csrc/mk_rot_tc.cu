@@ -147,14 +147,50 @@ __global__ void k_bprep(const float *__restrict__ A, int ndet, char *__restrict_
 }
 
 // shared memory: [stage][Ahi 16KB | Alo 16KB | Bhi ndet*128 | Blo ndet*128], 1024-aligned
+// Raw X chunks (32 detectors x 128 samples, 16 KB) are fetched RSTAGE chunks
+// ahead with 4-byte cp.async into a ring in shared memory.  Each thread
+// copies exactly the 32 values of its own sample row, so after its own
+// cp.async.wait_group it can read them back without a CTA barrier.
+constexpr int RSTAGE = 2;
+
+__device__ __forceinline__ void cp_async4(float *dst, const float *src, bool valid) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(dst)), "l"(src),
+               "r"(valid ? 4 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// queue the copy of chunk q (tile, c) of this CTA into raw slot q % RSTAGE;
+// always commits one group so that group counting stays uniform
+__device__ __forceinline__ void prefetch_chunk(const float *__restrict__ X, int64_t ldx, int64_t ncol,
+                                               int nchunk, int64_t ntile, uint32_t q, float *raw,
+                                               int tid) {
+  const int64_t tile = blockIdx.x + (int64_t)(q / nchunk) * gridDim.x;
+  const int c = (int)(q % nchunk);
+  if (tile < ntile) {
+    const int64_t my = tile * TILE_M + tid;
+    const bool ok = my < ncol;
+    const float *src = X + (int64_t)(c * KC) * ldx + (ok ? my : 0);
+    float *dst = raw + (size_t)(q % RSTAGE) * KC * TILE_M + tid;
+#pragma unroll
+    for (int kk = 0; kk < KC; kk++) cp_async4(dst + kk * TILE_M, src + (int64_t)kk * ldx, ok);
+  }
+  cp_async_commit();
+}
+
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_rot_tc(const float *__restrict__ X, int64_t ldx, float *__restrict__ R, int64_t ldr, int ndet,
-             int64_t ncol, const char *__restrict__ bimg, int *__restrict__ err) {
+             int64_t ncol, const char *__restrict__ bimg, int *__restrict__ err, int64_t mirror_n) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const uint32_t a_bytes = TILE_M * 128;          // 16 KB
   const uint32_t b_bytes = (uint32_t)ndet * 128;  // per hi or lo tile
   const uint32_t stage_bytes = 2 * a_bytes + 2 * b_bytes;
+  float *raw = (float *)(smem + NSTAGE * stage_bytes);
   __shared__ uint64_t bar_b[NSTAGE], bar_mma[NSTAGE];
   __shared__ uint32_t tmem_base_sh;
   __shared__ int abort_sh;
@@ -187,6 +223,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   // Control flow is CTA-uniform: only thread 0 waits on mbarriers; the
   // outcome reaches the other threads through abort_sh and __syncthreads.
   const int64_t ntile = (ncol + TILE_M - 1) / TILE_M;
+  for (uint32_t q = 0; q < (uint32_t)RSTAGE; q++) prefetch_chunk(X, ldx, ncol, nchunk, ntile, q, raw, tid);
   uint32_t g = 0;  // chunks issued by this CTA so far
   for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
     const int64_t n0 = tile * TILE_M;
@@ -194,15 +231,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     for (int c = 0; c < nchunk; c++, g++) {
       const uint32_t s = g % NSTAGE, use = g / NSTAGE;
       unsigned char *st = smem + s * stage_bytes;
-      // this thread's sample row: 32 detectors of chunk c, split into hi / lo
-      // (global loads issued before the stage wait so their latency overlaps it)
+      // this thread's sample row: 32 detectors of chunk c from the raw ring,
+      // split into hi / lo; then queue the chunk RSTAGE ahead into that slot
       float h[KC], l[KC];
+      cp_async_wait<RSTAGE - 1>();
+      const float *rw = raw + (size_t)(g % RSTAGE) * KC * TILE_M + tid;
 #pragma unroll
       for (int kk = 0; kk < KC; kk++) {
-        float x = (my < ncol) ? __ldcs(X + (int64_t)(c * KC + kk) * ldx + my) : 0.f;
+        float x = rw[kk * TILE_M];
         h[kk] = tf32_round(x);
         l[kk] = tf32_round(x - h[kk]);
       }
+      prefetch_chunk(X, ldx, ncol, nchunk, ntile, g + RSTAGE, raw, tid);
       if (tid == 0) {
         // stage s is free once the MMAs of chunk g-2 have completed
         if (g >= NSTAGE && !mbar_wait(&bar_mma[s], (use - 1) & 1)) {
@@ -257,11 +297,17 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (my < ncol) {
 #pragma unroll
         for (int j = 0; j < 32; j++) __stcs(R + (int64_t)(c0 + j) * ldr + my, v[j]);
+        // even extension for the DCT-I that follows: R[., mirror_n - my] = R[., my]
+        if (mirror_n > 0 && my >= 1 && my <= ncol - 2) {
+#pragma unroll
+          for (int j = 0; j < 32; j++) __stcs(R + (int64_t)(c0 + j) * ldr + (mirror_n - my), v[j]);
+        }
       }
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
     __syncthreads();
   }
+  cp_async_wait<0>();  // no copy into this CTA's shared memory outlives it
   if (abort_sh && tid == 0) {
     atomicExch(err, 1);
     // bounded drain of MMAs possibly still in flight before freeing tensor memory
@@ -285,15 +331,17 @@ bool rot_tc_supported(int64_t nrow) {
 size_t rot_tc_bimg_bytes(int64_t nrow) { return (size_t)nrow * (size_t)nrow * 8; }
 
 int rot_tc_f32(const float *A, const float *X, int64_t ldx, float *R, int64_t ldr, int64_t nrow,
-               int64_t ncol, void *bimg, int *err, cudaStream_t st) {
+               int64_t ncol, void *bimg, int *err, cudaStream_t st, int64_t mirror_n) {
   MK_CHECK_ARG(rot_tc_supported(nrow), "tensor-core rotation supports ndet in {32,64,128,256}, got %lld",
                (long long)nrow);
   MK_CHECK_ARG(bimg && err && ((uintptr_t)bimg % 16) == 0, "tensor-core rotation: bad scratch");
+  MK_CHECK_ARG(mirror_n == 0 || (mirror_n == 2 * (ncol - 1) && ldr >= mirror_n),
+               "tensor-core rotation: bad mirror extent");
   if (ncol <= 0) return MK_OK;
   const int nd = (int)nrow;
   k_bprep<<<(nd * nd + 255) / 256, 256, 0, st>>>(A, nd, (char *)bimg);
   const size_t stage = 2 * (size_t)TILE_M * 128 + 2 * (size_t)nd * 128;
-  const size_t smem = NSTAGE * stage + 1024;
+  const size_t smem = NSTAGE * stage + (size_t)RSTAGE * KC * TILE_M * sizeof(float) + 1024;
   static int attr_set[64] = {0};
   int dev = 0;
   MK_CUDA(cudaGetDevice(&dev));
@@ -307,7 +355,8 @@ int rot_tc_f32(const float *A, const float *X, int64_t ldx, float *R, int64_t ld
   int64_t ntile = (ncol + TILE_M - 1) / TILE_M;
   int64_t grid = (int64_t)sm_count() * per_sm;
   if (grid > ntile) grid = ntile;
-  k_rot_tc<<<(unsigned)grid, NTHREADS, smem, st>>>(X, ldx, R, ldr, nd, ncol, (const char *)bimg, err);
+  k_rot_tc<<<(unsigned)grid, NTHREADS, smem, st>>>(X, ldx, R, ldr, nd, ncol, (const char *)bimg, err,
+                                                   mirror_n);
   return launch_status("rot_tc_f32");
 }
 

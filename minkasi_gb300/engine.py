@@ -38,14 +38,29 @@ class MapmakingOperator:
         self.dims = [t.get_data_dims() for t in self.tods]
         self.offsets = np.concatenate([[0], np.cumsum(self.sizes)]).astype(np.int64)
         self.S = int(self.offsets[-1])
-        self.ipix = torch.empty(self.S, dtype=torch.int32, device=self.device)
-        for t, o, n in zip(self.tods, self.offsets, self.sizes):
-            src = t.device_pix(self.tag, self.npix).reshape(-1)
-            self.ipix[o:o + n].copy_(src)
-            view = self.ipix[o:o + n].view(t.get_data_dims())
-            view._mk_npix = self.npix
-            t._dev_pix[self.tag] = view  # the pool replaces the per-TOD copy
-        self.tmp = torch.empty(self.S, dtype=dtype, device=self.device)
+        # one pixel-index pool and one timestream scratch per TodVec, shared by
+        # its operators of every precision (FP64 and FP32 passes never overlap)
+        shared = todvec._shared
+        key = (self.tag, self.npix, self.S)
+        if shared.get("ipix_key") == key:
+            self.ipix = shared["ipix"]
+        else:
+            self.ipix = torch.empty(self.S, dtype=torch.int32, device=self.device)
+            for t, o, n in zip(self.tods, self.offsets, self.sizes):
+                src = t.device_pix(self.tag, self.npix).reshape(-1)
+                self.ipix[o:o + n].copy_(src)
+                view = self.ipix[o:o + n].view(t.get_data_dims())
+                view._mk_npix = self.npix
+                t._dev_pix[self.tag] = view  # the pool replaces the per-TOD copy
+                if isinstance(t.info.get(self.tag), torch.Tensor) and t.info[self.tag].is_cuda:
+                    t.info[self.tag] = view  # and frees the caller's device copy
+            shared.update(ipix_key=key, ipix=self.ipix)
+        nbytes = self.S * torch.finfo(dtype).bits // 8
+        buf = shared.get("tmp")
+        if buf is None or buf.numel() < nbytes:
+            buf = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+            shared["tmp"] = buf
+        self.tmp = buf[:nbytes].view(dtype)
         self.rot_mode = int(rot_mode)
         self.ops = None
         self.plans: Dict[Tuple[int, int], K.NoisePlan] = {}

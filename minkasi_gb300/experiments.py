@@ -65,7 +65,6 @@ def run(config: str = "c1", tol: float = 1e-6, learned: bool = True, pairs: int 
     rhs = mapset.copy()
     tv.make_rhs(rhs)
     hits = make_hits(tv, m)
-    whits = make_hits(tv, m, do_weights=True)   # ~diag(A): the learned preconditioner's D
     pre = jacobi_precon(hits)
     x0 = rhs.copy()
     x0.clear()
@@ -108,22 +107,28 @@ def run(config: str = "c1", tol: float = 1e-6, learned: bool = True, pairs: int 
         shape = (m.nx, m.ny)
         R, E, its = [], [], []
         seed = seed_skies
-        while sum(r.shape[0] for r in R) < pairs:
+        # half the pairs from converged solves on seeded skies, half white
+        n_solve = pairs // 2
+        while sum(r.shape[0] for r in R) < n_solve:
             r, e, it = L.solve_pairs(op64, m, hits.map.reshape(-1), [seed], cfg.pixsize_arcsec)
             R.append(r)
             E.append(e)
             its += it
             seed += 1
-        R = torch.cat(R)[:pairs]
-        E = torch.cat(E)[:pairs]
+        R = [torch.cat(R)[:n_solve]]
+        E = [torch.cat(E)[:n_solve]]
+        rw, ew = L.white_pairs(op32, hits.map, pairs - n_solve)
+        R = torch.cat(R + [rw])
+        E = torch.cat(E + [ew])
+        del rw, ew
         t_pairs = time.perf_counter() - t1
         net = L.ConvNet.init(seed=0, device=dev)
         t2 = time.perf_counter()
-        hist_loss = L.train(net, whits.map, shape, R, E, epochs=epochs)
+        hist_loss = L.train(net, hits.map, shape, R, E, epochs=epochs)
         torch.cuda.synchronize()
         t_train = time.perf_counter() - t2
         del R, E
-        Mlearn = L.LearnedPrecon(whits.map, net, shape)
+        Mlearn = L.LearnedPrecon(hits.map, net, shape)
         xl, tl = timed(lambda: run_pcg_mixed(rhs, x0, tv, pre, tol=tol, inner_precon=Mlearn))
         xlf, tlf = timed(lambda: run_pcg(rhs, x0, tv, Mlearn, maxiter=5000, tol=tol, verbose=False))
         # held-out skies: iterations to tol, learned vs Jacobi (FP64 PCG)
@@ -148,6 +153,106 @@ def run(config: str = "c1", tol: float = 1e-6, learned: bool = True, pairs: int 
     return out
 
 
+def hit_density(hits: torch.Tensor) -> float:
+    """Hit pixels / pixels inside the convex hull of the hit pixels."""
+    from scipy.spatial import ConvexHull, Delaunay
+
+    h = hits.detach().cpu().numpy()
+    pts = np.argwhere(h > 0)
+    if len(pts) < 3:
+        return 1.0
+    hull = pts[ConvexHull(pts).vertices]
+    x0, y0 = pts.min(0)
+    x1, y1 = pts.max(0)
+    gx, gy = np.meshgrid(np.arange(x0, x1 + 1), np.arange(y0, y1 + 1), indexing="ij")
+    inside = Delaunay(hull).find_simplex(np.stack([gx.ravel(), gy.ravel()], 1)) >= 0
+    return float(len(pts) / max(int(inside.sum()), 1))
+
+
+def run_large(config: str = "c4", tol: float = 1e-6, max_iter: int = 3000, wall_limit_s: float = 900.0,
+              log=print) -> dict:
+    """The batching configuration: TODs generated one at a time (each TOD's
+    RHS contribution is accumulated and its timestream dropped), one pooled
+    operator per precision over all TODs, per-iteration times of FP64 Jacobi
+    PCG and of the mixed-precision PCG, and a mixed-precision solve to ``tol``
+    (bounded by ``wall_limit_s``)."""
+    from . import kernels as K
+    from .maps import SkyMap
+    from .noise import NoiseSmoothedSVD
+    from .pcg import DevicePCG, MixedOp
+    from .synth import make_tod_info, tod_shapes
+    from .tods import Tod, TodVec
+
+    dev = torch.device("cuda", torch.cuda.current_device())
+    cfg = CONFIGS[config]
+    t0 = time.perf_counter()
+    m = SkyMap(nx=cfg.nx, ny=cfg.ny, device=dev)
+    rhs = torch.zeros(m.npix, dtype=torch.float64, device=dev)
+    tv = TodVec()
+    for k, (ndet, n) in enumerate(tod_shapes(cfg)):
+        info = make_tod_info(cfg, k, ndet, n, dev, with_radec=False)
+        tod = Tod(info)
+        tod.set_noise(NoiseSmoothedSVD)
+        dd = tod.noise.apply_noise(info["dat_calib"])
+        K.tod2map(rhs, dd, info["ipix"])
+        del dd
+        tod.info["dat_calib"] = torch.empty((ndet, n), dtype=torch.float64, device="meta")
+        tv.add_tod(tod)
+        del tod, info
+        if (k + 1) % 25 == 0:
+            log(f"  {k + 1}/{cfg.ntod} TODs, {torch.cuda.memory_allocated() / 1e9:.1f} GB allocated")
+    hits = make_hits(tv, m).map.reshape(-1)
+    pre = torch.where(hits > 0, 1.0 / hits.clamp(min=1), torch.zeros_like(hits))
+    op64 = tv.engine(m, torch.float64)
+    op32 = tv.engine(m, torch.float32)
+    torch.cuda.synchronize()
+    out = {"config": config, "ntod": tv.ntod, "samples": tv.get_nsamp(), "npix": m.npix,
+           "setup_s": time.perf_counter() - t0, "hit_density_in_footprint": hit_density(hits.view(m.nx, m.ny)),
+           "tod2map_kernel_f64": op64.method, "tod2map_kernel_f32": op32.method,
+           "rot_mode_f64": op64.rot_mode, "rot_mode_f32": op32.rot_mode,
+           "gpu_mem_GB": torch.cuda.max_memory_allocated() / 1e9}
+
+    def per_iter(op, b, M, n_it):
+        x = torch.zeros_like(b)
+        st = DevicePCG(op, b, x, M, graph=True)
+        st.start()
+        st.step()
+        st.step()  # eager, then the captured graph
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n_it):
+            st.step()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n_it
+
+    S = out["samples"]
+    ms64 = per_iter(op64, rhs, pre, 2)
+    out["jacobi_f64_iter"] = {"ms": ms64, "Msamp_per_s": S / ms64 / 1e3}
+    msmx = per_iter(MixedOp(op32, m.npix, dev), rhs, pre, 5)
+    out["mixed_iter"] = {"ms": msmx, "Msamp_per_s": S / msmx / 1e3}
+    # mixed-precision solve to tol, bounded in wall time
+    mp = m.copy()
+    mp.map.copy_(rhs.view(m.nx, m.ny))
+    b = Mapset()
+    b.add_map(mp)
+    x0 = b.copy()
+    x0.clear()
+    pre_ms = b.copy()
+    pre_ms.maps[0].map.copy_(pre.view(m.nx, m.ny))
+    hist = []
+    t1 = time.perf_counter()
+    budget = max(50, min(max_iter, int(wall_limit_s * 1e3 / max(msmx * 1.3, 1e-3))))
+    xs, tm = timed(lambda: run_pcg_mixed(b, x0, tv, pre_ms, tol=tol, max_iter=budget, history=hist))
+    out["mixed_solve"] = {"iters": xs.niter, "fp64_residuals": xs.outer, "wall_s": tm,
+                          "true_rel_residual": xs.rel_residual, "reached_tol": xs.rel_residual <= tol,
+                          "iteration_budget": budget}
+    out["jacobi_f64_projected_s"] = xs.niter * ms64 / 1e3
+    out["projected_speedup_mixed_vs_jacobi_f64"] = out["jacobi_f64_projected_s"] / tm
+    return out
+
+
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--config", default="c1")
@@ -156,6 +261,11 @@ if __name__ == "__main__":
     ap.add_argument("--pairs", type=int, default=5000)
     ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--inner", type=int, default=20)
+    ap.add_argument("--large", action="store_true", help="the pooled large-configuration run")
+    ap.add_argument("--wall", type=float, default=900.0)
     a = ap.parse_args()
-    res = run(a.config, a.tol, not a.no_learned, a.pairs, a.epochs, a.inner)
+    if a.large:
+        res = run_large(a.config, a.tol, wall_limit_s=a.wall)
+    else:
+        res = run(a.config, a.tol, not a.no_learned, a.pairs, a.epochs, a.inner)
     print(json.dumps(res))

@@ -1,0 +1,117 @@
+"""Kernel micro-benchmarks on one synthetic TOD shape (CUDA events, best of N).
+
+    python -m minkasi_gb300.kbench [--config c2s] [--only tod2map,map2tod,rot,noise,dct]
+
+Uses the first TOD shape and daisy pointing of a synthetic configuration
+(default c2s: 256 detectors x 130978 samples onto a 1024x1024 map) with
+random data, and reports per kernel the time and, for the projections, the
+algorithmic GB/s (4 B pixel index + one sample per sample; the map is
+L2-resident).  Rotations report their relative error against cuBLAS on the
+FP64 / FP32 units and their TF/s counted as 2 ndet^2 ndata flops
+(3 split products for the tensor-core 3xTF32 kernel are not counted).
+Prints one JSON object.  This is also the command the ncu captures use.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+import torch
+
+from . import kernels as K
+from .synth import CONFIGS, make_tod_info, tod_shapes
+
+
+def best_ms(fn, reps: int = 5, warm: int = 2) -> float:
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    best = float("inf")
+    s = torch.cuda.current_stream()
+    for _ in range(reps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(s)
+        fn()
+        b.record(s)
+        b.synchronize()
+        best = min(best, a.elapsed_time(b))
+    return best
+
+
+def run(config: str = "c2s", only=None) -> dict:
+    dev = torch.device("cuda", torch.cuda.current_device())
+    cfg = CONFIGS[config]
+    ndet, n = tod_shapes(cfg)[0]
+    info = make_tod_info(cfg, 0, ndet, n, dev, with_data=False)
+    ipix = info["ipix"]
+    npix = cfg.nx * cfg.ny
+    N = ndet * n
+    out = {"config": config, "ndet": ndet, "ndata": n, "npix": npix, "samples": N}
+    want = set(only) if only else {"map2tod", "tod2map", "rot", "noise", "dct"}
+    g = torch.Generator(device=dev).manual_seed(0)
+    for dt, es in ((torch.float64, 8), (torch.float32, 4)):
+        tag = "f64" if es == 8 else "f32"
+        dat = torch.randn((ndet, n), generator=g, dtype=dt, device=dev)
+        mp = torch.randn(npix, generator=g, dtype=dt, device=dev)
+        if "map2tod" in want:
+            d2 = torch.empty_like(dat)
+            ms = best_ms(lambda: K.map2tod(d2, mp, ipix, False))
+            out[f"map2tod_{tag}"] = {"ms": ms, "GBs": N * (4 + es) / ms / 1e6}
+        if "tod2map" in want:
+            acc = torch.zeros(npix, dtype=dt, device=dev)
+            ms = best_ms(lambda: K.tod2map(acc, dat, ipix))
+            out[f"tod2map_atomic_{tag}"] = {"ms": ms, "GBs": N * (4 + es) / ms / 1e6}
+            hits = torch.zeros(npix, dtype=torch.float64, device=dev)
+            K.tod2map_rows(hits, ipix)
+            hmax = int(hits.max().item())
+            scr = K.FixedScratch(npix, dev)
+            ms = best_ms(lambda: K.tod2map_fixed(acc, dat, ipix, hmax, scr))
+            out[f"tod2map_fixed_{tag}"] = {"ms": ms, "GBs": N * (4 + es) / ms / 1e6}
+            plan = K.PixPlan(ipix, npix)
+            ms = best_ms(lambda: plan.tod2map(acc, dat))
+            out[f"tod2map_sorted_{tag}"] = {"ms": ms, "GBs": N * (4 + es) / ms / 1e6}
+            del plan
+        plan = None
+        if want & {"rot", "noise"}:
+            plan = K.NoisePlan(ndet, n, dt, dev)
+            A = torch.linalg.qr(torch.randn(ndet, ndet, dtype=torch.float64, device="cpu"))[0]
+            A = A.to(dev).to(dt).contiguous()
+        if "rot" in want:
+            ref = plan.rotate(A, dat, rot_mode=1)
+            for mode in ((1, 3) if es == 8 else (1, 2, 3)):
+                try:
+                    y = plan.rotate(A, dat, rot_mode=mode)
+                except K._lib.MkError as e:
+                    out[f"rot{mode}_{tag}"] = {"error": str(e)[:120]}
+                    continue
+                err = float((y - ref).abs().max() / ref.abs().max())
+                ms = best_ms(lambda m=mode: plan.rotate(A, dat, out=y, rot_mode=m))
+                out[f"rot{mode}_{tag}"] = {"ms": ms, "TFs": 2 * ndet * ndet * n / ms / 1e9,
+                                           "GBs": 2 * N * es / ms / 1e6, "rel_err_vs_blas": err}
+        if "noise" in want:
+            w = torch.rand((ndet, n), generator=g, dtype=dt, device=dev)
+            o = torch.empty_like(dat)
+            for mode in ((1, 3) if es == 8 else (1, 2)):
+                try:
+                    ms = best_ms(lambda m=mode: plan.apply(A, A.T.contiguous(), w, dat, out=o, rot_mode=m),
+                                 reps=3)
+                    out[f"apply_noise_rot{mode}_{tag}"] = {"ms": ms, "GBs_algorithmic": 3 * N * es / ms / 1e6}
+                except K._lib.MkError as e:
+                    out[f"apply_noise_rot{mode}_{tag}"] = {"error": str(e)[:120]}
+        if "dct" in want:
+            d = K.DCT1(ndet, n, dt, dev)
+            o = torch.empty_like(dat)
+            ms = best_ms(lambda: d(dat, out=o))
+            out[f"dct1_{tag}"] = {"ms": ms}
+            del d
+        del plan
+        torch.cuda.empty_cache()
+    return out
+
+
+if __name__ == "__main__":
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--config", default="c2s")
+    ap.add_argument("--only", default="")
+    a = ap.parse_args()
+    print(json.dumps(run(a.config, [s for s in a.only.split(",") if s] or None)))

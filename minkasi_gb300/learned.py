@@ -241,6 +241,25 @@ def solve_pairs(op64, m, hits: torch.Tensor, skies: Sequence[int], pix_arcsec: f
     return torch.stack(R), torch.stack(E), iters
 
 
+def white_pairs(op, hits: torch.Tensor, n: int, seed: int = 0):
+    """(A v, v) pairs with v white noise on the hit pixels, scaled by
+    hits^-1/2.  Least squares over such pairs fits M A ~ I in the Frobenius
+    sense (all modes weighted alike), complementing the solve pairs whose
+    errors are dominated by the slowest modes."""
+    dev = hits.device
+    h = hits.reshape(-1)
+    scale = torch.where(h > 0, 1.0 / torch.sqrt(h.clamp(min=1)), torch.zeros_like(h)).to(op.dtype)
+    g = torch.Generator(device=dev).manual_seed(20_000 + seed)
+    R, E = [], []
+    out = torch.empty(h.numel(), dtype=op.dtype, device=dev)
+    for _ in range(n):
+        v = torch.randn(h.numel(), generator=g, dtype=op.dtype, device=dev) * scale
+        op.apply(v, out)
+        R.append(out.float().clone())
+        E.append(v.float())
+    return torch.stack(R), torch.stack(E)
+
+
 def iterations_to(op64, b: torch.Tensor, precon, tol: float = 1e-6, max_iter: int = 2000):
     """PCG iterations until the recursive residual reaches tol, then the FP64
     true residual; ``precon`` is a diagonal map or an object with apply()."""

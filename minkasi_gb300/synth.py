@@ -112,7 +112,7 @@ def _one_over_f(gen: torch.Generator, nrow: int, n: int, cfg: SynthConfig, devic
 
 
 def make_tod_info(cfg: SynthConfig, k: int, ndet: int, ndata: int, device,
-                  with_data: bool = True) -> dict:
+                  with_data: bool = True, with_radec: bool = True) -> dict:
     """info dict of TOD k: 'ipix' (int32, device), 'dat_calib' (float64,
     device) and the RA/dec offsets 'dx', 'dy' in radians."""
     gen = torch.Generator(device=device)
@@ -137,7 +137,9 @@ def make_tod_info(cfg: SynthConfig, k: int, ndet: int, ndata: int, device,
     px = torch.round(x / cfg.pixsize_arcsec + cfg.nx / 2).clamp(0, cfg.nx - 1)
     py = torch.round(y / cfg.pixsize_arcsec + cfg.ny / 2).clamp(0, cfg.ny - 1)
     ipix = (px * cfg.ny + py).to(torch.int32).contiguous()
-    info = {"ipix": ipix, "dx": (x * ARCSEC), "dy": (y * ARCSEC)}
+    info = {"ipix": ipix}
+    if with_radec:  # 16 B per sample: skipped for the largest configurations
+        info["dx"], info["dy"] = x * ARCSEC, y * ARCSEC
     if with_data:
         rad2 = x * x + y * y
         sig = cfg.amp * (1 + rad2 / cfg.theta_c_arcsec ** 2) ** (0.5 - 1.5 * cfg.beta)

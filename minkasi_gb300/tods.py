@@ -206,6 +206,7 @@ class TodVec:
         self.tods: List[Tod] = []
         self.ntod = 0
         self._engines: Dict[Any, Any] = {}
+        self._shared: Dict[str, Any] = {}   # pooled device buffers shared by the engines
         # kernel choices for the batched operator: "auto" = project autotuner
         self.tod2map_method = "auto"
         self.rot_mode = 0
@@ -215,6 +216,7 @@ class TodVec:
         self.tods[-1].set_tag(self.ntod)
         self.ntod += 1
         self._engines.clear()
+        self._shared.clear()
 
     def lims(self) -> Optional[List[float]]:
         if self.ntod == 0:
