@@ -42,12 +42,15 @@ sys.path.insert(0, REPO)
 WORKLOAD = "c2: 32 TODs x 256 det x U[2^17,2^19] samples (truncated), 1024x1024 map at 1in, FP64"
 METRIC = "tod2map GB/s"
 BYTES_PER_SAMPLE = 12  # int32 pixel index + float64 sample
+# measured DRAM bytes per sample (read + write) of each FP64 tod2map kernel
+# on the 256 x 130978 small case (profiles/tod2map_fp64_c2.md)
+NCU_DRAM_BYTES_PER_SAMPLE = {"atomic": (404.58e6 + 2.9e6) / 33530368}
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c2")
@@ -74,13 +77,14 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.lines = []
+        self.lines = []          # (host time, csv line)
+        self.window = None       # (t0, t1) of the timed region
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self._t = threading.Thread(target=self._read, daemon=True)
             self._t.start()
@@ -90,7 +94,10 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def mark(self, t0: float, t1: float) -> None:
+        self.window = (t0, t1)
 
     def __exit__(self, *a):
         if self.proc is not None:
@@ -101,9 +108,24 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        """Samples taken inside the timed window; if the window is shorter
+        than the sampling period, the samples just before and after it."""
         sm, mx, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        lines = self.lines
+        scope = "timed region"
+        if self.window is not None:
+            t0, t1 = self.window
+            inside = [l for t, l in lines if t0 <= t <= t1]
+            if not inside:
+                before = [l for t, l in lines if t < t0][-1:]
+                after = [l for t, l in lines if t > t1][:1]
+                inside = before + after
+                scope = "nearest samples around the timed region"
+            lines = inside
+        else:
+            lines = [l for _, l in lines]
+        for ln in lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 8:
                 continue
@@ -116,7 +138,7 @@ class ClockSampler:
                 if val.lower().startswith("active"):
                     reasons.add(nm)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "scope": scope}
 
 
 # ---------------------------------------------------------------- workload
@@ -144,7 +166,7 @@ def build_workload(cfg_name, device, with_noise):
     return cfg, tv, m
 
 
-def time_steps(fn, steps, warmup, stream):
+def time_steps(fn, steps, warmup, stream, clk=None):
     import torch
     for _ in range(warmup):
         fn()
@@ -156,9 +178,11 @@ def time_steps(fn, steps, warmup, stream):
         fn()
         b.record(stream)
     torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    if clk is not None:
+        clk.mark(t0, t1)
     per = [a.elapsed_time(b) for a, b in ev]
-    return sum(per), per, wall
+    return sum(per), per, t1 - t0
 
 
 # ---------------------------------------------------------------- CPU baseline
@@ -278,7 +302,7 @@ def run_ours(args):
     # dominant-kernel timing: the scatter kernel alone, on the launching stream
     parallel.barrier()
     with ClockSampler(local) as clk:
-        total_ms, per, wall = time_steps(step, args.steps, args.warmup, stream)
+        total_ms, per, wall = time_steps(step, args.steps, args.warmup, stream, clk)
     parallel.barrier()
     tmax = torch.tensor([total_ms], dtype=torch.float64, device=dev)
     if world > 1:
@@ -293,22 +317,35 @@ def run_ours(args):
     h2d = sum(h.numel() * 8 for h in host)
     devbuf = [torch.empty_like(t.info["dat_calib"]) for t in tv.tods]
 
-    def e2e_step():
+    def e2e_zero_copy():
+        # SkyMap.tod2map on pinned host timestreams: the kernel reads them
+        # over NVLink-C2C in place, no staging copy
+        m.clear()
+        for t, h in zip(tv.tods, host):
+            m.tod2map(t, h)
+        return m.map.cpu()
+
+    def e2e_copy():
         m.clear()
         for t, h, d in zip(tv.tods, host, devbuf):
             d.copy_(h, non_blocking=True)
             m.tod2map(t, d)
         return m.map.cpu()
 
-    for _ in range(args.warmup):
-        e2e_step()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
-    torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / args.steps
+    def wall(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            fn()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t0) / args.steps
+
+    e2e_s = wall(e2e_zero_copy)
+    e2e_copy_s = wall(e2e_copy)
     e2e_gbs = world * S * BYTES_PER_SAMPLE / e2e_s / 1e9
+    e2e_copy_gbs = world * S * BYTES_PER_SAMPLE / e2e_copy_s / 1e9
     del devbuf, host
 
     # extras: the full hot path per PCG iteration
@@ -330,13 +367,11 @@ def run_ours(args):
     if rank != 0:
         return
     clocks = clk.summary()
-    traffic = None
-    tr_file = os.path.join(REPO, "profiles", "tod2map_c2_traffic.json")
-    if os.path.exists(tr_file):
-        try:
-            traffic = json.load(open(tr_file)).get(op.method)
-        except (OSError, ValueError):
-            traffic = None
+    # DRAM bytes per sample of the scatter kernel from one ncu capture of the
+    # small case (dram__bytes_read.sum + dram__bytes_write.sum, scaled to a
+    # full launch by the sample count); see profiles/tod2map_fp64_c2.md
+    per_sample = NCU_DRAM_BYTES_PER_SAMPLE.get(op.method)
+    traffic = None if per_sample is None else per_sample * S
     line = {
         "metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
@@ -348,7 +383,9 @@ def run_ours(args):
                      "frac": gbs / world / peak, "traffic": traffic,
                      "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"},
         "e2e": {"value": e2e_gbs, "unit": "GB/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": op.npix * 8},
+                "d2h_bytes_per_step": op.npix * 8,
+                "mode": "SkyMap.tod2map per TOD on pinned host timestreams read in place by the kernel",
+                "with_staging_copy": e2e_copy_gbs},
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clocks,
         "cpu_baseline": cpu,

@@ -37,6 +37,16 @@ def _dev(t: torch.Tensor, name: str) -> None:
         raise ValueError(f"{name} must be C-contiguous")
 
 
+def _dev_or_pinned(t: torch.Tensor, name: str) -> None:
+    """A CUDA tensor, or a pinned host tensor that the kernel reads in place
+    (zero copy: with unified addressing a pinned host pointer is valid on the
+    device, and on a Grace-Blackwell node the reads travel over NVLink-C2C)."""
+    if not (t.is_cuda or (t.device.type == "cpu" and t.is_pinned())):
+        raise ValueError(f"{name} must be a CUDA tensor or a pinned host tensor (no CPU fallback)")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be C-contiguous")
+
+
 def dtype_code(t: torch.Tensor) -> int:
     try:
         return _DT[t.dtype]
@@ -72,8 +82,9 @@ def map2tod(dat: torch.Tensor, map: torch.Tensor, ipix: torch.Tensor, do_add: bo
 
 
 def tod2map(map: torch.Tensor, dat: torch.Tensor, ipix: torch.Tensor) -> None:
-    """map.flat[ipix] += dat with warp-aggregated atomics (mk_tod2map)."""
-    _dev(dat, "dat"), _dev(map, "map"), _ipix(ipix, dat.shape)
+    """map.flat[ipix] += dat with warp-aggregated atomics (mk_tod2map).
+    ``dat`` may be a pinned host tensor, read in place by the kernel."""
+    _dev_or_pinned(dat, "dat"), _dev(map, "map"), _ipix(ipix, dat.shape)
     if map.dtype != dat.dtype:
         raise TypeError("map and dat must have the same dtype")
     ndet, ndata = _nd(dat)

@@ -143,9 +143,15 @@ class SkyMap:
         if not do_add:
             self.clear()
         ipix = self.get_pix(tod)
-        d = dat if isinstance(dat, torch.Tensor) else as_device(dat, self.map.dtype)
-        if d.dtype != self.map.dtype:
-            d = d.to(self.map.dtype)
+        if isinstance(dat, torch.Tensor) and dat.device.type == "cpu" and dat.is_pinned() \
+                and dat.dtype == self.map.dtype and dat.is_contiguous():
+            d = dat  # pinned host timestream: the scatter kernel reads it in place
+        else:
+            d = dat if isinstance(dat, torch.Tensor) else as_device(dat, self.map.dtype)
+            if not d.is_cuda:
+                d = d.to(self.map.device)
+            if d.dtype != self.map.dtype:
+                d = d.to(self.map.dtype)
         K.tod2map(self.map, d, ipix)
         if self.purge_pixellization:
             tod.clear_saved_pix(self.tag)

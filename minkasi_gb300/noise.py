@@ -15,6 +15,7 @@ so the operator vT diag(w) DCT v is unchanged by it.
 """
 from __future__ import annotations
 
+from collections import OrderedDict
 from typing import Dict, Optional, Tuple
 
 import numpy as np
@@ -23,13 +24,20 @@ import torch
 from . import kernels as K
 from .maps import as_device, default_device
 
-_PLAN_CACHE: Dict[Tuple[int, int, torch.dtype, str], K.NoisePlan] = {}
+_PLAN_CACHE: "OrderedDict[Tuple[int, int, torch.dtype, str], K.NoisePlan]" = OrderedDict()
+_PLAN_CACHE_SIZE = 4  # each plan holds an FFT workspace of ~40 B per sample
 
 
 def noise_plan(ndet: int, ndata: int, dtype: torch.dtype, device) -> K.NoisePlan:
+    """Plan for one-off apply_noise calls, from a small LRU cache (the batched
+    operator keeps its own plans on one shared workspace)."""
     key = (int(ndet), int(ndata), dtype, str(device))
-    if key not in _PLAN_CACHE:
-        _PLAN_CACHE[key] = K.NoisePlan(ndet, ndata, dtype, device)
+    if key in _PLAN_CACHE:
+        _PLAN_CACHE.move_to_end(key)
+        return _PLAN_CACHE[key]
+    while len(_PLAN_CACHE) >= _PLAN_CACHE_SIZE:
+        _PLAN_CACHE.popitem(last=False)
+    _PLAN_CACHE[key] = K.NoisePlan(ndet, ndata, dtype, device)
     return _PLAN_CACHE[key]
 
 

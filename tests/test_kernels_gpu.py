@@ -104,6 +104,16 @@ def test_tod2map_large_runs_f64_f32(K):
     assert rel(ms.cpu().numpy(), ref) < 1e-12
 
 
+def test_tod2map_reads_pinned_host_timestream_in_place(K, gold):
+    g = gold("proj.npz")
+    host = torch.from_numpy(np.ascontiguousarray(g["dat"])).pin_memory()
+    m = dev(g["map"])
+    K.tod2map(m, host, dev(g["ipix"]))
+    assert rel(m.cpu().numpy(), g["tod2map_omp"]) < 1e-13
+    with pytest.raises(ValueError):
+        K.tod2map(dev(g["map"]), torch.from_numpy(np.ascontiguousarray(g["dat"])), dev(g["ipix"]))
+
+
 def test_tod2map_rows_hits(K, gold):
     g = gold("solve.npz")
     hits = torch.zeros(int(g["nx"]) * int(g["ny"]), dtype=torch.float64, device=cuda)
