@@ -25,6 +25,13 @@
  *                         bound in minkasi/lib/minkasi.py:10-60 (tod2map_omp_c)
  *  mk_tod2map_sorted   <- tod2map_everyone / tod2map_cached, minkasi/lib/minkasi.c:68-95
  *                         (the reference's owner-computes variants; here deterministic)
+ *  mk_pix_car / mk_pix_wcs_car <- SkyMapCar.pix_from_radec, radec2pix_car and
+ *                         SkyMap.pix_from_radec, minkasi/maps/skymap.py:457-490,958-984,
+ *                         minkasi/maps/utils.py:178-216
+ *  mk_polmap2tod / mk_tod2polmap / mk_pol_precon_mul <- map2tod_{iqu,qu}_omp,
+ *                         tod2map_{iqu,qu}_simple, tod2map_{iqu,qu}_precon_simple,
+ *                         minkasi/lib/minkasi.c:146-245, and PolMap.__mul__,
+ *                         minkasi/maps/polmap.py:624-684
  *  mk_tod2map_rows     <- make_hits' tod2map of a ones / outer(weights, ones) TOD,
  *                         minkasi/mapmaking/tod2map.py:343-400
  *  mk_dct1_*           <- many_fft_r2r_1d / many_fftf_r2r_1d (REDFT00),
@@ -76,6 +83,91 @@ int mk_map2tod(void *dat, const void *map, const int32_t *ipix, int64_t ndet,
  * Replaces tod2map_omp / tod2map_atomic, minkasi/lib/minkasi.c:59-66,97-112. */
 int mk_tod2map(void *map, const void *dat, const int32_t *ipix, int64_t ndet,
                int64_t ndata, int64_t npix, int dtype, void *stream);
+
+/* The same sum as mk_tod2map, with the sample and pixel streams staged
+ * through shared memory by bulk asynchronous copies (a ring of chunks per
+ * CTA, so several chunks per SM are in flight from HBM while the previous
+ * one is reduced).  dat and ipix must be 16-byte aligned device memory (not
+ * host-mapped); MK_ERR_ARG otherwise.  If a copy never arrives, the kernel
+ * stops after a bounded wait and mk_tod2map_status reports it.
+ * Replaces tod2map_omp, minkasi/lib/minkasi.c:97-112. */
+int mk_tod2map_staged(void *map, const void *dat, const int32_t *ipix, int64_t ndet,
+                      int64_t ndata, int64_t npix, int dtype, void *stream);
+
+/* *code = 1 if a mk_tod2map_staged kernel on the current device stopped on
+ * a timed-out wait since the last call (its map update is then incomplete),
+ * else 0.  Reads and clears the flag; synchronises `stream`.  No reference
+ * counterpart (the reference's CPU loops cannot time out). */
+int mk_tod2map_status(int *code, void *stream);
+
+/* ---- pointing -> pixel index ------------------------------------------
+ * ra, dec: n FP64 samples in radians (device); ipix: n int32 (device).
+ * trunc = 0: SkyMapCar.pix_from_radec, minkasi/maps/skymap.py:958-984:
+ *   ipix = int32(round_half_even((ra - ra0) * cosdec / pixsize) * ny
+ *                + (dec - dec0) / pixsize + 0.5)
+ * trunc = 1: radec2pix_car, minkasi/maps/utils.py:178-216:
+ *   ipix = int((ra - ra0) * cosdec / pixsize + 0.5) * ny + int((dec - dec0) / pixsize + 0.5)
+ * ra0 = lims[0], dec0 = lims[2].  Same FP64 operation order as the
+ * reference and no fused multiply-adds: bit-identical indices.  A value
+ * outside the int32 range (or NaN) gives INT32_MIN, as numpy does on x86-64. */
+int mk_pix_car(int32_t *ipix, const double *ra, const double *dec, int64_t n, double ra0,
+               double dec0, double pixsize, double cosdec, int64_t ny, int trunc, void *stream);
+
+/* SkyMap.pix_from_radec, minkasi/maps/skymap.py:457-490, for the CAR WCS of
+ * get_wcs (minkasi/maps/utils.py:13-67).  wcs6 (host): crval1, crval2,
+ * crpix1, crpix2, cdelt1, cdelt2 in degrees.  World -> native rotation with
+ * the default LONPOLE/LATPOLE, CAR projection, p = crpix + x / cdelt, then
+ * ipix = int32(round(p1 - 1) * ny + round(p2 - 1)).  Replaces astropy's
+ * wcs_world2pix on this path; FP64 trigonometry, so a coordinate within a
+ * few ulp of a half-pixel boundary may round the other way than astropy. */
+int mk_pix_wcs_car(int32_t *ipix, const double *ra, const double *dec, int64_t n,
+                   const double *wcs6, int64_t ny, void *stream);
+
+/* ---- polarized projections (PolMap) ------------------------------------
+ * Stokes maps are pixel-major, map[p * npol + k], as the reference's
+ * (nx, ny, npol) array.  With c = cos(twogamma), s = sin(twogamma):
+ *   MK_POL_QU          npol 2  (Q, U)                   minkasi/lib/minkasi.c:162-174,187-194
+ *   MK_POL_IQU         npol 3  (I, Q, U)                minkasi.c:146-159,176-185
+ *   MK_POL_QU_PRECON   npol 3  (QQ, UU, QU)             minkasi.c:196-207
+ *   MK_POL_IQU_PRECON  npol 6  (I, Q, U, QQ, QU, UU)    minkasi.c:231-245
+ * The angle terms come either from cos2g/sin2g (dtype-typed, n each, made
+ * once per TOD by mk_pol_sincos) or, when cos2g is NULL, from twogamma (n
+ * doubles, FP64 only): the reference's argument, evaluated per call. */
+enum { MK_POL_QU = 1, MK_POL_IQU = 2, MK_POL_QU_PRECON = 3, MK_POL_IQU_PRECON = 4 };
+
+/* Stokes components per pixel of a mode (0 for an unknown mode); not a status. */
+int mk_pol_npol(int mode);
+
+/* cos2g[i] = cos(twogamma[i]), sin2g[i] = sin(twogamma[i]) (FP64 math,
+ * stored in dtype).  No reference counterpart: the reference recomputes
+ * them inside every projection call (minkasi.c:146-245). */
+int mk_pol_sincos(void *cos2g, void *sin2g, const double *twogamma, int64_t n, int dtype,
+                  void *stream);
+
+/* dat (+)= the IQU or QU projection of map (modes MK_POL_QU / MK_POL_IQU;
+ * the PRECON modes have no map2tod in the reference either).  Out-of-range
+ * pixels gather 0.  Replaces map2tod_iqu_omp / map2tod_qu_omp,
+ * minkasi/lib/minkasi.c:146-174, called by polmap2tod,
+ * minkasi/mapmaking/map2tod.py:57-122. */
+int mk_polmap2tod(void *dat, const void *map, const void *cos2g, const void *sin2g,
+                  const double *twogamma, const int32_t *ipix, int64_t ndet, int64_t ndata,
+                  int64_t npix, int mode, int dtype, int do_add, void *stream);
+
+/* map += the mode's Stokes weights of dat (atomic adds; one per component
+ * per run of equal pixels).  dat == NULL: d = rowval[det] (rowval == NULL:
+ * 1), the hit / weight maps of make_hits on a PolMap.  Out-of-range pixels
+ * are skipped.  Replaces tod2map_{qu,iqu}_simple and tod2map_{qu,iqu}_precon_simple,
+ * minkasi/lib/minkasi.c:176-207,231-245, called by tod2polmap,
+ * minkasi/mapmaking/tod2map.py:164-215. */
+int mk_tod2polmap(void *map, const void *dat, const void *cos2g, const void *sin2g,
+                  const double *twogamma, const int32_t *ipix, int64_t ndet, int64_t ndata,
+                  int64_t npix, int mode, int dtype, const void *rowval, void *stream);
+
+/* out = P . map per pixel for a PRECON map P (mode MK_POL_QU_PRECON with a
+ * QU map, MK_POL_IQU_PRECON with an IQU map; out may alias map).
+ * Replaces PolMap.__mul__, minkasi/maps/polmap.py:624-684. */
+int mk_pol_precon_mul(void *out, const void *precon, const void *map, int64_t npix, int mode,
+                      int dtype, void *stream);
 
 /* make_hits helper: map[ipix[d,t]] += w[d] (w == NULL: += 1).  w and map
  * dtype-typed.  Replaces the tod2map of np.ones / np.outer(weights, ones)

@@ -28,6 +28,7 @@ class MkError(RuntimeError):
 
 
 _vp, _i64, _i32, _sz = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int, ctypes.c_size_t
+_dbl = ctypes.c_double
 _pp = ctypes.POINTER(ctypes.c_void_p)
 
 # name -> (restype, argtypes)
@@ -36,7 +37,16 @@ SIGNATURES = {
     "mk_version": (_i32, []),
     "mk_map2tod": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _i32, _i32, _vp]),
     "mk_tod2map": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _i32, _vp]),
+    "mk_tod2map_staged": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _i32, _vp]),
+    "mk_tod2map_status": (_i32, [ctypes.POINTER(ctypes.c_int), _vp]),
     "mk_tod2map_rows": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _i32, _vp]),
+    "mk_pix_car": (_i32, [_vp, _vp, _vp, _i64, _dbl, _dbl, _dbl, _dbl, _i64, _i32, _vp]),
+    "mk_pix_wcs_car": (_i32, [_vp, _vp, _vp, _i64, _vp, _i64, _vp]),
+    "mk_pol_npol": (_i32, [_i32]),
+    "mk_pol_sincos": (_i32, [_vp, _vp, _vp, _i64, _i32, _vp]),
+    "mk_polmap2tod": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _i64, _i64, _i32, _i32, _i32, _vp]),
+    "mk_tod2polmap": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _i64, _i64, _i32, _i32, _vp, _vp]),
+    "mk_pol_precon_mul": (_i32, [_vp, _vp, _vp, _i64, _i32, _i32, _vp]),
     "mk_check_pix": (_i32, [_vp, _i64, _i64, ctypes.POINTER(ctypes.c_int64), _vp]),
     "mk_tod2map_fixed_scratch_bytes": (_sz, [_i64]),
     "mk_tod2map_fixed": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _i64, _i32, _vp, _vp]),

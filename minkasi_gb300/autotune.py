@@ -4,7 +4,7 @@ the choice in a JSON file keyed on (GPU, dtype, detector counts, samples,
 map size, hit density).
 
 Cache file: $MINKASI_GB300_AUTOTUNE, else ~/.cache/minkasi_gb300/autotune.json.
-Set MINKASI_GB300_TOD2MAP=atomic|fixed|sorted (or ..._ROT=1|2|3) to force a choice.
+Set MINKASI_GB300_TOD2MAP=atomic|staged|fixed|sorted (or ..._ROT=1|2|3) to force a choice.
 """
 from __future__ import annotations
 
@@ -84,7 +84,7 @@ def choose_tod2map(op, candidates: Optional[Iterable[str]] = None) -> str:
     if forced:
         return forced
     if candidates is None:
-        candidates = ["atomic", "fixed"]
+        candidates = ["atomic", "staged", "fixed"]
         if op.S < (1 << 30) and max(op.sizes) < (1 << 31):
             candidates.append("sorted")  # plan memory 4 B/sample
     key = workload_key(op, "tod2map")

@@ -2,6 +2,10 @@
 #include <stdarg.h>
 #include <string.h>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "mk_common.cuh"
 
 namespace mk {
@@ -26,6 +30,22 @@ int sm_count() {
     cached[dev] = n;
   }
   return cached[dev];
+}
+
+int resident_ctas(const void *kernel, int block, size_t smem) {
+  static std::mutex mu;
+  static std::map<std::pair<const void *, long long>, int> cache;
+  const long long key2 = ((long long)block << 32) | (long long)smem;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find({kernel, key2});
+  if (it != cache.end()) return it->second;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, block, smem) != cudaSuccess || n < 1) {
+    cudaGetLastError();
+    n = 1;
+  }
+  cache[{kernel, key2}] = n;
+  return n;
 }
 
 int launch_status(const char *what) {

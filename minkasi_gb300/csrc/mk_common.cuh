@@ -16,6 +16,11 @@ int sm_count();
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// CTAs of `kernel` that fit on one SM at `block` threads and `smem` bytes of
+// dynamic shared memory (occupancy calculator; cached, the same on every
+// device of one architecture).
+int resident_ctas(const void *kernel, int block, size_t smem);
+
 // Status of the last launch on this thread, folded into an MK status.
 int launch_status(const char *what);
 
@@ -48,4 +53,12 @@ inline unsigned mk_grid(int64_t work_items, int block, int per_sm) {
   int64_t cap = (int64_t)mk::sm_count() * per_sm;
   if (need < 1) need = 1;
   return (unsigned)(need < cap ? need : cap);
+}
+
+// Grid size for a grid-stride kernel: exactly one wave of resident CTAs
+// (registers and shared memory decide how many fit per SM), so that no CTA
+// waits for a second wave and runs in a tail at low occupancy.
+template <typename Kern>
+inline unsigned mk_grid_fit(Kern *kernel, int64_t work_items, int block, size_t smem = 0) {
+  return mk_grid(work_items, block, mk::resident_ctas((const void *)kernel, block, smem));
 }

@@ -17,7 +17,10 @@
 //   G         = Re F, columns 0 and n-1 halved  (k_real_halve; G aliases E)
 //   out       = vT . G                          (GEMM)
 // Halving before the second rotation equals halving after it (a column
-// scale commutes with a left multiplication).
+// scale commutes with a left multiplication).  With the tensor-core rotation
+// (rot_mode 2) the mirror is written by the first rotation's epilogue and the
+// second rotation reads Re F in place and halves while splitting, so k_mirror
+// and k_real_halve do not run.
 #include <cublas_v2.h>
 #include <cufft.h>
 
@@ -312,14 +315,15 @@ int blas_rotate(int dtype, const void *A, const void *X, int64_t ldx, void *R, i
 // mirror_n: see rot_tc_f32 (only the tensor-core kernel fuses the extension;
 // the caller runs k_mirror otherwise).
 int rotate(DctCore *c, int mode, const void *A, const void *X, int64_t ldx, void *R, int64_t ldr,
-           int64_t nrow, int64_t ncol, cudaStream_t st, int64_t mirror_n = 0) {
+           int64_t nrow, int64_t ncol, cudaStream_t st, int64_t mirror_n = 0, int64_t x_stride = 1,
+           int halve_ends = 0) {
   const int dtype = c->dtype;
   if (mode == 0) mode = 1;
   if (mode == 2) {
     MK_CHECK_ARG(dtype == MK_F32, "tensor-core rotation (rot_mode 2) is FP32 only");
     MK_CHECK_ARG(c->tc_bimg != nullptr, "tensor-core rotation needs ndet in {32,64,128,256}");
     return mk::rot_tc_f32((const float *)A, (const float *)X, ldx, (float *)R, ldr, nrow, ncol,
-                          c->tc_bimg, c->tc_err, st, mirror_n);
+                          c->tc_bimg, c->tc_err, st, mirror_n, x_stride, halve_ends);
   }
   MK_CHECK_ARG(mode == 1 || mode == 3, "bad rot_mode %d", mode);
   return blas_rotate(dtype, A, X, ldx, R, ldr, nrow, ncol, mode == 3, st);
@@ -341,6 +345,11 @@ int apply_noise_t(DctCore *c, const T *v, const T *vT, const T *w, int64_t ldw, 
   k_filter_extend<T, C><<<g, 256, 0, st>>>((const C *)c->F, w, ldw, (T *)c->E, n, N, nd);
   if ((rc = mk::launch_status("apply_noise/filter"))) return rc;
   if ((rc = core_fft(c, st))) return rc;
+  if (fused_mirror) {
+    // the tensor-core kernel reads the real parts of F in place (stride 2)
+    // and halves the end columns while splitting its operand
+    return rotate(c, rot_mode, vT, c->F, 2 * n, out, n, nd, n, st, 0, 2, 1);
+  }
   k_real_halve<T, C><<<g, 256, 0, st>>>((const C *)c->F, (T *)c->E, n, nd);
   if ((rc = mk::launch_status("apply_noise/halve"))) return rc;
   return rotate(c, rot_mode, vT, c->E, n, out, n, nd, n, st);

@@ -235,7 +235,7 @@ int pcg_update_t(T *x, T *r, T *z, T *p, const T *Ap, const T *M, int64_t n, dou
   unsigned g = red_grid(n);
   k_pcg_pap<T><<<g, RB, 0, st>>>(p, Ap, n, s, sc);
   k_pcg_xrz<T><<<g, RB, 0, st>>>(x, r, z, p, Ap, M, n, s, sc);
-  k_pcg_p<T><<<mk_grid(n, 256, 8), 256, 0, st>>>(p, z, n, s);
+  k_pcg_p<T><<<mk_grid_fit(k_pcg_p<T>, n, 256), 256, 0, st>>>(p, z, n, s);
   return mk::launch_status("mk_pcg_update");
 }
 
@@ -263,9 +263,9 @@ extern "C" int mk_axpy(void *y, const void *x, double alpha, int64_t n, int dtyp
   MK_CHECK_ARG(x && y, "mk_axpy: null pointer");
   cudaStream_t st = mk::as_stream(stream);
   if (dtype == MK_F64)
-    k_axpy<double><<<mk_grid(n, 256, 8), 256, 0, st>>>((double *)y, (const double *)x, alpha, n);
+    k_axpy<double><<<mk_grid_fit(k_axpy<double>, n, 256), 256, 0, st>>>((double *)y, (const double *)x, alpha, n);
   else
-    k_axpy<float><<<mk_grid(n, 256, 8), 256, 0, st>>>((float *)y, (const float *)x, alpha, n);
+    k_axpy<float><<<mk_grid_fit(k_axpy<float>, n, 256), 256, 0, st>>>((float *)y, (const float *)x, alpha, n);
   return mk::launch_status("mk_axpy");
 }
 
@@ -275,10 +275,10 @@ extern "C" int mk_mul(void *out, const void *a, const void *b, int64_t n, int dt
   MK_CHECK_ARG(out && a && b, "mk_mul: null pointer");
   cudaStream_t st = mk::as_stream(stream);
   if (dtype == MK_F64)
-    k_mul<double><<<mk_grid(n, 256, 8), 256, 0, st>>>((double *)out, (const double *)a,
+    k_mul<double><<<mk_grid_fit(k_mul<double>, n, 256), 256, 0, st>>>((double *)out, (const double *)a,
                                                       (const double *)b, n);
   else
-    k_mul<float><<<mk_grid(n, 256, 8), 256, 0, st>>>((float *)out, (const float *)a, (const float *)b, n);
+    k_mul<float><<<mk_grid_fit(k_mul<float>, n, 256), 256, 0, st>>>((float *)out, (const float *)a, (const float *)b, n);
   return mk::launch_status("mk_mul");
 }
 
@@ -339,10 +339,10 @@ extern "C" int mk_pcg_step_zp(const void *z, const void *r, void *p, int64_t n, 
   unsigned g = red_grid(n);
   if (dtype == MK_F64) {
     k_pcg_zr<double><<<g, RB, 0, st>>>((const double *)r, (const double *)z, n, s, (Scratch *)scratch);
-    k_pcg_p<double><<<mk_grid(n, 256, 8), 256, 0, st>>>((double *)p, (const double *)z, n, s);
+    k_pcg_p<double><<<mk_grid_fit(k_pcg_p<double>, n, 256), 256, 0, st>>>((double *)p, (const double *)z, n, s);
   } else {
     k_pcg_zr<float><<<g, RB, 0, st>>>((const float *)r, (const float *)z, n, s, (Scratch *)scratch);
-    k_pcg_p<float><<<mk_grid(n, 256, 8), 256, 0, st>>>((float *)p, (const float *)z, n, s);
+    k_pcg_p<float><<<mk_grid_fit(k_pcg_p<float>, n, 256), 256, 0, st>>>((float *)p, (const float *)z, n, s);
   }
   return mk::launch_status("mk_pcg_step_zp");
 }
@@ -354,10 +354,10 @@ extern "C" int mk_scale_add(void *out, const void *d, const void *a, const void 
   MK_CHECK_ARG(out && d && a, "mk_scale_add: null pointer");
   cudaStream_t st = mk::as_stream(stream);
   if (dtype == MK_F64)
-    k_scale_add<double><<<mk_grid(n, 256, 8), 256, 0, st>>>((double *)out, (const double *)d,
+    k_scale_add<double><<<mk_grid_fit(k_scale_add<double>, n, 256), 256, 0, st>>>((double *)out, (const double *)d,
                                                             (const double *)a, (const double *)b, n);
   else
-    k_scale_add<float><<<mk_grid(n, 256, 8), 256, 0, st>>>((float *)out, (const float *)d,
+    k_scale_add<float><<<mk_grid_fit(k_scale_add<float>, n, 256), 256, 0, st>>>((float *)out, (const float *)d,
                                                            (const float *)a, (const float *)b, n);
   return mk::launch_status("mk_scale_add");
 }

@@ -12,6 +12,7 @@
 
 #include <mutex>
 
+#include "mk_async.cuh"
 #include "mk_common.cuh"
 
 namespace {
@@ -372,7 +373,7 @@ __device__ __forceinline__ void load8i(const int32_t *__restrict__ p, int32_t (&
 }
 
 template <typename T>
-__global__ void __launch_bounds__(256) k_absmax8(const T *__restrict__ dat, int64_t n, FixHdr *h) {
+__global__ void __launch_bounds__(256, 8) k_absmax8(const T *__restrict__ dat, int64_t n, FixHdr *h) {
   using U = typename AbsBits<T>::U;
   U m = 0;
   const int64_t n8 = n >> 3;
@@ -458,17 +459,19 @@ int map2tod_t(void *dat, const void *map, const int32_t *ipix, int64_t n, int64_
   bool vec = ((uintptr_t)dat % 16 == 0) && ((uintptr_t)ipix % 16 == 0) && n >= 4;
   const int B = 256;
   if (vec) {
-    unsigned g = mk_grid((n >> 2), B, 8);
     if (do_add)
-      k_map2tod_vec<T, true><<<g, B, 0, st>>>((T *)dat, (const T *)map, ipix, n, npix);
+      k_map2tod_vec<T, true><<<mk_grid_fit(k_map2tod_vec<T, true>, n >> 2, B), B, 0, st>>>(
+          (T *)dat, (const T *)map, ipix, n, npix);
     else
-      k_map2tod_vec<T, false><<<g, B, 0, st>>>((T *)dat, (const T *)map, ipix, n, npix);
+      k_map2tod_vec<T, false><<<mk_grid_fit(k_map2tod_vec<T, false>, n >> 2, B), B, 0, st>>>(
+          (T *)dat, (const T *)map, ipix, n, npix);
   } else {
-    unsigned g = mk_grid(n, B, 8);
     if (do_add)
-      k_map2tod_scalar<T, true><<<g, B, 0, st>>>((T *)dat, (const T *)map, ipix, n, npix);
+      k_map2tod_scalar<T, true><<<mk_grid_fit(k_map2tod_scalar<T, true>, n, B), B, 0, st>>>(
+          (T *)dat, (const T *)map, ipix, n, npix);
     else
-      k_map2tod_scalar<T, false><<<g, B, 0, st>>>((T *)dat, (const T *)map, ipix, n, npix);
+      k_map2tod_scalar<T, false><<<mk_grid_fit(k_map2tod_scalar<T, false>, n, B), B, 0, st>>>(
+          (T *)dat, (const T *)map, ipix, n, npix);
   }
   return mk::launch_status("mk_map2tod");
 }
@@ -513,14 +516,222 @@ int tod2map_t(void *map, const void *dat, const int32_t *ipix, int64_t n, int64_
               const void *rowval, int64_t ndata, cudaStream_t st) {
   const int B = 256;
   if (!ROWS && sizeof(T) == 8 && (uintptr_t)dat % 16 == 0 && (uintptr_t)ipix % 16 == 0) {
-    k_tod2map_atomic8<T><<<mk_grid((n + 7) / 8, B, 8), B, 0, st>>>((T *)map, (const T *)dat, ipix, n, npix);
+    k_tod2map_atomic8<T><<<mk_grid_fit(k_tod2map_atomic8<T>, (n + 7) / 8, B), B, 0, st>>>((T *)map, (const T *)dat, ipix, n, npix);
     return mk::launch_status("mk_tod2map");
   }
   constexpr int U = 4;
-  unsigned g = mk_grid((n + U - 1) / U, B, 8);
+  unsigned g = mk_grid_fit(k_tod2map_atomic<T, ROWS, U>, (n + U - 1) / U, B);
   k_tod2map_atomic<T, ROWS, U><<<g, B, 0, st>>>((T *)map, (const T *)dat, ipix, n, npix,
                                                  (const T *)rowval, ndata);
   return mk::launch_status("mk_tod2map");
+}
+
+// ---- tod2map, bulk-staged, warp-specialised ---------------------------------
+// A persistent CTA streams chunks of SCH consecutive samples (pixel indices
+// and values) through a ring of SSTG shared-memory stages.  One producer
+// warp issues the cp.async.bulk copies of each chunk; they complete on the
+// stage's "full" mbarrier.  SCW consumer warps each reduce their 256 samples
+// of the chunk (8 consecutive samples per lane: runs of equal pixels summed in
+// registers, one L2 atomic per run, as k_tod2map_atomic8) and arrive on the
+// stage's "empty" mbarrier, which the producer waits on before refilling the
+// stage.  No CTA-wide barrier sits in the loop, so the consumer warps drift
+// freely and several chunks per CTA are in flight from HBM at any time.
+// Chunk c holds samples [c*SCH, min(c*SCH + SCH, n4)), n4 = n rounded down to
+// a multiple of 4 so every copy is a multiple of 16 bytes; CTA 0 adds the last
+// n - n4 samples with plain loads.  Needs ipix and dat 16-byte aligned device
+// memory.  Every wait is bounded; on a timeout the CTA records it in
+// g_staged_err, the producer stops issuing and waits (bounded) for its copies
+// in flight, and every warp leaves its loop.
+constexpr int SCW = 8;                    // consumer warps
+constexpr int SCH = SCW * 32 * 8;         // samples per chunk (2048)
+constexpr int SSTG = 3;                   // stages in the ring
+constexpr int STHREADS = (SCW + 1) * 32;  // + one producer warp
+
+template <typename T>
+struct StagedSmem {
+  int32_t pix[SSTG][SCH];
+  T val[SSTG][SCH];
+  uint64_t full[SSTG];
+  uint64_t empty[SSTG];
+  int abort;
+};
+
+// 1 once a bounded wait of k_tod2map_staged timed out (mk_tod2map_status)
+__device__ int g_staged_err = 0;
+
+template <typename T>
+__device__ __forceinline__ void staged_issue(StagedSmem<T> &sm, int s, int64_t c, int64_t n4,
+                                             const int32_t *ipix, const T *dat, uint64_t pol) {
+  const int64_t base = c * SCH;
+  const int64_t rem = n4 - base;
+  const uint32_t cnt = (uint32_t)(rem < SCH ? rem : SCH);
+  mk::mbar_expect_tx(&sm.full[s], cnt * (uint32_t)(sizeof(int32_t) + sizeof(T)));
+  mk::bulk_g2s_hint(sm.pix[s], ipix + base, cnt * (uint32_t)sizeof(int32_t), &sm.full[s], pol);
+  mk::bulk_g2s_hint(sm.val[s], dat + base, cnt * (uint32_t)sizeof(T), &sm.full[s], pol);
+}
+
+template <typename V>
+__device__ __forceinline__ V pick4(V a, V b, V c, V d, int i) {
+  return i == 0 ? a : (i == 1 ? b : (i == 2 ? c : d));
+}
+
+// Thread t's 8 samples at sp[8t..8t+7] / sv[8t..8t+7].  The 16-byte
+// shared-memory loads are issued in a per-thread rotated order so that each
+// group of 8 threads served together touches all 32 banks (no conflicts),
+// then put back in sample order with selects.
+template <typename T>
+__device__ __forceinline__ void smem_load8(const int32_t *sp, const T *sv, int t, int32_t (&p)[8], T (&v)[8]) {
+  const int4 *qp = reinterpret_cast<const int4 *>(sp + 8 * t);
+  const int r1 = (t >> 2) & 1;
+  int4 a = qp[r1], b = qp[r1 ^ 1];
+  int4 lo = r1 ? b : a, hi = r1 ? a : b;
+  p[0] = lo.x; p[1] = lo.y; p[2] = lo.z; p[3] = lo.w;
+  p[4] = hi.x; p[5] = hi.y; p[6] = hi.z; p[7] = hi.w;
+  if constexpr (sizeof(T) == 8) {
+    const double2 *qv = reinterpret_cast<const double2 *>(sv + 8 * t);
+    const int r = (t >> 1) & 3;
+    double2 L0 = qv[r], L1 = qv[(1 + r) & 3], L2 = qv[(2 + r) & 3], L3 = qv[(3 + r) & 3];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      double2 P = pick4(L0, L1, L2, L3, (j - r) & 3);
+      v[2 * j] = P.x;
+      v[2 * j + 1] = P.y;
+    }
+  } else {
+    const float4 *qv = reinterpret_cast<const float4 *>(sv + 8 * t);
+    float4 c = qv[r1], d = qv[r1 ^ 1];
+    float4 vl = r1 ? d : c, vh = r1 ? c : d;
+    v[0] = vl.x; v[1] = vl.y; v[2] = vl.z; v[3] = vl.w;
+    v[4] = vh.x; v[5] = vh.y; v[6] = vh.z; v[7] = vh.w;
+  }
+}
+
+template <typename T, int M>
+__device__ __forceinline__ void reduce_runs(T *__restrict__ map, const int32_t *p, const T *v, int64_t npix) {
+  int32_t key = p[0];
+  T cur = v[0];
+#pragma unroll
+  for (int k = 1; k < M; k++) {
+    if (p[k] == key) {
+      cur += v[k];
+    } else {
+      if ((uint32_t)key < (uint64_t)npix) atomicAdd(map + key, cur);
+      key = p[k];
+      cur = v[k];
+    }
+  }
+  if ((uint32_t)key < (uint64_t)npix) atomicAdd(map + key, cur);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(STHREADS) k_tod2map_staged(T *__restrict__ map, const T *__restrict__ dat,
+                                                             const int32_t *__restrict__ ipix, int64_t n,
+                                                             int64_t npix) {
+  extern __shared__ __align__(128) unsigned char smraw[];
+  StagedSmem<T> &sm = *reinterpret_cast<StagedSmem<T> *>(smraw);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int64_t n4 = n & ~(int64_t)3;
+  const int64_t nchunk = (n4 + SCH - 1) / SCH;
+  const int64_t G = gridDim.x;
+  if (tid == 0) {
+    for (int s = 0; s < SSTG; s++) {
+      mk::mbar_init(&sm.full[s], 1);
+      mk::mbar_init(&sm.empty[s], SCW);
+    }
+    sm.abort = 0;
+    mk::mbar_init_fence();
+  }
+  __syncthreads();
+  volatile int *abort_flag = &sm.abort;
+  int64_t issued = 0;
+
+  if (warp == SCW) {
+    // ---- producer
+    if (lane == 0) {
+      const uint64_t pol = mk::l2_evict_first_policy();
+      for (int64_t c = blockIdx.x; c < nchunk; c += G, issued++) {
+        const int s = (int)(issued % SSTG);
+        if (issued >= SSTG) {
+          // wait until every consumer warp released the stage's previous chunk
+          if (!mk::mbar_wait(&sm.empty[s], (uint32_t)(((issued / SSTG) - 1) & 1))) {
+            atomicExch(&g_staged_err, 1);
+            *abort_flag = 1;
+          }
+        }
+        if (*abort_flag) break;
+        mk::fence_proxy_async_smem();
+        staged_issue(sm, s, c, n4, ipix, dat, pol);
+      }
+    }
+  } else {
+    // ---- consumers: warp w takes samples [w*256, w*256 + 256) of every chunk
+    const int t = warp * 32 + lane;
+    const int j0 = t * 8;
+    int64_t k = 0;
+    for (int64_t c = blockIdx.x; c < nchunk; c += G, k++) {
+      const int s = (int)(k % SSTG);
+      const bool ok = mk::mbar_wait(&sm.full[s], (uint32_t)((k / SSTG) & 1));
+      const int ab = __shfl_sync(0xffffffffu, *abort_flag, 0);  // one warp-uniform reading
+      if (__any_sync(0xffffffffu, !ok) || ab) {
+        if (lane == 0) {
+          atomicExch(&g_staged_err, 1);
+          *abort_flag = 1;
+        }
+        break;
+      }
+      const int64_t rem = n4 - c * SCH;
+      const int cnt = (int)(rem < SCH ? rem : SCH);
+      if (j0 + 8 <= cnt) {
+        int32_t p[8];
+        T v[8];
+        smem_load8(sm.pix[s], sm.val[s], t, p, v);
+        reduce_runs<T, 8>(map, p, v, npix);
+      } else if (j0 < cnt) {  // cnt is a multiple of 4: exactly 4 left
+        int32_t p[4];
+        T v[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          p[j] = sm.pix[s][j0 + j];
+          v[j] = sm.val[s][j0 + j];
+        }
+        reduce_runs<T, 4>(map, p, v, npix);
+      }
+      __syncwarp();
+      if (lane == 0) mk::mbar_arrive(&sm.empty[s]);
+    }
+    if (blockIdx.x == 0 && warp == 0 && lane < (int)(n - n4)) {
+      const int64_t i = n4 + lane;
+      const int32_t key = ipix[i];
+      if ((uint32_t)key < (uint64_t)npix) atomicAdd(map + key, dat[i]);
+    }
+  }
+  // every loop above ends in bounded time; after an abort, no copy of this
+  // CTA may still be landing in shared memory when it exits
+  __syncthreads();
+  if (warp == SCW && lane == 0 && *abort_flag) {
+    const int64_t from = issued > SSTG ? issued - SSTG : 0;
+    for (int64_t j = from; j < issued; j++) mk::mbar_wait(&sm.full[j % SSTG], (uint32_t)((j / SSTG) & 1));
+  }
+}
+
+template <typename T>
+int tod2map_staged_t(void *map, const void *dat, const int32_t *ipix, int64_t n, int64_t npix,
+                     cudaStream_t st) {
+  const size_t smem = sizeof(StagedSmem<T>);
+  static bool attr_set[64] = {false};
+  int dev = 0;
+  MK_CUDA(cudaGetDevice(&dev));
+  if (dev >= 0 && dev < 64 && !attr_set[dev]) {
+    MK_CUDA(cudaFuncSetAttribute(k_tod2map_staged<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set[dev] = true;
+  }
+  const int64_t nchunk = ((n & ~(int64_t)3) + SCH - 1) / SCH;
+  const int per_sm = mk::resident_ctas((const void *)k_tod2map_staged<T>, STHREADS, smem);
+  int64_t g = (int64_t)mk::sm_count() * per_sm;
+  if (g > nchunk) g = nchunk;
+  if (g < 1) g = 1;
+  k_tod2map_staged<T><<<(unsigned)g, STHREADS, smem, st>>>((T *)map, (const T *)dat, ipix, n, npix);
+  return mk::launch_status("mk_tod2map_staged");
 }
 
 template <typename T>
@@ -530,16 +741,16 @@ int tod2map_fixed_t(void *map, const void *dat, const int32_t *ipix, int64_t n, 
   unsigned long long *acc = (unsigned long long *)((char *)scratch + sizeof(FixHdr));
   const bool vec = ((uintptr_t)dat % 16 == 0) && ((uintptr_t)ipix % 16 == 0);
   if (vec) {
-    k_absmax8<T><<<mk_grid((n + 7) / 8, 256, 8), 256, 0, st>>>((const T *)dat, n, h);
-    k_scatter_fixed8<T><<<mk_grid((n + 7) / 8, 256, 8), 256, 0, st>>>(acc, (const T *)dat, ipix, n, npix,
+    k_absmax8<T><<<mk_grid_fit(k_absmax8<T>, (n + 7) / 8, 256), 256, 0, st>>>((const T *)dat, n, h);
+    k_scatter_fixed8<T><<<mk_grid_fit(k_scatter_fixed8<T>, (n + 7) / 8, 256), 256, 0, st>>>(acc, (const T *)dat, ipix, n, npix,
                                                                       hbits, h);
   } else {
-    k_absmax<T><<<mk_grid(n, 256, 8), 256, 0, st>>>((const T *)dat, n, h);
+    k_absmax<T><<<mk_grid_fit(k_absmax<T>, n, 256), 256, 0, st>>>((const T *)dat, n, h);
     constexpr int U = 4;
-    k_scatter_fixed<T, U><<<mk_grid((n + U - 1) / U, 256, 8), 256, 0, st>>>(acc, (const T *)dat, ipix, n,
+    k_scatter_fixed<T, U><<<mk_grid_fit(k_scatter_fixed<T, U>, (n + U - 1) / U, 256), 256, 0, st>>>(acc, (const T *)dat, ipix, n,
                                                                             npix, hbits, h);
   }
-  k_fixed_finalize<T><<<mk_grid(npix, 256, 8), 256, 0, st>>>((T *)map, acc, npix, h, n);
+  k_fixed_finalize<T><<<mk_grid_fit(k_fixed_finalize<T>, npix, 256), 256, 0, st>>>((T *)map, acc, npix, h, n);
   k_fixed_reset<T><<<1, 1, 0, st>>>(h);
   return mk::launch_status("mk_tod2map_fixed");
 }
@@ -576,6 +787,42 @@ extern "C" int mk_tod2map(void *map, const void *dat, const int32_t *ipix, int64
                          : tod2map_t<float, false>(map, dat, ipix, n, npix, nullptr, 1, st);
 }
 
+static bool is_device_ptr(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice;
+}
+
+extern "C" int mk_tod2map_staged(void *map, const void *dat, const int32_t *ipix, int64_t ndet,
+                                 int64_t ndata, int64_t npix, int dtype, void *stream) {
+  MK_CHECK_ARG(ndet >= 0 && ndata >= 0 && npix >= 0, "mk_tod2map_staged: negative size");
+  MK_CHECK_ARG(MK_DTYPE_OK(dtype), "mk_tod2map_staged: bad dtype %d", dtype);
+  int64_t n = ndet * ndata;
+  if (n == 0) return MK_OK;
+  MK_CHECK_ARG(dat && map && ipix, "mk_tod2map_staged: null pointer");
+  MK_CHECK_ARG((uintptr_t)dat % 16 == 0 && (uintptr_t)ipix % 16 == 0,
+               "mk_tod2map_staged: dat and ipix must be 16-byte aligned");
+  MK_CHECK_ARG(is_device_ptr(dat) && is_device_ptr(ipix) && is_device_ptr(map),
+               "mk_tod2map_staged: map, dat and ipix must be device memory");
+  cudaStream_t st = mk::as_stream(stream);
+  return dtype == MK_F64 ? tod2map_staged_t<double>(map, dat, ipix, n, npix, st)
+                         : tod2map_staged_t<float>(map, dat, ipix, n, npix, st);
+}
+
+extern "C" int mk_tod2map_status(int *code, void *stream) {
+  MK_CHECK_ARG(code, "mk_tod2map_status: null pointer");
+  cudaStream_t st = mk::as_stream(stream);
+  *code = 0;
+  MK_CUDA(cudaMemcpyFromSymbolAsync(code, g_staged_err, sizeof(int), 0, cudaMemcpyDeviceToHost, st));
+  const int zero = 0;
+  MK_CUDA(cudaMemcpyToSymbolAsync(g_staged_err, &zero, sizeof(int), 0, cudaMemcpyHostToDevice, st));
+  MK_CUDA(cudaStreamSynchronize(st));
+  return MK_OK;
+}
+
 extern "C" int mk_tod2map_rows(void *map, const void *w, const int32_t *ipix, int64_t ndet,
                                int64_t ndata, int64_t npix, int dtype, void *stream) {
   MK_CHECK_ARG(ndet >= 0 && ndata >= 0 && npix >= 0, "mk_tod2map_rows: negative size");
@@ -598,7 +845,7 @@ extern "C" int mk_check_pix(const int32_t *ipix, int64_t n, int64_t npix, int64_
   unsigned long long *d = nullptr;
   MK_CUDA(cudaMallocAsync((void **)&d, sizeof(*d), st));
   MK_CUDA(cudaMemsetAsync(d, 0, sizeof(*d), st));
-  k_count_bad<<<mk_grid(n, 256, 8), 256, 0, st>>>(ipix, n, npix, d);
+  k_count_bad<<<mk_grid_fit(k_count_bad, n, 256), 256, 0, st>>>(ipix, n, npix, d);
   int rc = mk::launch_status("mk_check_pix");
   unsigned long long h = 0;
   cudaError_t e1 = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, st);
@@ -656,7 +903,7 @@ extern "C" int mk_pixplan_create(mk_pixplan **plan, const int32_t *ipix, int64_t
   if ((e = cudaMalloc(&keys_out, nb)) != cudaSuccess) return fail("cudaMalloc", e);
   if ((e = cudaMalloc(&idx_in, nb)) != cudaSuccess) return fail("cudaMalloc", e);
   if (n > 0) {
-    k_iota<<<mk_grid(n, 256, 8), 256, 0, st>>>(idx_in, n);
+    k_iota<<<mk_grid_fit(k_iota, n, 256), 256, 0, st>>>(idx_in, n);
     if ((e = cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, ipix, keys_out, idx_in, pl->perm,
                                              (int)n, 0, end_bit, st)) != cudaSuccess)
       return fail("sort sizing", e);
@@ -665,7 +912,7 @@ extern "C" int mk_pixplan_create(mk_pixplan **plan, const int32_t *ipix, int64_t
                                              (int)n, 0, end_bit, st)) != cudaSuccess)
       return fail("sort", e);
   }
-  k_pix_offsets<<<mk_grid(npix + 1, 256, 8), 256, 0, st>>>(keys_out, n, pl->off, npix);
+  k_pix_offsets<<<mk_grid_fit(k_pix_offsets, npix + 1, 256), 256, 0, st>>>(keys_out, n, pl->off, npix);
   if ((e = cudaGetLastError()) != cudaSuccess) return fail("offsets", e);
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return fail("sync", e);
   cudaFree(keys_out);
@@ -682,12 +929,11 @@ extern "C" int mk_tod2map_sorted(void *map, const void *dat, const mk_pixplan *p
   if (plan->n == 0) return MK_OK;
   MK_CHECK_ARG(dat, "mk_tod2map_sorted: null dat");
   cudaStream_t st = mk::as_stream(stream);
-  unsigned g = mk_grid(plan->npix * 32, 256, 8);
   if (dtype == MK_F64)
-    k_tod2map_sorted<double><<<g, 256, 0, st>>>((double *)map, (const double *)dat, plan->perm,
+    k_tod2map_sorted<double><<<mk_grid_fit(k_tod2map_sorted<double>, plan->npix * 32, 256), 256, 0, st>>>((double *)map, (const double *)dat, plan->perm,
                                                  plan->off, plan->npix);
   else
-    k_tod2map_sorted<float><<<g, 256, 0, st>>>((float *)map, (const float *)dat, plan->perm,
+    k_tod2map_sorted<float><<<mk_grid_fit(k_tod2map_sorted<float>, plan->npix * 32, 256), 256, 0, st>>>((float *)map, (const float *)dat, plan->perm,
                                                 plan->off, plan->npix);
   return mk::launch_status("mk_tod2map_sorted");
 }

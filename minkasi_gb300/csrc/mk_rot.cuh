@@ -15,6 +15,9 @@ size_t rot_tc_bimg_bytes(int64_t nrow);
 // `err` is a device int set to 1 if a bounded wait inside the kernel timed out.
 // mirror_n > 0 (= 2(ncol-1), with ldr >= mirror_n) also writes the even
 // extension R[., mirror_n - j] = R[., j], 1 <= j <= ncol-2, for a DCT-I.
+// x_stride 2 reads X[r][j] at X + r*ldx + 2j (the real parts of an
+// interleaved complex array); halve_ends scales columns 0 and ncol-1 by 1/2.
 int rot_tc_f32(const float *A, const float *X, int64_t ldx, float *R, int64_t ldr, int64_t nrow,
-               int64_t ncol, void *bimg, int *err, cudaStream_t st, int64_t mirror_n = 0);
+               int64_t ncol, void *bimg, int *err, cudaStream_t st, int64_t mirror_n = 0,
+               int64_t x_stride = 1, int halve_ends = 0);
 }  // namespace mk

@@ -24,20 +24,22 @@
 // copies.  Every mbarrier wait is bounded: on timeout the CTA records an
 // error code, waits (bounded) for its outstanding MMAs, frees its tensor
 // memory and returns.
+#include "mk_async.cuh"
 #include "mk_common.cuh"
 #include "mk_rot.cuh"
 
 namespace {
 
+using mk::bulk_g2s;
+using mk::mbar_expect_tx;
+using mk::mbar_init;
+using mk::mbar_wait;
+using mk::smem_u32;
+
 constexpr int TILE_M = 128;      // samples per tile (MMA M)
 constexpr int KC = 32;           // K per chunk: one 128-byte swizzle row of tf32
 constexpr int NSTAGE = 2;
 constexpr int NTHREADS = 128;
-constexpr uint32_t SPIN_LIMIT = 1u << 24;
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-  return (uint32_t)__cvta_generic_to_shared(p);
-}
 
 __device__ __forceinline__ float tf32_round(float x) {
   uint32_t r;
@@ -49,41 +51,6 @@ __device__ __forceinline__ float tf32_round(float x) {
 // rows hold 32 fp32 (one swizzle row each); 8-row groups are 1024 B apart.
 __host__ __device__ __forceinline__ uint32_t sw128_off(uint32_t row, uint32_t k) {
   return (row >> 3) * 1024u + (row & 7u) * 128u + ((((k >> 2) ^ (row & 7u)) & 7u) << 4) + (k & 3u) * 4u;
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      " selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-
-// bounded wait; false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  for (uint32_t i = 0; i < SPIN_LIMIT; i++)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(dst)),
-      "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
 }
 
 // shared-memory matrix descriptor: K-major, SWIZZLE_128B, 8-row groups 1024 B apart
@@ -166,7 +133,7 @@ __device__ __forceinline__ void cp_async_wait() {
 
 // queue the copy of chunk q (tile, c) of this CTA into raw slot q % RSTAGE;
 // always commits one group so that group counting stays uniform
-__device__ __forceinline__ void prefetch_chunk(const float *__restrict__ X, int64_t ldx, int64_t ncol,
+__device__ __forceinline__ void prefetch_chunk(const float *__restrict__ X, int64_t ldx, int64_t xs, int64_t ncol,
                                                int nchunk, int64_t ntile, uint32_t q, float *raw,
                                                int tid) {
   const int64_t tile = blockIdx.x + (int64_t)(q / nchunk) * gridDim.x;
@@ -174,7 +141,7 @@ __device__ __forceinline__ void prefetch_chunk(const float *__restrict__ X, int6
   if (tile < ntile) {
     const int64_t my = tile * TILE_M + tid;
     const bool ok = my < ncol;
-    const float *src = X + (int64_t)(c * KC) * ldx + (ok ? my : 0);
+    const float *src = X + (int64_t)(c * KC) * ldx + (ok ? my : 0) * xs;
     float *dst = raw + (size_t)(q % RSTAGE) * KC * TILE_M + tid;
 #pragma unroll
     for (int kk = 0; kk < KC; kk++) cp_async4(dst + kk * TILE_M, src + (int64_t)kk * ldx, ok);
@@ -184,7 +151,8 @@ __device__ __forceinline__ void prefetch_chunk(const float *__restrict__ X, int6
 
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_rot_tc(const float *__restrict__ X, int64_t ldx, float *__restrict__ R, int64_t ldr, int ndet,
-             int64_t ncol, const char *__restrict__ bimg, int *__restrict__ err, int64_t mirror_n) {
+             int64_t ncol, const char *__restrict__ bimg, int *__restrict__ err, int64_t mirror_n,
+             int64_t xs, int halve_ends) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const uint32_t a_bytes = TILE_M * 128;          // 16 KB
@@ -195,7 +163,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   __shared__ uint32_t tmem_base_sh;
   __shared__ int abort_sh;
 
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tid = threadIdx.x, warp = tid >> 5;
   const int nchunk = ndet / KC;
   const uint32_t ncols = ndet < 32 ? 32u : (uint32_t)ndet;  // power of two by construction
   const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(ndet >> 3) << 17) |
@@ -223,11 +191,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   // Control flow is CTA-uniform: only thread 0 waits on mbarriers; the
   // outcome reaches the other threads through abort_sh and __syncthreads.
   const int64_t ntile = (ncol + TILE_M - 1) / TILE_M;
-  for (uint32_t q = 0; q < (uint32_t)RSTAGE; q++) prefetch_chunk(X, ldx, ncol, nchunk, ntile, q, raw, tid);
+  for (uint32_t q = 0; q < (uint32_t)RSTAGE; q++) prefetch_chunk(X, ldx, xs, ncol, nchunk, ntile, q, raw, tid);
   uint32_t g = 0;  // chunks issued by this CTA so far
   for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x) {
     const int64_t n0 = tile * TILE_M;
     const int64_t my = n0 + tid;
+    // DCT-I endpoint halving folded into the load (noise.py:710-711)
+    const float hscale = (halve_ends && (my == 0 || my == ncol - 1)) ? 0.5f : 1.0f;
     for (int c = 0; c < nchunk; c++, g++) {
       const uint32_t s = g % NSTAGE, use = g / NSTAGE;
       unsigned char *st = smem + s * stage_bytes;
@@ -238,11 +208,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const float *rw = raw + (size_t)(g % RSTAGE) * KC * TILE_M + tid;
 #pragma unroll
       for (int kk = 0; kk < KC; kk++) {
-        float x = rw[kk * TILE_M];
+        float x = rw[kk * TILE_M] * hscale;
         h[kk] = tf32_round(x);
         l[kk] = tf32_round(x - h[kk]);
       }
-      prefetch_chunk(X, ldx, ncol, nchunk, ntile, g + RSTAGE, raw, tid);
+      prefetch_chunk(X, ldx, xs, ncol, nchunk, ntile, g + RSTAGE, raw, tid);
       if (tid == 0) {
         // stage s is free once the MMAs of chunk g-2 have completed
         if (g >= NSTAGE && !mbar_wait(&bar_mma[s], (use - 1) & 1)) {
@@ -331,12 +301,14 @@ bool rot_tc_supported(int64_t nrow) {
 size_t rot_tc_bimg_bytes(int64_t nrow) { return (size_t)nrow * (size_t)nrow * 8; }
 
 int rot_tc_f32(const float *A, const float *X, int64_t ldx, float *R, int64_t ldr, int64_t nrow,
-               int64_t ncol, void *bimg, int *err, cudaStream_t st, int64_t mirror_n) {
+               int64_t ncol, void *bimg, int *err, cudaStream_t st, int64_t mirror_n, int64_t x_stride,
+               int halve_ends) {
   MK_CHECK_ARG(rot_tc_supported(nrow), "tensor-core rotation supports ndet in {32,64,128,256}, got %lld",
                (long long)nrow);
   MK_CHECK_ARG(bimg && err && ((uintptr_t)bimg % 16) == 0, "tensor-core rotation: bad scratch");
   MK_CHECK_ARG(mirror_n == 0 || (mirror_n == 2 * (ncol - 1) && ldr >= mirror_n),
                "tensor-core rotation: bad mirror extent");
+  MK_CHECK_ARG(x_stride == 1 || x_stride == 2, "tensor-core rotation: element stride must be 1 or 2");
   if (ncol <= 0) return MK_OK;
   const int nd = (int)nrow;
   k_bprep<<<(nd * nd + 255) / 256, 256, 0, st>>>(A, nd, (char *)bimg);
@@ -356,7 +328,7 @@ int rot_tc_f32(const float *A, const float *X, int64_t ldx, float *R, int64_t ld
   int64_t grid = (int64_t)sm_count() * per_sm;
   if (grid > ntile) grid = ntile;
   k_rot_tc<<<(unsigned)grid, NTHREADS, smem, st>>>(X, ldx, R, ldr, nd, ncol, (const char *)bimg, err,
-                                                   mirror_n);
+                                                   mirror_n, x_stride, halve_ends);
   return launch_status("rot_tc_f32");
 }
 

@@ -84,6 +84,10 @@ class MapmakingOperator:
         shapes = sorted(set(self.dims))
         ws_bytes = max(K.noise_workspace_bytes(nd, n, self.dtype) for nd, n in shapes)
         self.ws = torch.empty(ws_bytes, dtype=torch.uint8, device=self.device)
+        # cuFFT allocates its plan tables with cudaMalloc, outside torch's
+        # caching allocator: hand back cached blocks first so a near-full
+        # device can still build one plan per distinct TOD shape.
+        torch.cuda.empty_cache()
         self.plans = {s: K.NoisePlan(s[0], s[1], self.dtype, self.device, workspace=self.ws)
                       for s in shapes}
         if self.rot_mode == 0:
@@ -110,6 +114,8 @@ class MapmakingOperator:
         m = method or self.method
         if m == "atomic":
             K.tod2map(out, self.tmp, self.ipix)
+        elif m == "staged":
+            K.tod2map_staged(out, self.tmp, self.ipix)
         elif m == "fixed":
             if self._fixed is None:
                 self._fixed = K.FixedScratch(self.npix, self.device)

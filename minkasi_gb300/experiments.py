@@ -178,7 +178,7 @@ def run_large(config: str = "c4", tol: float = 1e-6, max_iter: int = 3000, wall_
     (bounded by ``wall_limit_s``)."""
     from . import kernels as K
     from .maps import SkyMap
-    from .noise import NoiseSmoothedSVD
+    from .noise import NoiseSmoothedSVD, clear_plan_cache
     from .pcg import DevicePCG, MixedOp
     from .synth import make_tod_info, tod_shapes
     from .tods import Tod, TodVec
@@ -201,6 +201,8 @@ def run_large(config: str = "c4", tol: float = 1e-6, max_iter: int = 3000, wall_
         del tod, info
         if (k + 1) % 25 == 0:
             log(f"  {k + 1}/{cfg.ntod} TODs, {torch.cuda.memory_allocated() / 1e9:.1f} GB allocated")
+    clear_plan_cache()
+    torch.cuda.empty_cache()
     hits = make_hits(tv, m).map.reshape(-1)
     pre = torch.where(hits > 0, 1.0 / hits.clamp(min=1), torch.zeros_like(hits))
     op64 = tv.engine(m, torch.float64)

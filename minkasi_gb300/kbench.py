@@ -61,6 +61,8 @@ def run(config: str = "c2s", only=None) -> dict:
             acc = torch.zeros(npix, dtype=dt, device=dev)
             ms = best_ms(lambda: K.tod2map(acc, dat, ipix))
             out[f"tod2map_atomic_{tag}"] = {"ms": ms, "GBs": N * (4 + es) / ms / 1e6}
+            ms = best_ms(lambda: K.tod2map_staged(acc, dat, ipix))
+            out[f"tod2map_staged_{tag}"] = {"ms": ms, "GBs": N * (4 + es) / ms / 1e6}
             hits = torch.zeros(npix, dtype=torch.float64, device=dev)
             K.tod2map_rows(hits, ipix)
             hmax = int(hits.max().item())

@@ -92,6 +92,140 @@ def tod2map(map: torch.Tensor, dat: torch.Tensor, ipix: torch.Tensor) -> None:
                            _stream()), "tod2map")
 
 
+def tod2map_staged(map: torch.Tensor, dat: torch.Tensor, ipix: torch.Tensor) -> None:
+    """map.flat[ipix] += dat, streams staged through shared memory by bulk
+    copies (mk_tod2map_staged).  Device tensors, 16-byte aligned."""
+    _dev(dat, "dat"), _dev(map, "map"), _ipix(ipix, dat.shape)
+    if map.dtype != dat.dtype:
+        raise TypeError("map and dat must have the same dtype")
+    ndet, ndata = _nd(dat)
+    check(lib().mk_tod2map_staged(_p(map), _p(dat), _p(ipix), ndet, ndata, map.numel(),
+                                  dtype_code(dat), _stream()), "tod2map_staged")
+
+
+def tod2map_status() -> int:
+    """1 if a staged tod2map kernel stopped on a timed-out wait since the last call."""
+    code = ctypes.c_int(0)
+    check(lib().mk_tod2map_status(ctypes.byref(code), _stream()), "tod2map_status")
+    return int(code.value)
+
+
+def _radec(ra: torch.Tensor, dec: torch.Tensor, out: Optional[torch.Tensor]) -> torch.Tensor:
+    _dev(ra, "ra"), _dev(dec, "dec")
+    if ra.dtype != torch.float64 or dec.dtype != torch.float64:
+        raise TypeError("ra and dec must be float64 (radians)")
+    if ra.shape != dec.shape:
+        raise ValueError("ra and dec must have the same shape")
+    if out is None:
+        out = torch.empty(ra.shape, dtype=torch.int32, device=ra.device)
+    else:
+        _dev(out, "out")
+        if out.dtype != torch.int32 or out.shape != ra.shape:
+            raise ValueError("out must be int32 with the shape of ra")
+    return out
+
+
+def pix_car(ra: torch.Tensor, dec: torch.Tensor, ra0: float, dec0: float, pixsize: float,
+            cosdec: float, ny: int, trunc: bool = False,
+            out: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """int32 pixel indices from RA/dec (radians): SkyMapCar.pix_from_radec
+    (trunc=False) or radec2pix_car (trunc=True), bit-identical (mk_pix_car)."""
+    out = _radec(ra, dec, out)
+    check(lib().mk_pix_car(_p(out), _p(ra), _p(dec), ra.numel(), float(ra0), float(dec0),
+                           float(pixsize), float(cosdec), int(ny), int(bool(trunc)), _stream()),
+          "pix_car")
+    return out
+
+
+def pix_wcs_car(ra: torch.Tensor, dec: torch.Tensor, wcs6, ny: int,
+                out: Optional[torch.Tensor] = None) -> torch.Tensor:
+    """int32 pixel indices through a CAR WCS given as (crval1, crval2, crpix1,
+    crpix2, cdelt1, cdelt2) in degrees (mk_pix_wcs_car)."""
+    out = _radec(ra, dec, out)
+    w = (ctypes.c_double * 6)(*[float(v) for v in wcs6])
+    check(lib().mk_pix_wcs_car(_p(out), _p(ra), _p(dec), ra.numel(), ctypes.cast(w, ctypes.c_void_p),
+                               int(ny), _stream()), "pix_wcs_car")
+    return out
+
+
+POL_MODES = {"QU": 1, "IQU": 2, "QU_PRECON": 3, "IQU_PRECON": 4}
+
+
+def pol_sincos(twogamma: torch.Tensor, dtype: torch.dtype = torch.float64):
+    """(cos(twogamma), sin(twogamma)) in ``dtype`` (mk_pol_sincos)."""
+    _dev(twogamma, "twogamma")
+    if twogamma.dtype != torch.float64:
+        raise TypeError("twogamma must be float64")
+    c = torch.empty(twogamma.shape, dtype=dtype, device=twogamma.device)
+    s = torch.empty_like(c)
+    check(lib().mk_pol_sincos(_p(c), _p(s), _p(twogamma), twogamma.numel(), _DT[dtype], _stream()),
+          "pol_sincos")
+    return c, s
+
+
+def _pol_args(map: torch.Tensor, ipix: torch.Tensor, angle, n: int):
+    _dev(map, "map"), _dev(ipix, "ipix")
+    if ipix.dtype != torch.int32 or ipix.numel() != n:
+        raise ValueError("ipix must be int32 with one entry per sample")
+    if isinstance(angle, tuple):
+        c, s = angle
+        _dev(c, "cos2g"), _dev(s, "sin2g")
+        if c.dtype != map.dtype or s.dtype != map.dtype or c.numel() != n or s.numel() != n:
+            raise ValueError("cos2g / sin2g must match the map dtype and the sample count")
+        return _p(c), _p(s), None
+    _dev(angle, "twogamma")
+    if angle.dtype != torch.float64 or angle.numel() != n:
+        raise ValueError("twogamma must be float64 with one entry per sample")
+    return None, None, _p(angle)
+
+
+def polmap2tod(dat: torch.Tensor, map: torch.Tensor, mode: str, angle, ipix: torch.Tensor,
+               do_add: bool = False) -> None:
+    """dat (+)= the QU / IQU projection of a (nx, ny, npol) map (mk_polmap2tod).
+    ``angle``: a (cos2g, sin2g) pair of the map's dtype, or float64 twogamma."""
+    _dev(dat, "dat")
+    if dat.dtype != map.dtype:
+        raise TypeError("map and dat must have the same dtype")
+    ndet, ndata = _nd(dat)
+    c, s, tg = _pol_args(map, ipix, angle, dat.numel())
+    npol = lib().mk_pol_npol(POL_MODES[mode])
+    check(lib().mk_polmap2tod(_p(dat), _p(map), c, s, tg, _p(ipix), ndet, ndata, map.numel() // npol,
+                              POL_MODES[mode], dtype_code(map), int(bool(do_add)), _stream()), "polmap2tod")
+
+
+def tod2polmap(map: torch.Tensor, dat: Optional[torch.Tensor], mode: str, angle, ipix: torch.Tensor,
+               rowval: Optional[torch.Tensor] = None, shape=None) -> None:
+    """map += the mode's Stokes weights of dat (mk_tod2polmap).  dat None:
+    per-detector ``rowval`` (or 1) for each sample of ``shape`` (hit maps)."""
+    if dat is not None:
+        _dev(dat, "dat")
+        if dat.dtype != map.dtype:
+            raise TypeError("map and dat must have the same dtype")
+        ndet, ndata = _nd(dat)
+    else:
+        ndet, ndata = int(shape[0]), int(shape[1])
+        if rowval is not None:
+            _dev(rowval, "rowval")
+            if rowval.dtype != map.dtype or rowval.numel() != ndet:
+                raise ValueError("rowval must have one entry per detector and the map's dtype")
+    c, s, tg = _pol_args(map, ipix, angle, ndet * ndata)
+    npol = lib().mk_pol_npol(POL_MODES[mode])
+    check(lib().mk_tod2polmap(_p(map), _p(dat), c, s, tg, _p(ipix), ndet, ndata, map.numel() // npol,
+                              POL_MODES[mode], dtype_code(map), _p(rowval), _stream()), "tod2polmap")
+
+
+def pol_precon_mul(out: torch.Tensor, precon: torch.Tensor, map: torch.Tensor, mode: str) -> None:
+    """out = P . map per pixel (mk_pol_precon_mul); mode QU_PRECON or IQU_PRECON."""
+    for t, nm in ((out, "out"), (precon, "precon"), (map, "map")):
+        _dev(t, nm)
+        if t.dtype != map.dtype:
+            raise TypeError("out, precon and map must share a dtype")
+    npol = lib().mk_pol_npol(POL_MODES[mode])
+    npix = precon.numel() // npol
+    check(lib().mk_pol_precon_mul(_p(out), _p(precon), _p(map), npix, POL_MODES[mode], dtype_code(map),
+                                  _stream()), "pol_precon_mul")
+
+
 def tod2map_rows(map: torch.Tensor, ipix: torch.Tensor, w: Optional[torch.Tensor] = None) -> None:
     """map.flat[ipix[d, t]] += w[d] (1 when w is None) -- hit / weight maps."""
     _dev(map, "map"), _dev(ipix, "ipix")

@@ -43,11 +43,12 @@ def as_device(a, dtype=None, device=None) -> torch.Tensor:
 class SkyMap:
     """A CAR sky map held on the GPU (minkasi/maps/skymap.py:38-790).
 
-    Parameters follow the reference.  Without astropy, the pixelization is
-    the reference's CAR layout restated with a flat-sky formula
-    (x = (lims[1] - ra) * cos(dec0) / pixsize, y = (dec - lims[2]) / pixsize,
-    ipix = x * ny + y); pixel indices supplied by the caller in
-    ``tod.info[tag]`` always take precedence, exactly as in the reference
+    Parameters follow the reference.  The WCS is the CAR WCS of get_wcs
+    (minkasi/maps/utils.py:13-67), kept as (crval1, crval2, crpix1, crpix2,
+    cdelt1, cdelt2) in degrees (``self.wcs``; ``mywcs`` may pass such a
+    6-sequence).  Pointing -> pixel runs on the GPU (mk_pix_wcs_car), the map
+    size follows get_npix (skymap.py:206-234), and pixel indices supplied by
+    the caller in ``tod.info[tag]`` take precedence, as in the reference
     (SkyMap.get_pix, skymap.py:492-540).
     """
 
@@ -59,25 +60,30 @@ class SkyMap:
         if proj != "CAR":
             raise ValueError(f"Unknown projection type, {proj}")
         self.lims = None if lims is None else list(lims)
-        self.pixsize = float(pixsize)
         self.proj = proj
         self.pad = pad
         self.primes = primes
-        if self.lims is not None and cosdec is None:
-            cosdec = math.cos(0.5 * (self.lims[2] + self.lims[3]))
+        self.ref_equ = ref_equ
+        self.wcs = None
+        if mywcs is not None:
+            self.wcs = [float(v) for v in mywcs]
+            if len(self.wcs) != 6:
+                raise ValueError("mywcs: (crval1, crval2, crpix1, crpix2, cdelt1, cdelt2) in degrees")
+            pixsize = self.wcs[5] * np.pi / 180
+        elif self.lims is not None and pixsize != 0:
+            self.wcs = car_wcs(self.lims, pixsize, ref_equ)
+        self.pixsize = float(pixsize)
         self.cosdec = cosdec
         if nx is None or ny is None:
-            if self.lims is None or self.pixsize <= 0:
+            if self.lims is None or self.wcs is None:
                 raise ValueError("SkyMap needs (lims, pixsize) or explicit nx, ny")
-            cnx = int(round((self.lims[1] - self.lims[0]) * self.cosdec / self.pixsize)) + 1 + pad
-            cny = int(round((self.lims[3] - self.lims[2]) / self.pixsize)) + 1 + pad
-            nx = cnx if nx is None else nx
-            ny = cny if ny is None else ny
+            gx, gy = self.get_npix(pad)
+            nx = gx if nx is None else nx
+            ny = gy if ny is None else ny
         self.nx, self.ny = int(nx), int(ny)
         self.tag = tag
         self.purge_pixellization = purge_pixellization
         self.caches = None
-        self.wcs = mywcs
         self.map = torch.zeros((self.nx, self.ny), dtype=dtype, device=device or default_device())
 
     # ---- construction helpers ------------------------------------------
@@ -101,14 +107,24 @@ class SkyMap:
         self.caches = None
 
     # ---- pointing -------------------------------------------------------
+    def get_npix(self, pad: int):
+        """nx, ny from the pixel coordinates of the lims corners
+        (skymap.py:206-234)."""
+        xs, ys = [], []
+        for ra, dec in ((0, 2), (0, 3), (1, 2), (1, 3)):
+            p1, p2 = car_world2pix(self.lims[ra] * 180 / np.pi, self.lims[dec] * 180 / np.pi, self.wcs)
+            xs.append(round_half_even(p1))
+            ys.append(round_half_even(p2))
+        return int(max(xs) + pad), int(max(ys) + pad)
+
     def pix_from_radec(self, ra, dec) -> torch.Tensor:
-        """int32 pixel indices from RA/dec in radians (flat CAR restatement of
-        SkyMap.pix_from_radec, skymap.py:457-490)."""
+        """int32 pixel indices from RA/dec in radians through the map's CAR
+        WCS (SkyMap.pix_from_radec, skymap.py:457-490), on the GPU."""
+        if self.wcs is None:
+            raise ValueError("this SkyMap has no WCS (built from nx, ny only)")
         ra = as_device(ra, torch.float64)
         dec = as_device(dec, torch.float64)
-        x = torch.round((self.lims[1] - ra) * self.cosdec / self.pixsize)
-        y = torch.round((dec - self.lims[2]) / self.pixsize)
-        return (x * self.ny + y).to(torch.int32).contiguous()
+        return K.pix_wcs_car(ra, dec, self.wcs, self.ny)
 
     def get_pix(self, tod, savepix: bool = True) -> torch.Tensor:
         """Cached pixellization of ``tod`` (skymap.py:492-540)."""
@@ -145,14 +161,15 @@ class SkyMap:
         ipix = self.get_pix(tod)
         if isinstance(dat, torch.Tensor) and dat.device.type == "cpu" and dat.is_pinned() \
                 and dat.dtype == self.map.dtype and dat.is_contiguous():
-            d = dat  # pinned host timestream: the scatter kernel reads it in place
+            # pinned host timestream: chunked copies overlapped with the scatter
+            _stager(self.map.device).tod2map(self.map, dat, ipix)
         else:
             d = dat if isinstance(dat, torch.Tensor) else as_device(dat, self.map.dtype)
             if not d.is_cuda:
                 d = d.to(self.map.device)
             if d.dtype != self.map.dtype:
                 d = d.to(self.map.dtype)
-        K.tod2map(self.map, d, ipix)
+            K.tod2map(self.map, d, ipix)
         if self.purge_pixellization:
             tod.clear_saved_pix(self.tag)
 
@@ -205,6 +222,68 @@ class SkyMap:
         return self.map.detach().cpu().numpy()
 
 
+class HostStager:
+    """Host -> device staging of timestreams in pinned host memory.
+
+    A timestream is cut into chunks of CHUNK samples.  Each chunk is copied on
+    a dedicated copy stream into one of two device buffers, and the scatter of
+    the chunk runs on the caller's stream as soon as its copy lands, while the
+    next chunk is already copying.  Consecutive calls (one per TOD) continue
+    the same two-buffer ring, so the copy engine stays busy across TODs and a
+    pass over host-resident TODs runs at the host -> device copy rate.
+    Ordering is by CUDA events only; the host never waits, so, as with any
+    non-blocking copy, the caller must not overwrite the host buffer before
+    the stream work of the call has run.
+    """
+
+    CHUNK = 1 << 24  # samples (128 MB of FP64 per buffer)
+
+    def __init__(self, device):
+        self.device = torch.device(device)
+        self.copy_stream = torch.cuda.Stream(self.device)
+        self.bufs = {}
+        self.free = [None, None]  # event: the scatter that last read buffer i is done
+        self.turn = 0
+
+    def _buffers(self, dtype):
+        if dtype not in self.bufs:
+            self.bufs[dtype] = [torch.empty(self.CHUNK, dtype=dtype, device=self.device) for _ in range(2)]
+            self.free = [None, None]
+        return self.bufs[dtype]
+
+    def tod2map(self, map: torch.Tensor, host: torch.Tensor, ipix: torch.Tensor) -> None:
+        bufs = self._buffers(host.dtype)
+        comp = torch.cuda.current_stream(self.device)
+        h = host.reshape(-1)
+        ip = ipix.reshape(-1)
+        n = h.numel()
+        for start in range(0, n, self.CHUNK):
+            m = min(self.CHUNK, n - start)
+            b = self.turn
+            self.turn ^= 1
+            if self.free[b] is not None:
+                self.copy_stream.wait_event(self.free[b])
+            with torch.cuda.stream(self.copy_stream):
+                bufs[b][:m].copy_(h[start:start + m], non_blocking=True)
+                landed = torch.cuda.Event()
+                landed.record(self.copy_stream)
+            comp.wait_event(landed)
+            K.tod2map(map, bufs[b][:m].view(1, m), ip[start:start + m].view(1, m))
+            done = torch.cuda.Event()
+            done.record(comp)
+            self.free[b] = done
+
+
+_STAGERS = {}
+
+
+def _stager(device) -> HostStager:
+    key = str(device)
+    if key not in _STAGERS:
+        _STAGERS[key] = HostStager(device)
+    return _STAGERS[key]
+
+
 _REDUCERS = {}
 
 
@@ -213,6 +292,71 @@ def _reducer(device) -> K.Reducer:
     if key not in _REDUCERS:
         _REDUCERS[key] = K.Reducer(device)
     return _REDUCERS[key]
+
+
+class SkyMapCar(SkyMap):
+    """SkyMap with the flat CAR pixelization of SkyMapCar.pix_from_radec
+    (minkasi/maps/skymap.py:952-984), computed on the GPU bit-identically."""
+
+    def pix_from_radec(self, ra, dec) -> torch.Tensor:
+        if self.cosdec is None:
+            self.cosdec = np.cos(0.5 * (self.lims[2] + self.lims[3]))
+        ra = as_device(ra, torch.float64)
+        dec = as_device(dec, torch.float64)
+        return K.pix_car(ra, dec, self.lims[0], self.lims[2], self.pixsize, float(self.cosdec),
+                         self.ny, trunc=False)
+
+
+def radec2pix_car(ra, dec, ipix: torch.Tensor, lims, pixsize: float, cosdec: float, ny: int) -> None:
+    """Fill ``ipix`` (int32 CUDA tensor, same size as ra) in place, as
+    radec2pix_car (minkasi/maps/utils.py:178-216)."""
+    ra = as_device(ra, torch.float64).reshape(-1)
+    dec = as_device(dec, torch.float64).reshape(-1)
+    if not (isinstance(ipix, torch.Tensor) and ipix.is_cuda and ipix.is_contiguous()):
+        raise ValueError("ipix must be a contiguous int32 CUDA tensor")
+    K.pix_car(ra, dec, lims[0], lims[2], pixsize, cosdec, ny, trunc=True, out=ipix.view(-1))
+
+
+def car_wcs(lims, pixsize: float, ref_equ: bool = False) -> List[float]:
+    """(crval1, crval2, crpix1, crpix2, cdelt1, cdelt2), degrees, of the CAR
+    WCS that get_wcs builds (minkasi/maps/utils.py:47-66; CAR uses cosdec = 1)."""
+    cosdec = 1.0
+    if ref_equ:
+        crval = [0.0, 0.0]
+        crpix = [lims[1] / pixsize + 1, -lims[2] / pixsize + 1]
+    else:
+        crpix = [1.0, 1.0]
+        crval = [lims[1] * 180 / np.pi, lims[2] * 180 / np.pi]
+    cdelt = [-pixsize / cosdec * 180 / np.pi, pixsize * 180 / np.pi]
+    return [float(v) for v in crval + crpix + cdelt]
+
+
+def car_world2pix(ra_deg: float, dec_deg: float, w) -> tuple:
+    """1-based pixel coordinates of one point through a CAR WCS (the map-size
+    corners; the per-sample version is the mk_pix_wcs_car kernel): rotation
+    to native spherical coordinates about the pole given by crval and the
+    default LONPOLE/LATPOLE (Calabretta & Greisen 2002, eqs. 5, 8-10), CAR
+    x = phi, y = theta, p = crpix + x / cdelt."""
+    ra0, dec0 = w[0], w[1]
+    if dec0 >= 0:
+        phi_p, delta_p, alpha_p = 0.0, 90.0 - dec0, ra0 - 180.0
+    else:
+        phi_p, delta_p, alpha_p = 180.0, 90.0 + dec0, ra0
+    d2r = math.pi / 180
+    sdp, cdp = math.sin(delta_p * d2r), math.cos(delta_p * d2r)
+    sd, cd = math.sin(dec_deg * d2r), math.cos(dec_deg * d2r)
+    sl, cl = math.sin((ra_deg - alpha_p) * d2r), math.cos((ra_deg - alpha_p) * d2r)
+    phi = phi_p + math.atan2(-cd * sl, sd * cdp - cd * sdp * cl) / d2r
+    if phi > 180:
+        phi -= 360
+    elif phi < -180:
+        phi += 360
+    theta = math.asin(max(-1.0, min(1.0, sd * sdp + cd * cdp * cl))) / d2r
+    return w[2] + phi / w[4], w[3] + theta / w[5]
+
+
+def round_half_even(x: float) -> float:
+    return float(np.round(x))
 
 
 class Mapset:

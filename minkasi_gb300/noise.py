@@ -41,6 +41,11 @@ def noise_plan(ndet: int, ndata: int, dtype: torch.dtype, device) -> K.NoisePlan
     return _PLAN_CACHE[key]
 
 
+def clear_plan_cache() -> None:
+    """Drop the one-off plans and their FFT workspaces."""
+    _PLAN_CACHE.clear()
+
+
 def dct1(x: torch.Tensor) -> torch.Tensor:
     """Unnormalised DCT-I along the last axis (fft_r2r, tools/fft.py:290-344)."""
     x2 = x.reshape(1, -1) if x.dim() == 1 else x

@@ -67,6 +67,9 @@ def make_hits(todvec, map: SkyMap, do_weights: bool = False) -> SkyMap:
     """Hit (or detector-weight) map summed over TODs and ranks
     (tod2map.py:343-400), without materialising a TOD of ones."""
     hits = map.copy()
+    pol = getattr(map, "npol", 1) > 1
+    if pol:
+        hits.set_polstate(map.poltag + "_PRECON")  # PolMap: the per-pixel Stokes matrices
     hits.clear()
     flat = hits.map.reshape(-1)
     for tod in todvec.tods:
@@ -82,7 +85,9 @@ def make_hits(todvec, map: SkyMap, do_weights: bool = False) -> SkyMap:
         if "mask" in tod.info:
             msk = as_device(tod.info["mask"], flat.dtype)
             tmp = msk if w is None else msk * w[:, None]
-            K.tod2map(flat, tmp.contiguous(), ip)
+            hits.tod2map(tod, tmp.contiguous())
+        elif pol:
+            hits.tod2map_rows(tod, w)
         else:
             K.tod2map_rows(flat, ip, w)
     hits.mpi_reduce()

@@ -102,6 +102,17 @@ class Tod:
             self._dev_pix[tag] = t
         return t
 
+    def device_sincos(self, dtype: torch.dtype = torch.float64):
+        """(cos, sin) of info['twogamma_saved'] on the device in ``dtype``,
+        computed once (mk_pol_sincos) and cached with the pixellization."""
+        key = ("sincos", dtype)
+        t = self._dev_pix.get(key)
+        if t is None:
+            tg = as_device(self.info["twogamma_saved"], torch.float64)
+            t = K.pol_sincos(tg.reshape(self.get_data_dims()).contiguous(), dtype)
+            self._dev_pix[key] = t
+        return t
+
     def set_tag(self, tag: Any):
         if "tag" in self.info:
             print("Warning: overwriting tag")
@@ -253,7 +264,8 @@ class TodVec:
         return self._engines[key]
 
     def _fast(self, mapset: Mapset) -> bool:
-        return mapset.nmap == 1 and isinstance(mapset.maps[0], SkyMap) and self.ntod > 0 and \
+        return mapset.nmap == 1 and isinstance(mapset.maps[0], SkyMap) and \
+            getattr(mapset.maps[0], "npol", 1) == 1 and self.ntod > 0 and \
             all(t.noise is not None and isinstance(t.noise, NoiseSmoothedSVD) for t in self.tods)
 
     def dot(self, mapset: Mapset, mapset_out: Optional[Mapset] = None, report_times: bool = False,

@@ -25,6 +25,16 @@ reference file:line it follows (paths relative to the minkasi project root):
 * ``run_pcg``                -> minkasi/mapmaking/pcg.py:22-238
 * ``find_good_fft_lens`` / ``truncate_len`` -> minkasi/tools/py_fft.py:300-395,
   minkasi/tods/processing.py:648-682
+* ``pix_car`` / ``pix_car_trunc`` -> SkyMapCar.pix_from_radec,
+  minkasi/maps/skymap.py:958-984 / radec2pix_car, minkasi/maps/utils.py:178-216
+* ``polmap2tod`` / ``tod2polmap`` -> minkasi/lib/minkasi.c:146-245 (via
+  minkasi/mapmaking/map2tod.py:57-122, tod2map.py:164-215)
+* ``pol_invert`` / ``pol_precon_mul`` -> PolMap.invert / PolMap.__mul__,
+  minkasi/maps/polmap.py:300-384,624-684
+* ``car_wcs`` / ``pix_wcs_car``  -> get_wcs (minkasi/maps/utils.py:13-67) and
+  SkyMap.pix_from_radec (minkasi/maps/skymap.py:457-490); astropy's CAR
+  world->pixel is restated from the published FITS equations (Calabretta &
+  Greisen 2002).  astropy is not installed, so this one is parity unpinned.
 
 Parity of this oracle with the reference itself is pinned by
 ``tests/test_oracle_golden.py`` against fixtures that
@@ -329,3 +339,147 @@ def truncate_len(ndata: int, primes: Sequence[int] = (2, 3, 5, 7, 11)) -> int:
     """Length that truncate_tod (processing.py:648-682) cuts ndata down to."""
     new = int(find_good_fft_lens(ndata - 1, primes).max()) + 1
     return new if new < ndata else ndata
+
+
+# ---------------------------------------------------------------- pointing
+def pix_car(ra: np.ndarray, dec: np.ndarray, lims, pixsize: float, ny: int,
+            cosdec: Optional[float] = None) -> np.ndarray:
+    """SkyMapCar.pix_from_radec (minkasi/maps/skymap.py:958-984): x rounded
+    half-to-even, y + 0.5, the sum truncated to int32."""
+    if cosdec is None:
+        cosdec = np.cos(0.5 * (lims[2] + lims[3]))
+    xpix = np.round((ra - lims[0]) * cosdec / pixsize)
+    ypix = ((dec - lims[2]) / pixsize) + 0.5
+    return np.asarray(xpix * ny + ypix, dtype="int32")
+
+
+def pix_car_trunc(ra: np.ndarray, dec: np.ndarray, lims, pixsize: float, cosdec: float,
+                  ny: int) -> np.ndarray:
+    """radec2pix_car (minkasi/maps/utils.py:178-216): int(x + 0.5) and
+    int(y + 0.5) (truncation toward zero), then xpix * ny + ypix."""
+    xs = ((np.ravel(ra) - lims[0]) * cosdec / pixsize + 0.5)
+    ys = ((np.ravel(dec) - lims[2]) / pixsize + 0.5)
+    xp = np.trunc(xs).astype(np.int64)
+    yp = np.trunc(ys).astype(np.int64)
+    return (xp * ny + yp).astype(np.int32).reshape(np.shape(ra))
+
+
+def car_wcs(lims, pixsize: float, ref_equ: bool = False) -> np.ndarray:
+    """crval1, crval2, crpix1, crpix2, cdelt1, cdelt2 (degrees) of the CAR WCS
+    that get_wcs builds (minkasi/maps/utils.py:47-66; CAR forces cosdec = 1)."""
+    cosdec = 1.0
+    if ref_equ:
+        crval = [0.0, 0.0]
+        crpix = [lims[1] / pixsize + 1, -lims[2] / pixsize + 1]
+    else:
+        crpix = [1.0, 1.0]
+        crval = [lims[1] * 180 / np.pi, lims[2] * 180 / np.pi]
+    cdelt = [-pixsize / cosdec * 180 / np.pi, pixsize * 180 / np.pi]
+    return np.array(crval + crpix + cdelt, dtype=np.float64)
+
+
+def wcs_car_world2pix(ra_deg: np.ndarray, dec_deg: np.ndarray, w: np.ndarray):
+    """1-based pixel coordinates of a CAR WCS (Calabretta & Greisen 2002):
+    celestial pole from crval with the defaults LONPOLE = 0 (180 if crval2 <
+    0) and LATPOLE = +90 (eqs. 8-10, native reference point (0, 0)), the
+    rotation to native (phi, theta) (eq. 5), CAR x = phi, y = theta, then
+    p = crpix + x / cdelt."""
+    ra0, dec0 = w[0], w[1]
+    if dec0 >= 0:
+        phi_p, delta_p, alpha_p = 0.0, 90.0 - dec0, ra0 - 180.0
+    else:
+        phi_p, delta_p, alpha_p = 180.0, 90.0 + dec0, ra0
+    d2r = np.pi / 180
+    sdp, cdp = np.sin(delta_p * d2r), np.cos(delta_p * d2r)
+    sd, cd = np.sin(dec_deg * d2r), np.cos(dec_deg * d2r)
+    dl = (ra_deg - alpha_p) * d2r
+    sl, cl = np.sin(dl), np.cos(dl)
+    phi = phi_p + np.arctan2(-cd * sl, sd * cdp - cd * sdp * cl) / d2r
+    phi = np.where(phi > 180, phi - 360, np.where(phi < -180, phi + 360, phi))
+    theta = np.arcsin(np.clip(sd * sdp + cd * cdp * cl, -1, 1)) / d2r
+    return w[2] + phi / w[4], w[3] + theta / w[5]
+
+
+def pix_wcs_car(ra: np.ndarray, dec: np.ndarray, w: np.ndarray, ny: int) -> np.ndarray:
+    """SkyMap.pix_from_radec (minkasi/maps/skymap.py:457-490) on a CAR WCS."""
+    p1, p2 = wcs_car_world2pix(ra * 180 / np.pi, dec * 180 / np.pi, w)
+    xpix = np.round(p1 - 1)
+    ypix = np.round(p2 - 1)
+    return np.asarray(xpix * ny + ypix, dtype="int32")
+
+
+# ---------------------------------------------------------------- polarization
+def polmap2tod(dat: np.ndarray, map: np.ndarray, poltag: str, twogamma: np.ndarray,
+               ipix: np.ndarray, do_add: bool = False) -> None:
+    """map2tod_iqu_omp / map2tod_qu_omp (minkasi.c:146-174), in place."""
+    c, s = np.cos(twogamma), np.sin(twogamma)
+    m = map.reshape(-1, map.shape[-1])[ipix]
+    if poltag == "IQU":
+        v = m[..., 0] + m[..., 1] * c + m[..., 2] * s
+    elif poltag == "QU":
+        v = m[..., 0] * c + m[..., 1] * s
+    else:
+        raise ValueError(poltag)
+    if do_add:
+        dat += v
+    else:
+        dat[:] = v
+
+
+def tod2polmap(map: np.ndarray, dat: np.ndarray, poltag: str, twogamma: np.ndarray,
+               ipix: np.ndarray) -> None:
+    """tod2map_{qu,iqu}_simple, tod2map_{qu,iqu}_precon_simple
+    (minkasi.c:176-207,231-245), in place, serial order (np.add.at)."""
+    c, s = np.cos(twogamma).ravel(), np.sin(twogamma).ravel()
+    d = dat.ravel()
+    terms = {"IQU": [d, d * c, d * s], "QU": [d * c, d * s],
+             "QU_PRECON": [d * c * c, d * s * s, d * s * c],
+             "IQU_PRECON": [d, d * c, d * s, d * c * c, d * s * c, d * s * s]}[poltag]
+    flat = map.reshape(-1, len(terms))
+    p = ipix.ravel()
+    for k, t in enumerate(terms):
+        np.add.at(flat[:, k], p, t)
+
+
+def pol_invert(map: np.ndarray, poltag: str, thresh: float = 1e-6) -> np.ndarray:
+    """PolMap.invert for QU_PRECON / IQU_PRECON (polmap.py:300-384)."""
+    nx, ny = map.shape[:2]
+    n = nx * ny
+    out = map.copy()
+    if poltag == "QU_PRECON":
+        t = np.zeros((n, 2, 2))
+        t[:, 0, 0] = map[:, :, 0].ravel()
+        t[:, 1, 1] = map[:, :, 1].ravel()
+        t[:, 0, 1] = t[:, 1, 0] = map[:, :, 2].ravel()
+        t = np.linalg.pinv(t, thresh)
+        out[:, :, 0], out[:, :, 1], out[:, :, 2] = (t[:, 0, 0].reshape(nx, ny), t[:, 1, 1].reshape(nx, ny),
+                                                    t[:, 0, 1].reshape(nx, ny))
+        return out
+    idx = (((0, 0), 0), ((0, 1), 1), ((0, 2), 2), ((1, 1), 3), ((1, 2), 4), ((2, 2), 5))
+    t = np.zeros((n, 3, 3))
+    for (i, j), k in idx:
+        t[:, i, j] = t[:, j, i] = map[:, :, k].ravel()
+    dets = np.linalg.det(t)
+    isbad = dets < thresh * dets.max()
+    inds = isbad & (t[:, 0, 0] > 0)
+    vec = t[inds, 0, 0]
+    t = np.linalg.pinv(t, thresh)
+    t[isbad] = 0
+    t[inds, 0, 0] = 1.0 / vec
+    for (i, j), k in idx:
+        out[:, :, k] = t[:, i, j].reshape(nx, ny)
+    return out
+
+
+def pol_precon_mul(precon: np.ndarray, map: np.ndarray, poltag: str) -> np.ndarray:
+    """PolMap.__mul__ of a PRECON map and a Stokes map (polmap.py:624-684)."""
+    a, x = precon, map
+    out = np.empty_like(x)
+    if poltag == "QU_PRECON":
+        out[..., 0] = a[..., 0] * x[..., 0] + a[..., 2] * x[..., 1]
+        out[..., 1] = a[..., 2] * x[..., 0] + a[..., 1] * x[..., 1]
+    else:
+        out[..., 0] = a[..., 0] * x[..., 0] + a[..., 1] * x[..., 1] + a[..., 2] * x[..., 2]
+        out[..., 1] = a[..., 1] * x[..., 0] + a[..., 3] * x[..., 1] + a[..., 4] * x[..., 2]
+        out[..., 2] = a[..., 2] * x[..., 0] + a[..., 4] * x[..., 1] + a[..., 5] * x[..., 2]
+    return out

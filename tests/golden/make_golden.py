@@ -17,6 +17,12 @@ Reference entry points exercised (paths in the minkasi project):
   make_hits          minkasi/mapmaking/tod2map.py:343-400
   run_pcg            minkasi/mapmaking/pcg.py:22-238
   truncate_tod / find_good_fft_lens  minkasi/tods/processing.py:648-682, minkasi/tools/py_fft.py:364-395
+  SkyMapCar.pix_from_radec  minkasi/maps/skymap.py:958-984
+  radec2pix_car      minkasi/maps/utils.py:178-216 (its pure-Python path: numba is absent)
+  polmap2tod / tod2polmap / PolMap  minkasi/mapmaking/map2tod.py:57-122, tod2map.py:164-215,
+                     minkasi/maps/polmap.py:273-684 -> minkasi/lib/minkasi.c:146-245
+
+    python tests/golden/make_golden.py [case ...]   # default: every case
 """
 import contextlib
 import io
@@ -187,10 +193,101 @@ def case_lens():
     save("lens.npz", ndata=ndata, truncated=np.array(new), good1000=good)
 
 
+def case_pointing():
+    """Pixel indices of SkyMapCar.pix_from_radec and radec2pix_car for
+    pointings inside and around the map limits, north and south of the
+    equator (points off the map exercise truncation toward zero)."""
+    from minkasi.maps import utils as map_utils
+    from minkasi.maps.skymap import SkyMapCar
+    rng = np.random.default_rng(11)
+    arcsec = np.pi / 180 / 3600
+    out = {}
+    for k, (ra_c, dec_c) in enumerate(((3.5, 0.31), (0.7, -0.42))):
+        pixsize = 2.0 * arcsec
+        half = 600 * arcsec
+        lims = np.array([ra_c - half, ra_c + half, dec_c - half, dec_c + half])
+        cosdec = np.cos(0.5 * (lims[2] + lims[3]))
+        ny = int((lims[3] - lims[2]) / pixsize) + 3
+        ra = ra_c + rng.uniform(-1.1, 1.1, size=(6, 1500)) * half / cosdec
+        dec = dec_c + rng.uniform(-1.1, 1.1, size=(6, 1500)) * half
+        m = SkyMapCar.__new__(SkyMapCar)
+        m.lims, m.pixsize, m.ny, m.cosdec = lims, pixsize, ny, None
+        car = m.pix_from_radec(ra, dec)
+        trunc = np.zeros(ra.size, dtype=np.int32)
+        map_utils.radec2pix_car(ra, dec, trunc, lims, pixsize, cosdec, ny)
+        out.update({f"c{k}_ra": ra, f"c{k}_dec": dec, f"c{k}_lims": lims, f"c{k}_pixsize": pixsize,
+                    f"c{k}_ny": ny, f"c{k}_cosdec": m.cosdec, f"c{k}_car": car,
+                    f"c{k}_trunc": trunc.reshape(ra.shape)})
+    save("pointing.npz", ncase=2, **out)
+
+
+def bare_polmap(nx, ny, poltag):
+    """A PolMap without astropy: the attributes its projections, make_hits,
+    copy, set_polstate, invert and __mul__ read (polmap.py:197-684)."""
+    from minkasi.maps.polmap import PolMap
+    m = PolMap.__new__(PolMap)
+    m.nx, m.ny, m.tag, m.purge_pixellization, m.caches = nx, ny, "ipix", False, None
+    quiet(m.set_polstate, poltag)
+    return m
+
+
+def case_pol():
+    """PolMap projections through the reference's own C (polmap2tod /
+    tod2polmap -> minkasi.c:146-245), make_hits on IQU and QU maps, the
+    preconditioner inversion and the PRECON x map product."""
+    from minkasi.mapmaking.map2tod import polmap2tod
+    from minkasi.mapmaking.tod2map import make_hits, tod2polmap
+    rng = np.random.default_rng(23)
+    nx, ny, ndet, ndata = 20, 17, 6, 1000
+    walk = np.cumsum(rng.integers(-1, 2, size=(ndet, ndata)), axis=1) // 4
+    ipix = np.mod(walk + rng.integers(0, nx * ny, size=(ndet, 1)), nx * ny).astype(np.int32)
+    twogamma = rng.uniform(0, 2 * np.pi, size=(ndet, ndata))
+    dat = rng.standard_normal((ndet, ndata))
+    out = {"ipix": ipix, "twogamma": twogamma, "dat": dat, "nx": nx, "ny": ny}
+    for tag, npol in (("IQU", 3), ("QU", 2)):
+        mp = rng.standard_normal((nx, ny, npol))
+        out[f"map_{tag}"] = mp
+        for add in (0, 1):
+            d = dat.copy()
+            polmap2tod(d, mp, tag, twogamma, ipix, do_add=bool(add))
+            out[f"m2t_{tag}_{add}"] = d
+    for tag, npol in (("IQU", 3), ("QU", 2), ("QU_PRECON", 3), ("IQU_PRECON", 6)):
+        m0 = rng.standard_normal((nx, ny, npol))
+        out[f"t2m_in_{tag}"] = m0.copy()
+        tod2polmap(m0, dat, tag, twogamma, ipix)
+        out[f"t2m_{tag}"] = m0
+    tods = TodVec()
+    for k in range(2):
+        info = {"dat_calib": dat * (k + 1), "ipix": np.roll(ipix, 7 * k, axis=1).copy(),
+                "twogamma_saved": np.roll(twogamma, 3 * k, axis=1).copy()}
+        tods.add_tod(Tod(info))
+        out[f"hits_t{k}_ipix"] = info["ipix"]
+        out[f"hits_t{k}_twogamma"] = info["twogamma_saved"]
+    for tag in ("IQU", "QU"):
+        h = quiet(make_hits, tods, bare_polmap(nx, ny, tag))
+        out[f"hits_{tag}"] = h.map.copy()
+        inv = h.copy()
+        quiet(inv.invert)
+        out[f"inv_{tag}"] = inv.map.copy()
+        x = bare_polmap(nx, ny, tag)
+        x.map[:] = rng.standard_normal(x.map.shape)
+        out[f"mulx_{tag}"] = x.map.copy()
+        out[f"mul_{tag}"] = (inv * x).map.copy()
+    save("pol.npz", **out)
+
+
+CASES = {"proj": case_proj, "dct": case_dct, "noise": case_noise, "solve": case_solve}
+
 if __name__ == "__main__":
-    rng = np.random.default_rng(0)
-    case_proj(rng)
-    case_dct(rng)
-    case_noise(rng)
-    case_solve(rng)
-    case_lens()
+    want = sys.argv[1:]
+    if not want or any(w in CASES for w in want):
+        # these share one generator, so they are made together, in order
+        rng = np.random.default_rng(0)
+        for name, fn in CASES.items():
+            fn(rng)
+    if not want or "lens" in want:
+        case_lens()
+    if not want or "pointing" in want:
+        case_pointing()
+    if not want or "pol" in want:
+        case_pol()

@@ -102,6 +102,9 @@ def test_tod2map_large_runs_f64_f32(K):
     ms = torch.zeros(npix, dtype=torch.float64, device=cuda)
     plan.tod2map(ms, dev(dat))
     assert rel(ms.cpu().numpy(), ref) < 1e-12
+    mt = torch.zeros(npix, dtype=torch.float64, device=cuda)
+    K.tod2map_staged(mt, dev(dat), dev(ipix))
+    assert rel(mt.cpu().numpy(), ref) < 1e-12
 
 
 def test_tod2map_reads_pinned_host_timestream_in_place(K, gold):
@@ -112,6 +115,45 @@ def test_tod2map_reads_pinned_host_timestream_in_place(K, gold):
     assert rel(m.cpu().numpy(), g["tod2map_omp"]) < 1e-13
     with pytest.raises(ValueError):
         K.tod2map(dev(g["map"]), torch.from_numpy(np.ascontiguousarray(g["dat"])), dev(g["ipix"]))
+
+
+def test_tod2map_staged_golden(K, gold):
+    g = gold("proj.npz")
+    m = dev(g["map"])
+    K.tod2map_staged(m, dev(g["dat"]), dev(g["ipix"]))
+    assert rel(m.cpu().numpy(), g["tod2map_omp"]) < 1e-13
+    assert K.tod2map_status() == 0
+
+
+@pytest.mark.parametrize("n", [1, 3, 4, 5, 2047, 2048, 2049, 2052, 3 * 2048 * 152 + 6, 6_000_001])
+def test_tod2map_staged_ragged_sizes_and_bad_pixels(K, n):
+    """Chunk edges, the <4-sample tail, more chunks than CTAs (6e6 samples:
+    every CTA wraps its stage ring several times), and pixels
+    outside [0, npix) (skipped), FP64 and FP32, against numpy."""
+    rng = np.random.default_rng(n)
+    npix = 300
+    walk = np.cumsum(rng.integers(-1, 2, size=n)) // 3
+    ipix = (np.mod(walk, npix + 6) - 3).astype(np.int32)  # includes -3..-1 and npix..npix+2
+    dat = rng.standard_normal(n)
+    ok = (ipix >= 0) & (ipix < npix)
+    ref = np.zeros(npix)
+    np.add.at(ref, ipix[ok], dat[ok])
+    for dt, tol in ((torch.float64, 1e-12), (torch.float32, 2e-5)):
+        m = torch.zeros(npix, dtype=dt, device=cuda)
+        K.tod2map_staged(m, dev(dat[None, :], dt), dev(ipix[None, :]))
+        assert rel(m.cpu().double().numpy(), ref) < tol, (n, dt)
+    assert K.tod2map_status() == 0
+
+
+def test_tod2map_staged_rejects_host_and_misaligned(K, gold):
+    g = gold("proj.npz")
+    host = torch.from_numpy(np.ascontiguousarray(g["dat"])).pin_memory()
+    with pytest.raises(ValueError):
+        K.tod2map_staged(dev(g["map"]), host, dev(g["ipix"]))
+    d = dev(g["dat"]).reshape(-1)
+    ip = dev(g["ipix"]).reshape(-1)
+    with pytest.raises(K._lib.MkError):  # 8-byte offset: not 16-byte aligned
+        K.tod2map_staged(dev(g["map"]), d[1:], ip[1:])
 
 
 def test_tod2map_rows_hits(K, gold):

@@ -85,3 +85,54 @@ def test_truncation_lengths_match_reference(gold):
     for n, t in zip(g["ndata"], g["truncated"]):
         assert oracle.truncate_len(int(n)) == int(t), n
     np.testing.assert_array_equal(oracle.find_good_fft_lens(1000, [2, 3, 5, 7, 11]), g["good1000"])
+
+
+def test_pointing_matches_reference(gold):
+    g = gold("pointing.npz")
+    for k in range(int(g["ncase"])):
+        ra, dec, lims = g[f"c{k}_ra"], g[f"c{k}_dec"], g[f"c{k}_lims"]
+        ps, ny, cosdec = float(g[f"c{k}_pixsize"]), int(g[f"c{k}_ny"]), float(g[f"c{k}_cosdec"])
+        assert np.array_equal(oracle.pix_car(ra, dec, lims, ps, ny), g[f"c{k}_car"])
+        assert np.array_equal(oracle.pix_car_trunc(ra, dec, lims, ps, cosdec, ny), g[f"c{k}_trunc"])
+        # points left of / below the limits: truncation toward zero differs from floor
+        assert (g[f"c{k}_trunc"] != g[f"c{k}_car"]).any()
+
+
+def test_wcs_car_reference_point_and_equatorial_case():
+    """Unpinned (astropy absent): the CAR WCS restatement maps crval to
+    crpix, and with crval on the equator it is the plain plate carree."""
+    ps = 2.0 / 3600 * np.pi / 180
+    for lims in ([3.5, 3.52, 0.30, 0.32], [0.7, 0.72, -0.42, -0.40]):
+        w = oracle.car_wcs(lims, ps)
+        p1, p2 = oracle.wcs_car_world2pix(np.array([w[0]]), np.array([w[1]]), w)
+        assert abs(p1[0] - 1) < 1e-9 and abs(p2[0] - 1) < 1e-9
+    w = np.array([0.0, 0.0, 1.0, 1.0, -0.01, 0.01])
+    ra, dec = np.array([-0.35, 0.2]), np.array([0.25, -0.3])
+    p1, p2 = oracle.wcs_car_world2pix(ra, dec, w)
+    assert np.allclose(p1, 1 + ra / -0.01, rtol=0, atol=1e-9)
+    assert np.allclose(p2, 1 + dec / 0.01, rtol=0, atol=1e-9)
+
+
+def test_pol_projections_invert_mul_match_reference(gold):
+    g = gold("pol.npz")
+    ipix, tg, dat = g["ipix"], g["twogamma"], g["dat"]
+    for tag in ("IQU", "QU"):
+        for add in (0, 1):
+            d = dat.copy()
+            oracle.polmap2tod(d, g[f"map_{tag}"], tag, tg, ipix, bool(add))
+            assert np.abs(d - g[f"m2t_{tag}_{add}"]).max() < 1e-12 * np.abs(g[f"m2t_{tag}_{add}"]).max()
+    for tag in ("IQU", "QU", "QU_PRECON", "IQU_PRECON"):
+        m = g[f"t2m_in_{tag}"].copy()
+        oracle.tod2polmap(m, dat, tag, tg, ipix)
+        assert np.abs(m - g[f"t2m_{tag}"]).max() < 1e-12 * np.abs(g[f"t2m_{tag}"]).max()
+    for tag in ("IQU", "QU"):
+        h = np.zeros_like(g[f"hits_{tag}"])
+        for k in range(2):
+            oracle.tod2polmap(h, np.ones(dat.shape), tag + "_PRECON", g[f"hits_t{k}_twogamma"],
+                              g[f"hits_t{k}_ipix"])
+        assert np.abs(h - g[f"hits_{tag}"]).max() < 1e-12 * np.abs(h).max()
+        inv = oracle.pol_invert(g[f"hits_{tag}"], tag + "_PRECON")
+        assert np.allclose(inv, g[f"inv_{tag}"], rtol=1e-9, atol=1e-12 * np.abs(inv).max())
+        mul = oracle.pol_precon_mul(g[f"inv_{tag}"], g[f"mulx_{tag}"], tag + "_PRECON")
+        assert np.allclose(mul, g[f"mul_{tag}"], rtol=1e-12, atol=0)
+        assert (h != 0).any()
