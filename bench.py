@@ -45,7 +45,8 @@ METRIC = "tod2map GB/s"
 BYTES_PER_SAMPLE = 12  # int32 pixel index + float64 sample
 # measured DRAM bytes per sample (read + write) of each FP64 tod2map kernel
 # on the 256 x 130978 small case (profiles/tod2map_fp64_c2.md)
-NCU_DRAM_BYTES_PER_SAMPLE = {"atomic": (404.58e6 + 2.9e6) / 33530368}
+NCU_DRAM_BYTES_PER_SAMPLE = {"atomic": (404.58e6 + 2.9e6) / 33530368,
+                             "staged": (404.27e6 + 3.14e6) / 33530368}
 
 
 def parse():
@@ -351,10 +352,17 @@ def run_ours(args):
     e2e_copy_gbs = world * S * BYTES_PER_SAMPLE / e2e_copy_s / 1e9
     del devbuf, host
 
-    # extras: the full hot path per PCG iteration
+    # extras: the other projection on the same samples (map2tod, FP64, set
+    # mode: 4 B pixel index read + 8 B sample written), and the full hot path
+    # per PCG iteration
     extras = {}
+    src = torch.randn(op.npix, dtype=torch.float64, device=dev)
+    m2t_ms, _, _ = time_steps(lambda: K.map2tod(op.tmp, src, op.ipix, False), args.steps, args.warmup, stream)
+    m2t_gbs = S * BYTES_PER_SAMPLE / (m2t_ms / args.steps * 1e-3) / 1e9
+    extras["map2tod"] = {"value": m2t_gbs, "unit": "GB/s", "ms_per_step": m2t_ms / args.steps,
+                         "frac_of_hbm": None, "bytes_per_sample": BYTES_PER_SAMPLE}
     if with_noise and rank == 0:
-        extras = pcg_extras(tv, m, dev)
+        extras.update(pcg_extras(tv, m, dev))
 
     peaks = {}
     try:
@@ -363,6 +371,7 @@ def run_ours(args):
         pass
     peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    extras["map2tod"]["frac_of_hbm"] = extras["map2tod"]["value"] / peak
     cpu = None
     if rank == 0 and world == 1:
         v, desc, kind, cores = cpu_tod2map_sample(host_sample(tv), op.npix, seconds=12.0)

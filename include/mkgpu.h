@@ -77,9 +77,10 @@ int mk_version(void);          /* returns the ABI version number (not a status) 
 int mk_map2tod(void *dat, const void *map, const int32_t *ipix, int64_t ndet,
                int64_t ndata, int64_t npix, int dtype, int do_add, void *stream);
 
-/* map[ipix[i]] += dat[i] with warp-aggregated atomic adds (runs of equal
- * consecutive pixels are summed in registers first).  Summation order, and
- * so the last bits, vary from run to run.  Out-of-range pixels are skipped.
+/* map[ipix[i]] += dat[i] with warp-aggregated atomic adds: runs of equal
+ * consecutive pixels are summed in registers and joined across the lanes of
+ * a warp, one atomic per run.  Summation order, and so the last bits, vary
+ * from run to run.  Out-of-range pixels are skipped.
  * Replaces tod2map_omp / tod2map_atomic, minkasi/lib/minkasi.c:59-66,97-112. */
 int mk_tod2map(void *map, const void *dat, const int32_t *ipix, int64_t ndet,
                int64_t ndata, int64_t npix, int dtype, void *stream);

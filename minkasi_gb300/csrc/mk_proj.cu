@@ -476,38 +476,102 @@ int map2tod_t(void *dat, const void *map, const int32_t *ipix, int64_t n, int64_
   return mk::launch_status("mk_map2tod");
 }
 
-// Per-thread runs over 8 consecutive samples (vector loads), one atomic per
-// run: ~1 add per sample instead of the warp scan's ~5, which matters for
-// FP64 on GB300 where the scan's FP64 adds bound the kernel.
+// Scatter with runs of equal pixel joined across the lanes of a warp: each
+// warp takes windows of 256 consecutive samples (8 per lane, 16-byte loads),
+// each lane sums its runs in registers, and warp_runs joins the runs that cross
+// lanes, so a run costs one L2 atomic whatever its alignment.  On GB300 the
+// scatter is bound by the L2 atomic rate, not by HBM: the same loads without
+// atomics stream at 7 TB/s, and one atomic per sample runs at 2.1 TB/s.
+//
+// warp_runs: lane l holds samples 8l .. 8l+7 of the window, the first m of
+// them valid (0 <= m <= 8; the valid samples of a window are a prefix of it).
+// Each lane sums its own runs and issues the atomics of the runs that start
+// and end inside it; the runs that cross lane boundaries are joined by a
+// segmented scan over the lanes, and each is added once, by the lane where it
+// ends.  With daisy scans a run of equal pixels is ~5 samples long, so joining
+// the runs cut by the 8-sample lane windows removes about 40 % of the atomics.
+template <typename T>
+__device__ __forceinline__ void warp_runs(T *__restrict__ map, const int32_t (&p)[8], const T (&v)[8], int m,
+                                          int lane, int64_t npix) {
+  int32_t kf = INT32_MIN, kl = INT32_MIN;  // first / last run keys of this lane
+  T sf = T(0), sl = T(0);
+  bool single = true;  // the lane's samples are one run
+  if (m > 0) {
+    int32_t key = p[0];
+    T cur = v[0];
+    kf = key;
+#pragma unroll
+    for (int j = 1; j < 8; j++) {
+      if (j < m) {
+        if (p[j] == key) {
+          cur += v[j];
+        } else {
+          if (single) {
+            sf = cur;
+            single = false;
+          } else if ((uint32_t)key < (uint64_t)npix) {
+            atomicAdd(map + key, cur);  // a run inside the lane
+          }
+          key = p[j];
+          cur = v[j];
+        }
+      }
+    }
+    kl = key;
+    sl = cur;
+    if (single) sf = cur;
+  }
+  const int32_t kl_prev = __shfl_up_sync(FULL, kl, 1);
+  const int32_t kf_next = __shfl_down_sync(FULL, kf, 1);
+  const bool cont_in = lane > 0 && m > 0 && kl_prev == kf;
+  const bool cont_out = lane < 31 && kf_next == kl && m > 0;
+  // out_l = y_l + [single_l and cont_in_l] out_{l-1}, y = the part handed on
+  T out = single ? sf : sl;
+  bool head = !(single && cont_in);
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const T up = __shfl_up_sync(FULL, out, off);
+    const bool hup = __shfl_up_sync(FULL, (int)head, off) != 0;
+    if (lane >= off) {
+      if (!head) out += up;
+      head = head || hup;
+    }
+  }
+  const T prev = __shfl_up_sync(FULL, out, 1);
+  const T cin = cont_in ? prev : T(0);
+  if (m == 0) return;
+  if (single) {
+    if (!cont_out && (uint32_t)kf < (uint64_t)npix) atomicAdd(map + kf, cin + sf);
+  } else {
+    if ((uint32_t)kf < (uint64_t)npix) atomicAdd(map + kf, cin + sf);
+    if (!cont_out && (uint32_t)kl < (uint64_t)npix) atomicAdd(map + kl, sl);
+  }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) k_tod2map_atomic8(T *__restrict__ map, const T *__restrict__ dat,
                                                          const int32_t *__restrict__ ipix, int64_t n,
                                                          int64_t npix) {
-  const int64_t n8 = n >> 3;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n8; g += stride) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t base = warp * 256; base < n; base += nwarp * 256) {
+    const int64_t i0 = base + 8 * lane;
+    const int64_t r = n - i0;
+    const int m = r <= 0 ? 0 : (r >= 8 ? 8 : (int)r);
     int32_t p[8];
     T v[8];
-    load8i(ipix + 8 * g, p);
-    load8(dat + 8 * g, v);
-    int32_t key = p[0];
-    T cur = v[0];
+    if (m == 8) {
+      load8i(ipix + i0, p);
+      load8(dat + i0, v);
+    } else {
 #pragma unroll
-    for (int k = 1; k < 8; k++) {
-      if (p[k] == key) {
-        cur += v[k];
-      } else {
-        if ((uint32_t)key < (uint64_t)npix) atomicAdd(map + key, cur);
-        key = p[k];
-        cur = v[k];
+      for (int j = 0; j < 8; j++) {
+        p[j] = j < m ? ipix[i0 + j] : INT32_MIN;
+        v[j] = j < m ? dat[i0 + j] : T(0);
       }
     }
-    if ((uint32_t)key < (uint64_t)npix) atomicAdd(map + key, cur);
-  }
-  if (blockIdx.x == 0 && threadIdx.x < (n & 7)) {
-    int64_t i = (n8 << 3) + threadIdx.x;
-    int32_t key = ipix[i];
-    if ((uint32_t)key < (uint64_t)npix) atomicAdd(map + key, dat[i]);
+    warp_runs<T>(map, p, v, m, lane, npix);
   }
 }
 
@@ -515,8 +579,10 @@ template <typename T, bool ROWS>
 int tod2map_t(void *map, const void *dat, const int32_t *ipix, int64_t n, int64_t npix,
               const void *rowval, int64_t ndata, cudaStream_t st) {
   const int B = 256;
-  if (!ROWS && sizeof(T) == 8 && (uintptr_t)dat % 16 == 0 && (uintptr_t)ipix % 16 == 0) {
-    k_tod2map_atomic8<T><<<mk_grid_fit(k_tod2map_atomic8<T>, (n + 7) / 8, B), B, 0, st>>>((T *)map, (const T *)dat, ipix, n, npix);
+  if (!ROWS && (uintptr_t)dat % 16 == 0 && (uintptr_t)ipix % 16 == 0) {
+    // more CTAs than fit at once: the warps' windows are short, and a deep
+    // queue of CTAs keeps every SM's atomic issue busy to the end
+    k_tod2map_atomic8<T><<<mk_grid((n + 7) / 8, B, 16), B, 0, st>>>((T *)map, (const T *)dat, ipix, n, npix);
     return mk::launch_status("mk_tod2map");
   }
   constexpr int U = 4;
@@ -531,8 +597,8 @@ int tod2map_t(void *map, const void *dat, const int32_t *ipix, int64_t n, int64_
 // and values) through a ring of SSTG shared-memory stages.  One producer
 // warp issues the cp.async.bulk copies of each chunk; they complete on the
 // stage's "full" mbarrier.  SCW consumer warps each reduce their 256 samples
-// of the chunk (8 consecutive samples per lane: runs of equal pixels summed in
-// registers, one L2 atomic per run, as k_tod2map_atomic8) and arrive on the
+// of the chunk (8 consecutive samples per lane; runs of equal pixels summed in
+// registers and joined across lanes by warp_runs, one L2 atomic per run) and arrive on the
 // stage's "empty" mbarrier, which the producer waits on before refilling the
 // stage.  No CTA-wide barrier sits in the loop, so the consumer warps drift
 // freely and several chunks per CTA are in flight from HBM at any time.
@@ -606,23 +672,6 @@ __device__ __forceinline__ void smem_load8(const int32_t *sp, const T *sv, int t
   }
 }
 
-template <typename T, int M>
-__device__ __forceinline__ void reduce_runs(T *__restrict__ map, const int32_t *p, const T *v, int64_t npix) {
-  int32_t key = p[0];
-  T cur = v[0];
-#pragma unroll
-  for (int k = 1; k < M; k++) {
-    if (p[k] == key) {
-      cur += v[k];
-    } else {
-      if ((uint32_t)key < (uint64_t)npix) atomicAdd(map + key, cur);
-      key = p[k];
-      cur = v[k];
-    }
-  }
-  if ((uint32_t)key < (uint64_t)npix) atomicAdd(map + key, cur);
-}
-
 template <typename T>
 __global__ void __launch_bounds__(STHREADS) k_tod2map_staged(T *__restrict__ map, const T *__restrict__ dat,
                                                              const int32_t *__restrict__ ipix, int64_t n,
@@ -681,21 +730,20 @@ __global__ void __launch_bounds__(STHREADS) k_tod2map_staged(T *__restrict__ map
       }
       const int64_t rem = n4 - c * SCH;
       const int cnt = (int)(rem < SCH ? rem : SCH);
-      if (j0 + 8 <= cnt) {
-        int32_t p[8];
-        T v[8];
+      int32_t p[8];
+      T v[8];
+      int mv = cnt - j0;
+      mv = mv < 0 ? 0 : (mv > 8 ? 8 : mv);
+      if (mv == 8) {
         smem_load8(sm.pix[s], sm.val[s], t, p, v);
-        reduce_runs<T, 8>(map, p, v, npix);
-      } else if (j0 < cnt) {  // cnt is a multiple of 4: exactly 4 left
-        int32_t p[4];
-        T v[4];
+      } else {
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-          p[j] = sm.pix[s][j0 + j];
-          v[j] = sm.val[s][j0 + j];
+        for (int j = 0; j < 8; j++) {
+          p[j] = j < mv ? sm.pix[s][j0 + j] : INT32_MIN;
+          v[j] = j < mv ? sm.val[s][j0 + j] : T(0);
         }
-        reduce_runs<T, 4>(map, p, v, npix);
       }
+      warp_runs<T>(map, p, v, mv, lane, npix);
       __syncwarp();
       if (lane == 0) mk::mbar_arrive(&sm.empty[s]);
     }

@@ -1,7 +1,14 @@
 """Solver experiments on the benchmark configurations (time to an FP64
 residual, map error per refinement step, learned vs Jacobi).
 
-    python -m minkasi_gb300.experiments --config c1 --tol 1e-6 [--learned] [--pairs 5000]
+    python -m minkasi_gb300.experiments --config c1 --tol 1e-6 [--no-learned] [--pairs 5000]
+    python -m minkasi_gb300.experiments --config c4 --large [--no-learned] [--wall 600]
+
+The --large form is the 200-TOD batching run (run_large): per-iteration
+times of FP64 Jacobi PCG and of the mixed-precision PCG, the mixed solve to
+tol, and (unless --no-learned) the learned preconditioner trained on pairs
+from PCG runs on b = A s with known synthetic skies s, then the mixed solve
+with it.
 
 For one synthetic configuration this builds the TODs and noise models on the
 GPU, the FP64 right-hand side b = sum P^T N d, the hit map and the Jacobi
@@ -170,7 +177,8 @@ def hit_density(hits: torch.Tensor) -> float:
 
 
 def run_large(config: str = "c4", tol: float = 1e-6, max_iter: int = 3000, wall_limit_s: float = 900.0,
-              log=print) -> dict:
+              learned: bool = False, pair_skies=(1000, 1001), pair_iters: int = 240, n_white: int = 64,
+              epochs: int = 12, batch: int = 4, log=print) -> dict:
     """The batching configuration: TODs generated one at a time (each TOD's
     RHS contribution is accumulated and its timestream dropped), one pooled
     operator per precision over all TODs, per-iteration times of FP64 Jacobi
@@ -252,6 +260,38 @@ def run_large(config: str = "c4", tol: float = 1e-6, max_iter: int = 3000, wall_
                           "iteration_budget": budget}
     out["jacobi_f64_projected_s"] = xs.niter * ms64 / 1e3
     out["projected_speedup_mixed_vs_jacobi_f64"] = out["jacobi_f64_projected_s"] / tm
+    if learned:
+        # training pairs: PCG iterates on b = A s for seeded skies s (known
+        # solution), through the FP32 operator, plus white (A v, v) pairs
+        del xs
+        torch.cuda.empty_cache()
+        t2 = time.perf_counter()
+        mop = MixedOp(op32, m.npix, dev)
+        R, E = L.known_solution_pairs(mop, m, hits, list(pair_skies), cfg.pixsize_arcsec,
+                                      n_iter=pair_iters, every=3)
+        rw, ew = L.white_pairs(op32, hits, n_white)
+        R, E = torch.cat([R, rw]), torch.cat([E, ew])
+        del rw, ew
+        torch.cuda.synchronize()
+        t_pairs = time.perf_counter() - t2
+        net = L.ConvNet.init(seed=0, device=dev)
+        t3 = time.perf_counter()
+        hist_loss = L.train(net, hits, (m.nx, m.ny), R, E, epochs=epochs, batch=batch)
+        torch.cuda.synchronize()
+        t_train = time.perf_counter() - t3
+        npairs = int(R.shape[0])
+        del R, E
+        torch.cuda.empty_cache()
+        mlearn = L.LearnedPrecon(hits, net, (m.nx, m.ny))
+        hist_l = []
+        xl, tl = timed(lambda: run_pcg_mixed(b, x0, tv, pre_ms, tol=tol, max_iter=budget, history=hist_l,
+                                             inner_precon=mlearn))
+        out["learned"] = {"pairs": npairs, "pair_gen_s": t_pairs, "train_s": t_train, "epochs": epochs,
+                          "loss_first": hist_loss[0], "loss_last": hist_loss[-1]}
+        out["mixed_learned_solve"] = {"iters": xl.niter, "fp64_residuals": xl.outer, "wall_s": tl,
+                                      "true_rel_residual": xl.rel_residual, "reached_tol": xl.rel_residual <= tol}
+        out["projected_speedup_mixed_learned_vs_jacobi_f64"] = out["jacobi_f64_projected_s"] / tl
+        L.save(net, f"/tmp/mk_learned_{config}.npz")
     return out
 
 
@@ -265,9 +305,11 @@ if __name__ == "__main__":
     ap.add_argument("--inner", type=int, default=20)
     ap.add_argument("--large", action="store_true", help="the pooled large-configuration run")
     ap.add_argument("--wall", type=float, default=900.0)
+    ap.add_argument("--large-epochs", type=int, default=12)
     a = ap.parse_args()
     if a.large:
-        res = run_large(a.config, a.tol, wall_limit_s=a.wall)
+        res = run_large(a.config, a.tol, wall_limit_s=a.wall, learned=not a.no_learned,
+                        epochs=a.large_epochs)
     else:
         res = run(a.config, a.tol, not a.no_learned, a.pairs, a.epochs, a.inner)
     print(json.dumps(res))

@@ -1,6 +1,6 @@
 """Kernel micro-benchmarks on one synthetic TOD shape (CUDA events, best of N).
 
-    python -m minkasi_gb300.kbench [--config c2s] [--only tod2map,map2tod,rot,noise,dct]
+    python -m minkasi_gb300.kbench [--config c2s] [--only tod2map,map2tod,rot,noise,dct,conv]
 
 Uses the first TOD shape and daisy pointing of a synthetic configuration
 (default c2s: 256 detectors x 130978 samples onto a 1024x1024 map) with
@@ -47,7 +47,7 @@ def run(config: str = "c2s", only=None) -> dict:
     npix = cfg.nx * cfg.ny
     N = ndet * n
     out = {"config": config, "ndet": ndet, "ndata": n, "npix": npix, "samples": N}
-    want = set(only) if only else {"map2tod", "tod2map", "rot", "noise", "dct"}
+    want = set(only) if only else {"map2tod", "tod2map", "rot", "noise", "dct", "conv"}
     g = torch.Generator(device=dev).manual_seed(0)
     for dt, es in ((torch.float64, 8), (torch.float32, 4)):
         tag = "f64" if es == 8 else "f32"
@@ -108,7 +108,27 @@ def run(config: str = "c2s", only=None) -> dict:
             del d
         del plan
         torch.cuda.empty_cache()
+    if "conv" in want:
+        out.update(conv_bench(dev))
     return out
+
+
+def conv_bench(dev, hw: int = 2048, batch: int = 1, c: int = 16) -> dict:
+    """The learned preconditioner's 3x3 convolutions on (batch, c, hw, hw)
+    FP32 maps: fwd, adjoint and weight gradient of a c->c layer, counted as
+    2 * 9 * c * c flops per pixel each."""
+    from . import learned as L
+    g = torch.Generator(device=dev).manual_seed(1)
+    x = torch.randn((batch, c, hw, hw), generator=g, dtype=torch.float32, device=dev)
+    w = torch.randn((c, c, 3, 3), generator=g, dtype=torch.float32, device=dev) * 0.1
+    h = torch.randn_like(x)
+    flops = 2 * 9 * c * c * batch * hw * hw
+    res = {}
+    for name, fn in (("conv_fwd", lambda: L.conv_fwd(x, w)), ("conv_adj", lambda: L.conv_adj(h, w)),
+                     ("conv_wgrad", lambda: L.conv_wgrad(x, h))):
+        ms = best_ms(fn)
+        res[name] = {"ms": ms, "TFLOPs": flops / ms / 1e9, "shape": [batch, c, hw, hw]}
+    return res
 
 
 if __name__ == "__main__":

@@ -12,7 +12,9 @@ the elementwise ``precon * r`` of run_pcg (minkasi/mapmaking/pcg.py:157-158).
 Training data are (r_k, A^-1 r_k) pairs from the mapmaker's own converged
 solves on seeded synthetic skies: for each sky, Jacobi PCG runs to a tight
 FP64 tolerance, recording every iterate; once converged, x* - x_k = A^-1 r_k
-for every recorded residual r_k.  Skies are a Gaussian random field with
+for every recorded residual r_k.  At large map sizes, where converged
+solves are costly, known_solution_pairs runs PCG on b = A s for a seeded sky
+s whose solution is known.  Skies are a Gaussian random field with
 C_l ~ l^-2.5 plus random beta-model clusters.
 
 Loss per pair: ||P(M r - e)||^2 / ||P e||^2, P removing the hit-region mean
@@ -239,6 +241,38 @@ def solve_pairs(op64, m, hits: torch.Tensor, skies: Sequence[int], pix_arcsec: f
             R.append(rk.float())
             E.append((xstar - xk).float())
     return torch.stack(R), torch.stack(E), iters
+
+
+def known_solution_pairs(op, m, hits: torch.Tensor, skies: Sequence[int], pix_arcsec: float,
+                         n_iter: int = 300, every: int = 3, keep_above: float = 1e-5):
+    """(r_k, s - x_k) pairs from Jacobi PCG runs on b = A s for seeded
+    synthetic skies s.  The solution is known, so no converged solve is
+    needed; the constant map that A annihilates is removed by the loss's
+    projection.  ``op`` is any operator with apply(x, out) on FP64 maps (the
+    FP32 operator through MixedOp at large sizes).  Every ``every``-th iterate
+    whose recursive residual is above ``keep_above`` becomes a pair."""
+    from ._lib import MK_S_RR
+    from .pcg import DevicePCG
+
+    dev = hits.device
+    M = torch.where(hits > 0, 1.0 / hits.clamp(min=1), torch.zeros_like(hits)).reshape(-1).double()
+    R, E = [], []
+    for seed in skies:
+        truth = sky(m.nx, m.ny, pix_arcsec, seed, dev).reshape(-1)
+        b = torch.zeros_like(truth)
+        op.apply(truth, b)
+        bn2 = float((b * b).sum())
+        x = torch.zeros_like(b)
+        st = DevicePCG(op, b, x, M, graph=True)
+        st.start()
+        for k in range(n_iter):
+            if math.sqrt(max(float(st.s[MK_S_RR]), 0.0) / bn2) <= keep_above:
+                break
+            if k % every == 0:
+                R.append(st.r.float())
+                E.append((truth - st.x).float())
+            st.step()
+    return torch.stack(R), torch.stack(E)
 
 
 def white_pairs(op, hits: torch.Tensor, n: int, seed: int = 0):

@@ -125,11 +125,13 @@ def test_tod2map_staged_golden(K, gold):
     assert K.tod2map_status() == 0
 
 
-@pytest.mark.parametrize("n", [1, 3, 4, 5, 2047, 2048, 2049, 2052, 3 * 2048 * 152 + 6, 6_000_001])
-def test_tod2map_staged_ragged_sizes_and_bad_pixels(K, n):
-    """Chunk edges, the <4-sample tail, more chunks than CTAs (6e6 samples:
-    every CTA wraps its stage ring several times), and pixels
-    outside [0, npix) (skipped), FP64 and FP32, against numpy."""
+@pytest.mark.parametrize("kern", ["tod2map", "tod2map_staged"])
+@pytest.mark.parametrize("n", [1, 3, 4, 5, 255, 257, 2047, 2048, 2049, 2052, 3 * 2048 * 152 + 6, 6_000_001])
+def test_tod2map_ragged_sizes_and_bad_pixels(K, n, kern):
+    """Warp-window and chunk edges, the <4-sample tail, more chunks than CTAs
+    (6e6 samples: every staged CTA wraps its stage ring several times), runs
+    that cross lanes and windows, and pixels outside [0, npix) (skipped),
+    FP64 and FP32, against numpy."""
     rng = np.random.default_rng(n)
     npix = 300
     walk = np.cumsum(rng.integers(-1, 2, size=n)) // 3
@@ -140,7 +142,7 @@ def test_tod2map_staged_ragged_sizes_and_bad_pixels(K, n):
     np.add.at(ref, ipix[ok], dat[ok])
     for dt, tol in ((torch.float64, 1e-12), (torch.float32, 2e-5)):
         m = torch.zeros(npix, dtype=dt, device=cuda)
-        K.tod2map_staged(m, dev(dat[None, :], dt), dev(ipix[None, :]))
+        getattr(K, kern)(m, dev(dat[None, :], dt), dev(ipix[None, :]))
         assert rel(m.cpu().double().numpy(), ref) < tol, (n, dt)
     assert K.tod2map_status() == 0
 
