@@ -45,8 +45,8 @@ METRIC = "tod2map GB/s"
 BYTES_PER_SAMPLE = 12  # int32 pixel index + float64 sample
 # measured DRAM bytes per sample (read + write) of each FP64 tod2map kernel
 # on the 256 x 130978 small case (profiles/tod2map_fp64_c2.md)
-NCU_DRAM_BYTES_PER_SAMPLE = {"atomic": (404.58e6 + 2.9e6) / 33530368,
-                             "staged": (404.27e6 + 3.14e6) / 33530368}
+NCU_DRAM_BYTES_PER_SAMPLE = {"atomic": (404.32e6 + 3.30e6) / 33530368,
+                             "staged": (404.30e6 + 2.87e6) / 33530368}
 
 
 def parse():

@@ -525,25 +525,31 @@ __device__ __forceinline__ void warp_runs(T *__restrict__ map, const int32_t (&p
   const int32_t kf_next = __shfl_down_sync(FULL, kf, 1);
   const bool cont_in = lane > 0 && m > 0 && kl_prev == kf;
   const bool cont_out = lane < 31 && kf_next == kl && m > 0;
-  // out_l = y_l + [single_l and cont_in_l] out_{l-1}, y = the part handed on
+  // out_l = y_l + [single_l and cont_in_l] out_{l-1}, y = the part handed on.
+  // A run passes through a lane only if the lane is one run that continues
+  // a run from the previous lane; when no lane of the warp does (the common
+  // case), out = y and one shuffle suffices.  The segmented scan, whose FP64
+  // adds are costly on GB300's narrow FP64 pipe, runs only otherwise.
   T out = single ? sf : sl;
-  bool head = !(single && cont_in);
+  if (__ballot_sync(FULL, single && cont_in) != 0u) {
+    bool head = !(single && cont_in);
 #pragma unroll
-  for (int off = 1; off < 32; off <<= 1) {
-    const T up = __shfl_up_sync(FULL, out, off);
-    const bool hup = __shfl_up_sync(FULL, (int)head, off) != 0;
-    if (lane >= off) {
-      if (!head) out += up;
-      head = head || hup;
+    for (int off = 1; off < 32; off <<= 1) {
+      const T up = __shfl_up_sync(FULL, out, off);
+      const bool hup = __shfl_up_sync(FULL, (int)head, off) != 0;
+      if (lane >= off) {
+        if (!head) out += up;
+        head = head || hup;
+      }
     }
   }
   const T prev = __shfl_up_sync(FULL, out, 1);
-  const T cin = cont_in ? prev : T(0);
   if (m == 0) return;
+  const T first = cont_in ? prev + sf : sf;  // the first run, with what flows in
   if (single) {
-    if (!cont_out && (uint32_t)kf < (uint64_t)npix) atomicAdd(map + kf, cin + sf);
+    if (!cont_out && (uint32_t)kf < (uint64_t)npix) atomicAdd(map + kf, first);
   } else {
-    if ((uint32_t)kf < (uint64_t)npix) atomicAdd(map + kf, cin + sf);
+    if ((uint32_t)kf < (uint64_t)npix) atomicAdd(map + kf, first);
     if (!cont_out && (uint32_t)kl < (uint64_t)npix) atomicAdd(map + kl, sl);
   }
 }
