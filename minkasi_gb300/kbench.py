@@ -1,6 +1,6 @@
 """Kernel micro-benchmarks on one synthetic TOD shape (CUDA events, best of N).
 
-    python -m minkasi_gb300.kbench [--config c2s] [--only tod2map,map2tod,rot,noise,dct,conv]
+    python -m minkasi_gb300.kbench [--config c2s] [--only tod2map,map2tod,rot,noise,dct,conv,point,pol]
 
 Uses the first TOD shape and daisy pointing of a synthetic configuration
 (default c2s: 256 detectors x 130978 samples onto a 1024x1024 map) with
@@ -110,7 +110,49 @@ def run(config: str = "c2s", only=None) -> dict:
         torch.cuda.empty_cache()
     if "conv" in want:
         out.update(conv_bench(dev))
+    if want & {"point", "pol"}:
+        out.update(point_pol_bench(cfg, ndet, n, dev, want))
     return out
+
+
+def point_pol_bench(cfg, ndet: int, n: int, dev, want) -> dict:
+    """Pointing -> pixel (16 B of RA/dec read, 4 B written per sample) and
+    the IQU projections with cached cos/sin 2gamma (4 B pixel + 16 B angle
+    terms + 8 B sample per sample), FP64, on the configuration's first TOD."""
+    info = make_tod_info(cfg, 0, ndet, n, dev, with_data=False, with_radec=True)
+    ra, dec = info["dx"].contiguous(), info["dy"].contiguous()
+    N = ndet * n
+    res = {}
+    if "point" in want:
+        lims = [float(ra.min()), float(ra.max()), float(dec.min()), float(dec.max())]
+        ps = cfg.pixsize_arcsec * torch.pi / 180 / 3600
+        ny = int((lims[3] - lims[2]) / ps) + 3
+        cosdec = float(torch.cos(torch.tensor(0.5 * (lims[2] + lims[3]), dtype=torch.float64)))
+        out = torch.empty((ndet, n), dtype=torch.int32, device=dev)
+        ms = best_ms(lambda: K.pix_car(ra, dec, lims[0], lims[2], ps, cosdec, ny, out=out))
+        res["pix_car"] = {"ms": ms, "GBs": N * 20 / ms / 1e6}
+        w6 = [lims[1] * 180 / torch.pi, lims[2] * 180 / torch.pi, 1.0, 1.0, -ps * 180 / torch.pi,
+              ps * 180 / torch.pi]
+        ms = best_ms(lambda: K.pix_wcs_car(ra, dec, w6, ny, out=out))
+        res["pix_wcs_car"] = {"ms": ms, "GBs": N * 20 / ms / 1e6, "Gsamp_per_s": N / ms / 1e6}
+    if "pol" in want:
+        g = torch.Generator(device=dev).manual_seed(3)
+        tg = torch.rand((ndet, n), generator=g, dtype=torch.float64, device=dev) * 6.283185307179586
+        ms = best_ms(lambda: K.pol_sincos(tg))
+        res["pol_sincos"] = {"ms": ms, "GBs": N * 24 / ms / 1e6}
+        cs = K.pol_sincos(tg)
+        ipix = info["ipix"]
+        npix = cfg.nx * cfg.ny
+        mp = torch.randn((npix, 3), generator=g, dtype=torch.float64, device=dev)
+        dat = torch.empty((ndet, n), dtype=torch.float64, device=dev)
+        ms = best_ms(lambda: K.polmap2tod(dat, mp, "IQU", cs, ipix, False))
+        res["polmap2tod_iqu"] = {"ms": ms, "GBs": N * 28 / ms / 1e6}
+        acc = torch.zeros((npix, 3), dtype=torch.float64, device=dev)
+        ms = best_ms(lambda: K.tod2polmap(acc, dat, "IQU", cs, ipix))
+        res["tod2polmap_iqu"] = {"ms": ms, "GBs": N * 28 / ms / 1e6}
+        ms = best_ms(lambda: K.polmap2tod(dat, mp, "IQU", tg, ipix, False))
+        res["polmap2tod_iqu_twogamma"] = {"ms": ms, "GBs": N * 20 / ms / 1e6}
+    return res
 
 
 def conv_bench(dev, hw: int = 2048, batch: int = 1, c: int = 16) -> dict:
