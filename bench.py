@@ -16,9 +16,10 @@ region (in chunks overlapped with the scatter), and the map read back to the
 host every step; the pixel indices stay cached on the device as the API
 caches them (tod.info[tag]).
 
-Extra keys: per-iteration timings of the full hot path (FP64 Jacobi PCG
-iteration = batched A-apply + update, and the FP32 inner iteration of the
-mixed-precision solver) on the same TODs, and the CPU baseline.
+Extra keys: map2tod GB/s on the same samples; per-iteration timings of the
+full hot path (FP64 Jacobi PCG iteration = batched A-apply + update, and the
+FP32 inner iteration of the mixed-precision solver) on the same TODs, and
+the reference's CPU operator per iteration (a bounded sample, scaled).
 
 --impl reference times the reference's CPU tod2map (its own C compiled from
 source when available in oracle/_ref, else the C restatement in oracle/)
@@ -216,6 +217,39 @@ def cpu_tod2map_sample(tods_host, npix, seconds=12.0, prefer_ref=True):
     return nbytes / t_used / 1e9, desc, kind, cores
 
 
+def cpu_pcg_iter_sample(tv, npix, seconds=20.0):
+    """Seconds per PCG iteration of the reference's CPU operator (map2tod +
+    NoiseSmoothedSVD.apply_noise with scipy's DCT-I, the shipped transform,
+    on all host threads + tod2map), measured on the first TOD(s) of the
+    workload and scaled to all of its samples."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+
+    cores = os.cpu_count() or 1
+    x = np.random.default_rng(0).standard_normal(npix)
+    out = np.zeros(npix)
+    used, samp, ntod = 0.0, 0, 0
+    for t in tv.tods:
+        nz = t.noise
+        ip = np.ascontiguousarray(t.info["ipix"].cpu().numpy())
+        v, vT, w = (a.detach().cpu().numpy() for a in (nz.v, nz.vT, nz.mywt))
+        nv = None if nz.noisevec is None else nz.noisevec.detach().cpu().numpy()
+        d = np.zeros(ip.shape)
+        t0 = time.perf_counter()
+        oracle.map2tod(d, x, ip, False)
+        d = oracle.apply_noise(v, vT, w, d, nv, workers=cores)
+        oracle.tod2map(out, d, ip, nthread=cores)
+        used += time.perf_counter() - t0
+        samp += ip.size
+        ntod += 1
+        if used >= seconds:
+            break
+    total = tv.get_nsamp()
+    return {"s_per_iter": used / samp * total, "unit": "s", "cores": cores, "kind": "port",
+            "sample": f"{ntod} of the workload's TODs ({samp} samples), scaled to {total} samples; "
+                      f"oracle C projections + numpy/scipy DCT-I apply_noise, {cores} threads"}
+
+
 def host_sample(tv, max_samples=3.5e8):
     out, tot = [], 0
     for t in tv.tods:
@@ -376,6 +410,8 @@ def run_ours(args):
     if rank == 0 and world == 1:
         v, desc, kind, cores = cpu_tod2map_sample(host_sample(tv), op.npix, seconds=12.0)
         cpu = {"value": v, "unit": "GB/s", "cores": cores, "kind": kind, "sample": desc}
+        if with_noise:
+            extras["pcg_iter_cpu_reference"] = cpu_pcg_iter_sample(tv, op.npix)
     if rank != 0:
         return
     clocks = clk.summary()
