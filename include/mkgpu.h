@@ -32,6 +32,9 @@
  *                         tod2map_{iqu,qu}_simple, tod2map_{iqu,qu}_precon_simple,
  *                         minkasi/lib/minkasi.c:146-245, and PolMap.__mul__,
  *                         minkasi/maps/polmap.py:624-684
+ *  mk_cuts_* / mk_stripes_* / mk_binned_* <- tod2cuts / cuts2tod (minkasi/lib/minkasi.c:260-284),
+ *                         map2tod_destriped / tod2map_destriped / *_binned_det,
+ *                         minkasi/mapmaking/map2tod.py:156-253, tod2map.py:242-340
  *  mk_tod2map_rows     <- make_hits' tod2map of a ones / outer(weights, ones) TOD,
  *                         minkasi/mapmaking/tod2map.py:343-400
  *  mk_dct1_*           <- many_fft_r2r_1d / many_fftf_r2r_1d (REDFT00),
@@ -169,6 +172,51 @@ int mk_tod2polmap(void *map, const void *dat, const void *cos2g, const void *sin
  * Replaces PolMap.__mul__, minkasi/maps/polmap.py:624-684. */
 int mk_pol_precon_mul(void *out, const void *precon, const void *map, int64_t npix, int mode,
                       int dtype, void *stream);
+
+/* ---- per-TOD model members of a Mapset (cuts, stripes, binned) ---------
+ * dtype-typed dat / vec / pars; index arrays int64 (the reference's imap and
+ * segment edges).  Indices outside their array are skipped. */
+
+/* vec[i] (+)= dat[imap[i]], i < ncut, imap into the ndat samples of a TOD.
+ * Replaces tod2cuts, minkasi/lib/minkasi.c:260-268 (CutsCompact.tod2map,
+ * minkasi/tods/cuts.py:351-383). */
+int mk_cuts_gather(void *vec, const void *dat, const int64_t *imap, int64_t ncut, int64_t ndat,
+                   int dtype, int do_add, void *stream);
+
+/* dat[imap[i]] (+)= vec[i] (atomic adds with do_add, so overlapping cut
+ * segments add up as in the reference's serial loop).  Replaces cuts2tod,
+ * minkasi/lib/minkasi.c:271-284 (CutsCompact.map2tod, cuts.py:385-417). */
+int mk_cuts_scatter(void *dat, const void *vec, const int64_t *imap, int64_t ncut, int64_t ndat,
+                    int dtype, int do_add, void *stream);
+
+/* Destriper: dat[d, t] (+)= pars[d, s] for lims[s] <= t < lims[s+1];
+ * pars (ndet, nseg), lims (nseg + 1) on the device.  Replaces
+ * map2tod_destriped, minkasi/mapmaking/map2tod.py:156-190 (tsStripes). */
+int mk_stripes_map2tod(void *dat, const void *pars, const int64_t *lims, int64_t ndet,
+                       int64_t ndata, int64_t nseg, int dtype, int do_add, void *stream);
+
+/* pars[d, s] (+)= sum of dat[d, lims[s] .. lims[s+1]-1], a fixed reduction
+ * order per segment (reproducible): the transpose of mk_stripes_map2tod.
+ * Replaces tod2map_destriped, minkasi/mapmaking/tod2map.py:242-269. */
+int mk_stripes_tod2map(void *pars, const void *dat, const int64_t *lims, int64_t ndet,
+                       int64_t ndata, int64_t nseg, int dtype, int do_add, void *stream);
+
+/* Binned model: b(t) = int64((vec[t] - lo) * (nbin / (hi - lo))), vec FP64 of
+ * ndata entries shared by the detectors (vec_per_det = 0) or (ndet, ndata).
+ * dat[d, t] (+)= pars[d, b(t)] (0 outside [0, nbin) when not adding).
+ * Replaces map2tod_binned_det, minkasi/mapmaking/map2tod.py:195-253 (tsBinnedAz). */
+int mk_binned_map2tod(void *dat, const void *pars, const double *vec, int64_t ndet, int64_t ndata,
+                      int64_t nbin, double lo, double hi, int vec_per_det, int dtype, int do_add,
+                      void *stream);
+
+/* pars[d, b] (+)= sum of dat[d, t] over the samples with b(t) = b: the exact
+ * transpose of mk_binned_map2tod.  The reference's tod2map_binned_det
+ * (minkasi/mapmaking/tod2map.py:272-340) writes pars[det][inds] += mat[det]
+ * with numpy / numba fancy indexing, which keeps one sample per repeated bin;
+ * this sums them all, as the adjoint that a PCG operator needs. */
+int mk_binned_tod2map(void *pars, const void *dat, const double *vec, int64_t ndet, int64_t ndata,
+                      int64_t nbin, double lo, double hi, int vec_per_det, int dtype, int do_add,
+                      void *stream);
 
 /* make_hits helper: map[ipix[d,t]] += w[d] (w == NULL: += 1).  w and map
  * dtype-typed.  Replaces the tod2map of np.ones / np.outer(weights, ones)

@@ -42,6 +42,12 @@ SIGNATURES = {
     "mk_tod2map_rows": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _i32, _vp]),
     "mk_pix_car": (_i32, [_vp, _vp, _vp, _i64, _dbl, _dbl, _dbl, _dbl, _i64, _i32, _vp]),
     "mk_pix_wcs_car": (_i32, [_vp, _vp, _vp, _i64, _vp, _i64, _vp]),
+    "mk_cuts_gather": (_i32, [_vp, _vp, _vp, _i64, _i64, _i32, _i32, _vp]),
+    "mk_cuts_scatter": (_i32, [_vp, _vp, _vp, _i64, _i64, _i32, _i32, _vp]),
+    "mk_stripes_map2tod": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _i32, _i32, _vp]),
+    "mk_stripes_tod2map": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _i32, _i32, _vp]),
+    "mk_binned_map2tod": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _dbl, _dbl, _i32, _i32, _i32, _vp]),
+    "mk_binned_tod2map": (_i32, [_vp, _vp, _vp, _i64, _i64, _i64, _dbl, _dbl, _i32, _i32, _i32, _vp]),
     "mk_pol_npol": (_i32, [_i32]),
     "mk_pol_sincos": (_i32, [_vp, _vp, _vp, _i64, _i32, _vp]),
     "mk_polmap2tod": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _i64, _i64, _i64, _i32, _i32, _i32, _vp]),

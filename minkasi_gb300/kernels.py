@@ -226,6 +226,79 @@ def pol_precon_mul(out: torch.Tensor, precon: torch.Tensor, map: torch.Tensor, m
                                   _stream()), "pol_precon_mul")
 
 
+def _i64(t: torch.Tensor, name: str) -> None:
+    _dev(t, name)
+    if t.dtype != torch.int64:
+        raise TypeError(f"{name} must be int64")
+
+
+def cuts_gather(vec: torch.Tensor, dat: torch.Tensor, imap: torch.Tensor, do_add: bool = True) -> None:
+    """vec (+)= dat.flat[imap]  (mk_cuts_gather; tod2cuts)."""
+    _dev(vec, "vec"), _dev(dat, "dat"), _i64(imap, "imap")
+    if vec.dtype != dat.dtype or vec.numel() != imap.numel():
+        raise ValueError("vec must match dat's dtype and have one entry per index")
+    check(lib().mk_cuts_gather(_p(vec), _p(dat), _p(imap), imap.numel(), dat.numel(), dtype_code(dat),
+                               int(bool(do_add)), _stream()), "cuts_gather")
+
+
+def cuts_scatter(dat: torch.Tensor, vec: torch.Tensor, imap: torch.Tensor, do_add: bool = True) -> None:
+    """dat.flat[imap] (+)= vec  (mk_cuts_scatter; cuts2tod)."""
+    _dev(vec, "vec"), _dev(dat, "dat"), _i64(imap, "imap")
+    if vec.dtype != dat.dtype or vec.numel() != imap.numel():
+        raise ValueError("vec must match dat's dtype and have one entry per index")
+    check(lib().mk_cuts_scatter(_p(dat), _p(vec), _p(imap), imap.numel(), dat.numel(), dtype_code(dat),
+                                int(bool(do_add)), _stream()), "cuts_scatter")
+
+
+def _stripes_args(dat, pars, lims):
+    _dev(dat, "dat"), _dev(pars, "pars"), _i64(lims, "lims")
+    ndet, ndata = _nd(dat)
+    nseg = lims.numel() - 1
+    if pars.dtype != dat.dtype or pars.numel() != ndet * nseg:
+        raise ValueError("pars must be (ndet, nseg) of dat's dtype")
+    return ndet, ndata, nseg
+
+
+def stripes_map2tod(dat: torch.Tensor, pars: torch.Tensor, lims: torch.Tensor, do_add: bool = True) -> None:
+    """dat[d, lims[s]:lims[s+1]] (+)= pars[d, s]  (mk_stripes_map2tod)."""
+    ndet, ndata, nseg = _stripes_args(dat, pars, lims)
+    check(lib().mk_stripes_map2tod(_p(dat), _p(pars), _p(lims), ndet, ndata, nseg, dtype_code(dat),
+                                   int(bool(do_add)), _stream()), "stripes_map2tod")
+
+
+def stripes_tod2map(pars: torch.Tensor, dat: torch.Tensor, lims: torch.Tensor, do_add: bool = True) -> None:
+    """pars[d, s] (+)= dat[d, lims[s]:lims[s+1]].sum()  (mk_stripes_tod2map)."""
+    ndet, ndata, nseg = _stripes_args(dat, pars, lims)
+    check(lib().mk_stripes_tod2map(_p(pars), _p(dat), _p(lims), ndet, ndata, nseg, dtype_code(dat),
+                                   int(bool(do_add)), _stream()), "stripes_tod2map")
+
+
+def _binned_args(dat, pars, vec):
+    _dev(dat, "dat"), _dev(pars, "pars"), _dev(vec, "vec")
+    if vec.dtype != torch.float64:
+        raise TypeError("vec must be float64")
+    ndet, ndata = _nd(dat)
+    if vec.numel() not in (ndata, ndet * ndata):
+        raise ValueError("vec must have ndata or ndet*ndata entries")
+    if pars.dtype != dat.dtype or pars.dim() != 2 or pars.shape[0] != ndet:
+        raise ValueError("pars must be (ndet, nbin) of dat's dtype")
+    return ndet, ndata, pars.shape[1], int(vec.numel() == ndet * ndata and ndet > 1)
+
+
+def binned_map2tod(dat: torch.Tensor, pars: torch.Tensor, vec: torch.Tensor, lims, do_add: bool = True) -> None:
+    """dat[d, t] (+)= pars[d, bin(vec[t])]  (mk_binned_map2tod)."""
+    ndet, ndata, nbin, per_det = _binned_args(dat, pars, vec)
+    check(lib().mk_binned_map2tod(_p(dat), _p(pars), _p(vec), ndet, ndata, nbin, float(lims[0]), float(lims[1]),
+                                  per_det, dtype_code(dat), int(bool(do_add)), _stream()), "binned_map2tod")
+
+
+def binned_tod2map(pars: torch.Tensor, dat: torch.Tensor, vec: torch.Tensor, lims, do_add: bool = True) -> None:
+    """pars[d, b] (+)= sum of dat[d, t] with bin(vec[t]) = b  (mk_binned_tod2map)."""
+    ndet, ndata, nbin, per_det = _binned_args(dat, pars, vec)
+    check(lib().mk_binned_tod2map(_p(pars), _p(dat), _p(vec), ndet, ndata, nbin, float(lims[0]), float(lims[1]),
+                                  per_det, dtype_code(dat), int(bool(do_add)), _stream()), "binned_tod2map")
+
+
 def tod2map_rows(map: torch.Tensor, ipix: torch.Tensor, w: Optional[torch.Tensor] = None) -> None:
     """map.flat[ipix[d, t]] += w[d] (1 when w is None) -- hit / weight maps."""
     _dev(map, "map"), _dev(ipix, "ipix")

@@ -56,6 +56,23 @@ class Tod:
             raise ValueError("This TOD has no stored data. Populare tod.info['dat_calib']")
         return dat
 
+    def get_tvec(self):
+        """The time vector, info['ctime'] (core.py:262-271)."""
+        return self.info["ctime"]
+
+    def prior_from_skymap(self, skymap):
+        """A CutsCompact prior on the samples where ``skymap`` projects to a
+        non-zero value, weighted 1 / value^2 (core.py:750-780)."""
+        from .tsmodels import CutsCompact
+        tmp = self.get_empty(True)
+        skymap.map2tod(self, tmp)
+        prior = CutsCompact(self)
+        prior.cuts_from_array(tmp == 0)
+        prior.get_imap()
+        prior.tod2map(self, tmp)
+        prior.map = 1.0 / prior.map ** 2
+        return prior
+
     def get_radec(self):
         return self.info["dx"], self.info["dy"]
 

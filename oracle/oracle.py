@@ -31,6 +31,13 @@ reference file:line it follows (paths relative to the minkasi project root):
   minkasi/mapmaking/map2tod.py:57-122, tod2map.py:164-215)
 * ``pol_invert`` / ``pol_precon_mul`` -> PolMap.invert / PolMap.__mul__,
   minkasi/maps/polmap.py:300-384,624-684
+* ``cuts_gather`` / ``cuts_scatter`` -> tod2cuts / cuts2tod, minkasi/lib/minkasi.c:260-284
+* ``stripe_edges`` / ``stripes_map2tod`` / ``stripes_tod2map`` -> split_partitioned_vec,
+  tsStripes (minkasi/mapmaking/timestream.py:442-531), map2tod_destriped
+  (minkasi/mapmaking/map2tod.py:156-190); tod2map_destriped
+  (minkasi/mapmaking/tod2map.py:242-269) as the transpose of map2tod_destriped
+* ``binned_map2tod`` / ``binned_tod2map`` -> map2tod_binned_det / tod2map_binned_det
+  (map2tod.py:195-253, tod2map.py:272-340), the latter as a true histogram
 * ``car_wcs`` / ``pix_wcs_car``  -> get_wcs (minkasi/maps/utils.py:13-67) and
   SkyMap.pix_from_radec (minkasi/maps/skymap.py:457-490); astropy's CAR
   world->pixel is restated from the published FITS equations (Calabretta &
@@ -483,3 +490,94 @@ def pol_precon_mul(precon: np.ndarray, map: np.ndarray, poltag: str) -> np.ndarr
         out[..., 1] = a[..., 1] * x[..., 0] + a[..., 3] * x[..., 1] + a[..., 4] * x[..., 2]
         out[..., 2] = a[..., 2] * x[..., 0] + a[..., 4] * x[..., 1] + a[..., 5] * x[..., 2]
     return out
+
+
+# ---------------------------------------------------------------- cuts and timestream models
+def cuts_gather(vec: np.ndarray, dat: np.ndarray, imap: np.ndarray, do_add: bool = True) -> None:
+    """tod2cuts (minkasi.c:260-268)."""
+    v = np.ravel(dat)[imap]
+    if do_add:
+        vec += v
+    else:
+        vec[:] = v
+
+
+def cuts_scatter(dat: np.ndarray, vec: np.ndarray, imap: np.ndarray, do_add: bool = True) -> None:
+    """cuts2tod (minkasi.c:271-284), serial order."""
+    flat = dat.reshape(-1)
+    if do_add:
+        np.add.at(flat, imap, vec)
+    else:
+        flat[imap] = vec
+
+
+def stripe_edges(ndata: int, tvec: np.ndarray, seg_len: int = 500, tthresh: float = 10) -> np.ndarray:
+    """tsStripes segment edges: partition_interval / split_partitioned_vec
+    (timestream.py:442-483) at the time gaps > tthresh * median dt."""
+    def part(start, stop):
+        if (stop - start) <= seg_len:
+            return np.asarray([start, stop], dtype="int")
+        nseg = (stop - start) // seg_len
+        sl = (stop - start) // nseg
+        nextra = (stop - start) - sl * nseg
+        inds = np.arange(start, stop + 1, sl)
+        if nextra > 0:
+            vec = np.zeros(len(inds), dtype="int")
+            vec[1:nextra + 1] = 1
+            inds = inds + np.cumsum(vec)
+        return inds
+
+    dt = np.median(np.diff(tvec))
+    breaks = list(np.where(np.abs(np.diff(tvec)) > tthresh * dt)[0])
+    if breaks and breaks[0] == 0:
+        breaks = breaks[1:]
+    if breaks and breaks[-1] == ndata:
+        breaks = breaks[:-1]
+    if not breaks:
+        return part(0, ndata)
+    edges = np.hstack([0, breaks, ndata])
+    segs = [part(edges[i], edges[i + 1])[:-1] if i < len(edges) - 2 else part(edges[i], edges[i + 1])
+            for i in range(len(edges) - 1)]
+    return np.hstack(segs)
+
+
+def stripes_map2tod(dat: np.ndarray, pars: np.ndarray, lims: np.ndarray, do_add: bool = True) -> None:
+    """map2tod_destriped (map2tod.py:156-190)."""
+    for s in range(len(lims) - 1):
+        if do_add:
+            dat[:, lims[s]:lims[s + 1]] += pars[:, s][:, None]
+        else:
+            dat[:, lims[s]:lims[s + 1]] = pars[:, s][:, None]
+
+
+def stripes_tod2map(pars: np.ndarray, dat: np.ndarray, lims: np.ndarray, do_add: bool = True) -> None:
+    """Segment sums: the transpose of map2tod_destriped (the intent of
+    tod2map_destriped, tod2map.py:242-269)."""
+    if not do_add:
+        pars[:] = 0
+    for s in range(len(lims) - 1):
+        pars[:, s] += np.sum(dat[:, lims[s]:lims[s + 1]], axis=1)
+
+
+def _bins(vec: np.ndarray, lims, nbin: int) -> np.ndarray:
+    fac = nbin / (lims[1] - lims[0])
+    return np.asarray((vec - lims[0]) * fac, dtype="int64")
+
+
+def binned_map2tod(dat: np.ndarray, pars: np.ndarray, vec: np.ndarray, lims, nbin: int,
+                   do_add: bool = True) -> None:
+    """map2tod_binned_det (map2tod.py:195-253), vec shared by the detectors."""
+    inds = _bins(vec, lims, nbin)
+    if not do_add:
+        dat[:] = 0
+    dat += pars[:, inds]
+
+
+def binned_tod2map(pars: np.ndarray, dat: np.ndarray, vec: np.ndarray, lims, nbin: int,
+                   do_add: bool = True) -> None:
+    """Histogram of dat per detector: the transpose of binned_map2tod."""
+    inds = _bins(vec, lims, nbin)
+    if not do_add:
+        pars[:] = 0
+    for d in range(dat.shape[0]):
+        np.add.at(pars[d], inds, dat[d])

@@ -19,6 +19,8 @@ Reference entry points exercised (paths in the minkasi project):
   truncate_tod / find_good_fft_lens  minkasi/tods/processing.py:648-682, minkasi/tools/py_fft.py:364-395
   SkyMapCar.pix_from_radec  minkasi/maps/skymap.py:958-984
   radec2pix_car      minkasi/maps/utils.py:178-216 (its pure-Python path: numba is absent)
+  CutsCompact / tsStripes / tsBinnedAz  minkasi/tods/cuts.py:201-490,
+                     minkasi/mapmaking/timestream.py:442-560, map2tod.py:156-253, tod2map.py:242-340
   polmap2tod / tod2polmap / PolMap  minkasi/mapmaking/map2tod.py:57-122, tod2map.py:164-215,
                      minkasi/maps/polmap.py:273-684 -> minkasi/lib/minkasi.c:146-245
 
@@ -276,6 +278,78 @@ def case_pol():
     save("pol.npz", **out)
 
 
+def case_tsmodel():
+    """CutsCompact (tod2cuts / cuts2tod through the reference's C), the
+    destriper (tsStripes segment edges, map2tod_destriped,
+    set_prior_from_corr, apply_prior) and the binned model
+    (map2tod_binned_det, tod2map_binned_det)."""
+    from minkasi.mapmaking import map2tod as m2t
+    from minkasi.mapmaking import tod2map as t2m
+    from minkasi.mapmaking.timestream import tsStripes
+    from minkasi.tods.cuts import CutsCompact
+    rng = np.random.default_rng(31)
+    ndet, ndata = 5, 3000
+    dat = rng.standard_normal((ndet, ndata))
+    out = {"dat": dat}
+    # cuts: a mask with short runs of False per detector
+    mask = rng.random((ndet, ndata)) > 0.02
+    mask = mask & np.roll(mask, 1, axis=1) & np.roll(mask, 2, axis=1)
+    tod = Tod({"dat_calib": dat.copy(), "fname": "t0"})
+    cc = quiet(CutsCompact, tod)
+    cc.cuts_from_array(mask)
+    quiet(cc.get_imap)
+    cc.tod2map(tod, dat)
+    out.update(cut_mask=mask, cut_imap=cc.imap, cut_map=cc.map.copy())
+    cc.map[:] = rng.standard_normal(cc.map.size)
+    out["cut_vals"] = cc.map.copy()
+    for add in (0, 1):
+        d = dat.copy()
+        cc.map2tod(tod, d, do_add=bool(add))
+        out[f"cut_m2t_{add}"] = d
+    # stripes: a time vector with two gaps
+    ctime = np.arange(ndata) * 0.01
+    ctime[1100:] += 5.0
+    ctime[2400:] += 3.0
+    tod_s = Tod({"dat_calib": dat.copy(), "fname": "t0", "ctime": ctime})
+    st = tsStripes(tod_s, seg_len=170)
+    pars = rng.standard_normal(st.params.shape)
+    out.update(ctime=ctime, stripe_inds=np.asarray(st.inds), stripe_pars=pars)
+    for add in (0, 1):
+        d = dat.copy()
+        m2t.map2tod_destriped(d, pars, st.inds, do_add=bool(add))
+        out[f"stripe_m2t_{add}"] = d
+    # tod2map_destriped raises on numpy's path (an (ndet, 1) operand added
+    # into an (ndet,) slice), so it yields no fixture; its transpose
+    # relation with map2tod_destriped is what the tests check
+    corr = np.abs(rng.standard_normal((ndet, st.nseg + 7))) + 0.1
+    st.set_prior_from_corr(corr, thresh=0.5)
+    out.update(stripe_corr=corr, stripe_prior=st.params.copy())
+    x = tsStripes(tod_s, seg_len=170)
+    x.params = rng.standard_normal(x.params.shape)
+    ax = tsStripes(tod_s, seg_len=170)
+    ax.params = rng.standard_normal(ax.params.shape)
+    out.update(stripe_x=x.params.copy(), stripe_ax0=ax.params.copy())
+    st.apply_prior(x, ax)
+    out["stripe_ax"] = ax.params
+    # binned: azimuth shared by the detectors
+    az = np.mod(0.3 + np.cumsum(np.abs(rng.standard_normal(ndata))) * 0.01, 2 * np.pi)
+    nbin = 37
+    bpars = rng.standard_normal((ndet, nbin))
+    out.update(az=az, bin_pars=bpars, nbin=nbin)
+    for add in (0, 1):
+        d = dat.copy()
+        m2t.map2tod_binned_det(d, bpars, az, (0, 2 * np.pi), nbin, do_add=bool(add))
+        out[f"bin_m2t_{add}"] = d
+    # the reference's tod2map_binned_det; it agrees with a histogram on the
+    # bins that a single sample hits
+    az1 = np.sort(rng.uniform(0, 2 * np.pi, size=ndata))
+    nbin1 = 100000
+    p1 = np.zeros((ndet, nbin1))
+    t2m.tod2map_binned_det(dat, p1, az1, (0, 2 * np.pi), nbin1, do_add=True)
+    out.update(az_unique=az1, nbin_unique=nbin1, bin_t2m_unique=p1)
+    save("tsmodel.npz", **out)
+
+
 CASES = {"proj": case_proj, "dct": case_dct, "noise": case_noise, "solve": case_solve}
 
 if __name__ == "__main__":
@@ -291,3 +365,5 @@ if __name__ == "__main__":
         case_pointing()
     if not want or "pol" in want:
         case_pol()
+    if not want or "tsmodel" in want:
+        case_tsmodel()

@@ -136,3 +136,47 @@ def test_pol_projections_invert_mul_match_reference(gold):
         mul = oracle.pol_precon_mul(g[f"inv_{tag}"], g[f"mulx_{tag}"], tag + "_PRECON")
         assert np.allclose(mul, g[f"mul_{tag}"], rtol=1e-12, atol=0)
         assert (h != 0).any()
+
+
+def test_cuts_stripes_binned_match_reference(gold):
+    g = gold("tsmodel.npz")
+    dat = g["dat"]
+    # cuts: imap from the mask, gather and scatter through the reference's C
+    parts = []
+    for d in range(dat.shape[0]):
+        edges = np.where(np.diff(np.r_[True, g["cut_mask"][d], True]))[0]
+        for a, b in zip(edges[::2], edges[1::2]):
+            parts.append(np.arange(d * dat.shape[1] + a, d * dat.shape[1] + b))
+    imap = np.concatenate(parts)
+    assert np.array_equal(imap, g["cut_imap"])
+    v = np.zeros(imap.size)
+    oracle.cuts_gather(v, dat, imap)
+    assert np.array_equal(v, g["cut_map"])
+    for add in (0, 1):
+        d = dat.copy()
+        oracle.cuts_scatter(d, g["cut_vals"], imap, bool(add))
+        assert np.array_equal(d, g[f"cut_m2t_{add}"])
+    # stripes: segment edges, map2tod, and tod2map as its transpose
+    lims = oracle.stripe_edges(dat.shape[1], g["ctime"], seg_len=170)
+    assert np.array_equal(lims, g["stripe_inds"])
+    for add in (0, 1):
+        d = dat.copy()
+        oracle.stripes_map2tod(d, g["stripe_pars"], lims, bool(add))
+        assert np.array_equal(d, g[f"stripe_m2t_{add}"])
+    p = np.zeros_like(g["stripe_pars"])
+    oracle.stripes_tod2map(p, dat, lims)
+    m = np.zeros_like(dat)
+    oracle.stripes_map2tod(m, g["stripe_pars"], lims, False)
+    assert abs(np.sum(m * dat) - np.sum(p * g["stripe_pars"])) < 1e-10 * abs(np.sum(m * dat))
+    # binned: map2tod, and the histogram where the reference's buffered add agrees
+    for add in (0, 1):
+        d = dat.copy()
+        oracle.binned_map2tod(d, g["bin_pars"], g["az"], (0, 2 * np.pi), int(g["nbin"]), bool(add))
+        assert np.array_equal(d, g[f"bin_m2t_{add}"])
+    nb = int(g["nbin_unique"])
+    p1 = np.zeros((dat.shape[0], nb))
+    oracle.binned_tod2map(p1, dat, g["az_unique"], (0, 2 * np.pi), nb)
+    inds = np.asarray(g["az_unique"] * (nb / (2 * np.pi)), dtype="int64")
+    once = np.bincount(inds, minlength=nb) == 1
+    assert np.array_equal(p1[:, once], g["bin_t2m_unique"][:, once])
+    assert (~once[inds]).any()  # some bins repeat: there the reference keeps one sample
