@@ -211,12 +211,17 @@ class SkyMap:
         """Sum the map over ranks (skymap.py:742-783); a no-op on one rank."""
         parallel.allreduce_(self.map)
 
-    def write(self, fname: str = "map.npy"):
-        """Save the map.  FITS needs astropy (not a dependency here): the map
-        is written as .npy next to the requested name."""
-        root, ext = os.path.splitext(os.path.abspath(fname))
-        os.makedirs(os.path.dirname(root), exist_ok=True)
-        np.save(root + ".npy", self.map.detach().cpu().numpy())
+    def write(self, fname: str = "map.fits"):
+        """Write the map as a FITS image, transposed, with its CAR WCS in the
+        header (skymap.py:705-722), through minkasi_gb300.fits; a name ending
+        in .npy saves the untransposed array with numpy instead."""
+        from . import fits
+        if fname.endswith(".npy"):
+            os.makedirs(os.path.dirname(os.path.abspath(fname)), exist_ok=True)
+            np.save(fname, self.map.detach().cpu().numpy())
+            return
+        cards = fits.car_header(self.wcs) if self.wcs is not None else []
+        fits.write_image(fname, self.map.detach().cpu().numpy().T, cards)
 
     def to_numpy(self) -> np.ndarray:
         return self.map.detach().cpu().numpy()

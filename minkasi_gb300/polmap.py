@@ -9,6 +9,7 @@ on the GPU from ``tod.info['twogamma_saved']`` and cached with the TOD.
 """
 from __future__ import annotations
 
+import os
 from typing import List, Optional
 
 import numpy as np
@@ -146,6 +147,20 @@ class PolMap(SkyMap):
             t[inds, 0, 0] = 1.0 / vec
             for (i, j), k in (((0, 0), 0), ((0, 1), 1), ((0, 2), 2), ((1, 1), 3), ((1, 2), 4), ((2, 2), 5)):
                 m[:, :, k] = t[:, i, j].reshape(self.nx, self.ny)
+
+    def write(self, fname: str = "map.fits"):
+        """One FITS image per Stokes component, <name>_<pol>.fits, each
+        transposed, with the map's CAR WCS (polmap.py:585-622)."""
+        if self.npol == 1:
+            return SkyMap.write(self, fname)
+        from . import fits
+        fname = os.path.abspath(fname)
+        ind = fname.rfind(".")
+        head, tail = (fname[:ind], fname[ind:]) if ind > 0 and fname[ind + 1:] == "fits" else (fname, ".fits")
+        cards = fits.car_header(self.wcs) if self.wcs is not None else []
+        m = self.map.detach().cpu().numpy()
+        for i, pol in enumerate(self.pols):
+            fits.write_image(head + "_" + pol + tail, np.ascontiguousarray(m[:, :, i].T), cards)
 
     def r_th_maps(self):
         """Radius and angle of every pixel about the map centre (polmap.py:547-566)."""

@@ -183,3 +183,23 @@ def test_tod2map_from_pinned_host_through_api(mk, gold):
         st.tod2map(flat, host, ip)
     want = g["map"].ravel() + 3 * (g["tod2map_omp"].ravel() - g["map"].ravel())
     assert rel(flat.cpu().numpy(), want) < 1e-12
+
+
+def test_skymap_and_polmap_write_fits(mk, tmp_path):
+    """SkyMap.write: the transposed map and its CAR WCS in a FITS image;
+    PolMap.write: one image per Stokes component."""
+    from minkasi_gb300 import fits
+    arcsec = np.pi / 180 / 3600
+    lims = [3.5 - 0.002, 3.5 + 0.002, 0.3 - 0.001, 0.3 + 0.001]
+    m = mk.SkyMap(lims, 2 * arcsec)
+    m.map.copy_(torch.randn(m.map.shape, dtype=torch.float64))
+    m.write(str(tmp_path / "sky.fits"))
+    data, hdr = fits.read_image(str(tmp_path / "sky.fits"))
+    assert np.array_equal(data, m.map.cpu().numpy().T)
+    assert [hdr[k] for k in ("CRVAL1", "CRVAL2", "CRPIX1", "CRPIX2", "CDELT1", "CDELT2")] == list(m.wcs)
+    p = mk.PolMap(lims, 2 * arcsec, "IQU")
+    p.map.copy_(torch.randn(p.map.shape, dtype=torch.float64))
+    p.write(str(tmp_path / "pol.fits"))
+    for i, pol in enumerate("IQU"):
+        d, _ = fits.read_image(str(tmp_path / f"pol_{pol}.fits"))
+        assert np.array_equal(d, p.map[:, :, i].cpu().numpy().T)

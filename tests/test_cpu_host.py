@@ -80,3 +80,22 @@ def test_partition_balances_uneven_tods():
     loads = [sum(costs[i] for i in p) for p in parts]
     assert max(loads) / min(loads) < 1.6
     assert parallel.partition(costs, 2) == parts  # deterministic
+
+
+def test_fits_image_roundtrip(tmp_path):
+    """The FITS writer used by SkyMap.write / PolMap.write: 2880-byte blocks,
+    80-character cards, big-endian FP64 data that reads back exactly."""
+    from minkasi_gb300 import fits
+    rng = np.random.default_rng(0)
+    data = rng.standard_normal((7, 13))
+    w6 = [200.5, 17.75, 1.0, 1.0, -2.0 / 3600, 2.0 / 3600]
+    path = tmp_path / "sub" / "m.fits"
+    fits.write_image(str(path), data, fits.car_header(w6))
+    raw = path.read_bytes()
+    assert len(raw) % 2880 == 0
+    assert raw[:80].decode() == "SIMPLE  =                    T / conforms to FITS standard".ljust(80)
+    back, hdr = fits.read_image(str(path))
+    assert np.array_equal(back, data)
+    assert (hdr["NAXIS1"], hdr["NAXIS2"]) == (13, 7)
+    assert hdr["CTYPE1"] == "RA---CAR" and hdr["CTYPE2"] == "DEC--CAR"
+    assert [hdr[k] for k in ("CRVAL1", "CRVAL2", "CRPIX1", "CRPIX2", "CDELT1", "CDELT2")] == w6
