@@ -6,131 +6,173 @@
 //   conv_adj : X[b,ci,q]  = sum_co sum_d W[co,ci,d] Y[b,co,q-d]       (L^T y)
 //   conv_wgrad: G[co,ci,d] = sum_b sum_p H[b,co,p] X[b,ci,p+d]
 // with zero padding (pixels outside the map are 0).  Layout: [B][C][H][W],
-// FP32, at most 16 channels.  A CTA owns a 16x16 pixel tile of one map and
-// stages the input tile plus a 1-pixel halo for every channel in shared
-// memory; the weights (<= 16*16*9 floats) sit in shared memory and are read
-// as warp-wide broadcasts.  conv_wgrad writes one partial per CTA and a
+// FP32, at most 16 channels.  Each CTA stages its input tile plus a 1-pixel
+// halo for every channel in shared memory, and the weights (<= 16*16*9
+// floats) are read as warp-wide broadcasts; threads are register-blocked
+// (see k_conv and k_conv_wgrad).  conv_wgrad writes one partial per CTA and a
 // second kernel sums the partials in a fixed order (reproducible gradients).
 #include "mk_common.cuh"
 
 namespace {
 
 constexpr int CMAX = 16;
-constexpr int T = 16;            // tile edge
-constexpr int TH = T + 2;        // with halo
 constexpr int NW = CMAX * CMAX * 9;
 
 __device__ __forceinline__ float ld_pad(const float *__restrict__ x, int H, int W, int y, int xx) {
   return (y >= 0 && y < H && xx >= 0 && xx < W) ? x[(int64_t)y * W + xx] : 0.f;
 }
 
-__global__ void __launch_bounds__(256) k_conv_fwd(const float *__restrict__ X, const float *__restrict__ Wt,
-                                                  float *__restrict__ Y, int Cin, int Cout, int H, int W) {
-  __shared__ float sx[CMAX][TH][TH];
-  __shared__ float sw[NW];
-  const int b = blockIdx.z;
-  const int y0 = blockIdx.y * T, x0 = blockIdx.x * T;
-  const int tid = threadIdx.x;
-  for (int i = tid; i < Cout * Cin * 9; i += 256) sw[i] = Wt[i];
-  const float *xb = X + (int64_t)b * Cin * H * W;
-  for (int i = tid; i < Cin * TH * TH; i += 256) {
-    int c = i / (TH * TH), r = (i / TH) % TH, q = i % TH;
-    sx[c][r][q] = ld_pad(xb + (int64_t)c * H * W, H, W, y0 + r - 1, x0 + q - 1);
+// ---- fwd / adjoint: one kernel, register-blocked ------------------------
+// A CTA owns a 32x32 tile of output pixels; each thread a 1x4 strip of it for
+// every output channel (4 x 16 accumulators), so each shared-memory weight
+// load feeds 4 FMAs.  The input tile plus a 1-pixel halo is staged in shared
+// memory for every input channel.  The adjoint is the same loop with input
+// and output channels swapped and the taps flipped:
+//   adj(o = ci, i = co, d) = W[co][ci][8 - d].
+constexpr int TX = 32, TY = 32, PX = 4;
+constexpr int SXW = TX + 2, SXH = TY + 2;
+
+template <bool ADJ, int NOUT>
+__global__ void __launch_bounds__(256) k_conv(const float *__restrict__ In, const float *__restrict__ Wt,
+                                              float *__restrict__ Out, int Cin, int Cout, int H, int W) {
+  extern __shared__ float smem[];
+  const int nin = ADJ ? Cout : Cin, nout = ADJ ? Cin : Cout;
+  float *sx = smem;
+  float *sw = smem + nin * SXH * SXW;
+  const int b = blockIdx.z, y0 = blockIdx.y * TY, x0 = blockIdx.x * TX, tid = threadIdx.x;
+  for (int i = tid; i < nout * nin * 9; i += 256) {
+    const int o = i / (nin * 9), ii = (i / 9) % nin, d = i % 9;
+    sw[i] = ADJ ? Wt[(ii * Cin + o) * 9 + (8 - d)] : Wt[(o * Cin + ii) * 9 + d];
+  }
+  const float *ib = In + (int64_t)b * nin * H * W;
+  for (int i = tid; i < nin * SXH * SXW; i += 256) {
+    const int c = i / (SXH * SXW), r = (i / SXW) % SXH, q = i % SXW;
+    sx[i] = ld_pad(ib + (int64_t)c * H * W, H, W, y0 + r - 1, x0 + q - 1);
   }
   __syncthreads();
-  const int ty = tid / T, tx = tid % T;
-  float acc[CMAX];
+  const int ty = tid / (TX / PX), tx = (tid % (TX / PX)) * PX;
+  float acc[PX][NOUT];
 #pragma unroll
-  for (int co = 0; co < CMAX; co++) acc[co] = 0.f;
-  for (int ci = 0; ci < Cin; ci++) {
+  for (int p = 0; p < PX; p++)
+#pragma unroll
+    for (int o = 0; o < NOUT; o++) acc[p][o] = 0.f;
+  for (int ci = 0; ci < nin; ci++) {
+    const float *sp = sx + ci * SXH * SXW + ty * SXW + tx;
+    float win[3][PX + 2];
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+      for (int c = 0; c < PX + 2; c++) win[r][c] = sp[r * SXW + c];
+    const float *wc = sw + ci * 9;
 #pragma unroll
     for (int d = 0; d < 9; d++) {
-      const float v = sx[ci][ty + d / 3][tx + d % 3];
 #pragma unroll
-      for (int co = 0; co < CMAX; co++)
-        if (co < Cout) acc[co] = fmaf(sw[(co * Cin + ci) * 9 + d], v, acc[co]);
+      for (int o = 0; o < NOUT; o++) {
+        if (o < nout) {
+          const float wv = wc[o * nin * 9 + d];
+#pragma unroll
+          for (int p = 0; p < PX; p++) acc[p][o] = fmaf(wv, win[d / 3][p + d % 3], acc[p][o]);
+        }
+      }
     }
   }
-  const int yy = y0 + ty, xx = x0 + tx;
-  if (yy < H && xx < W) {
-    float *yb = Y + (int64_t)b * Cout * H * W + (int64_t)yy * W + xx;
+  const int yy = y0 + ty;
+  if (yy >= H) return;
+  float *ob = Out + (int64_t)b * nout * H * W + (int64_t)yy * W;
 #pragma unroll
-    for (int co = 0; co < CMAX; co++)
-      if (co < Cout) yb[(int64_t)co * H * W] = acc[co];
+  for (int p = 0; p < PX; p++) {
+    const int xx = x0 + tx + p;
+    if (xx < W) {
+#pragma unroll
+      for (int o = 0; o < NOUT; o++)
+        if (o < nout) ob[(int64_t)o * H * W + xx] = acc[p][o];
+    }
   }
 }
 
-// adjoint: the tap d of output pixel p reads input pixel p+d, so input pixel
-// q receives from output pixels q-d.
-__global__ void __launch_bounds__(256) k_conv_adj(const float *__restrict__ Yin, const float *__restrict__ Wt,
-                                                  float *__restrict__ Xout, int Cin, int Cout, int H, int W) {
-  __shared__ float sy[CMAX][TH][TH];
-  __shared__ float sw[NW];
-  const int b = blockIdx.z;
-  const int y0 = blockIdx.y * T, x0 = blockIdx.x * T;
-  const int tid = threadIdx.x;
-  for (int i = tid; i < Cout * Cin * 9; i += 256) sw[i] = Wt[i];
-  const float *yb = Yin + (int64_t)b * Cout * H * W;
-  for (int i = tid; i < Cout * TH * TH; i += 256) {
-    int c = i / (TH * TH), r = (i / TH) % TH, q = i % TH;
-    sy[c][r][q] = ld_pad(yb + (int64_t)c * H * W, H, W, y0 + r - 1, x0 + q - 1);
-  }
-  __syncthreads();
-  const int ty = tid / T, tx = tid % T;
-  float acc[CMAX];
-#pragma unroll
-  for (int ci = 0; ci < CMAX; ci++) acc[ci] = 0.f;
-  for (int co = 0; co < Cout; co++) {
-#pragma unroll
-    for (int d = 0; d < 9; d++) {
-      // q - d with d = (dy-1, dx-1): tile index (ty + 1 - (dy-1), tx + 1 - (dx-1))
-      const float v = sy[co][ty + 2 - d / 3][tx + 2 - d % 3];
-#pragma unroll
-      for (int ci = 0; ci < CMAX; ci++)
-        if (ci < Cin) acc[ci] = fmaf(sw[(co * Cin + ci) * 9 + d], v, acc[ci]);
-    }
-  }
-  const int yy = y0 + ty, xx = x0 + tx;
-  if (yy < H && xx < W) {
-    float *xb = Xout + (int64_t)b * Cin * H * W + (int64_t)yy * W + xx;
-#pragma unroll
-    for (int ci = 0; ci < CMAX; ci++)
-      if (ci < Cin) xb[(int64_t)ci * H * W] = acc[ci];
-  }
-}
+size_t conv_smem(int nin, int nout) { return ((size_t)nin * SXH * SXW + (size_t)nout * nin * 9) * sizeof(float); }
 
-// one partial gradient per CTA: part[cta][co][ci][d]
+// ---- weight gradient -----------------------------------------------------
+// G[co][ci][d] = sum_p H[co, p] X[ci, p + d] over a 16x32 pixel tile per CTA.
+// Thread (rowgroup, co-group, ci) keeps 4 output channels x 9 taps in
+// registers and slides a 3x3 window of X along its 4 rows: per pixel 3 new X
+// values and 4 H values feed 36 FMAs.  Shared-memory planes are padded so
+// that the 16 input channels (and the 8 output channels) a warp reads at once
+// fall in distinct banks.  The 4 row groups are summed in a fixed order and
+// each CTA writes one partial; k_wgrad_reduce sums the partials in CTA order.
+constexpr int WTX = 32, WTY = 16;
+constexpr int XPL = (WTY + 2) * (WTX + 2) + 1;  // X plane stride (mod 32 = 5)
+constexpr int HPL = WTY * WTX + 1;              // H plane stride (mod 32 = 1)
+
 __global__ void __launch_bounds__(256) k_conv_wgrad(const float *__restrict__ X, const float *__restrict__ Hg,
                                                     float *__restrict__ part, int Cin, int Cout, int H, int W) {
-  __shared__ float sx[CMAX][TH][TH];
-  __shared__ float sh[CMAX][T][T];
-  const int b = blockIdx.z;
-  const int y0 = blockIdx.y * T, x0 = blockIdx.x * T;
-  const int tid = threadIdx.x;
+  extern __shared__ float smem[];
+  float *sx = smem;                 // [CMAX][XPL]
+  float *sh = smem + CMAX * XPL;    // [CMAX][HPL]
+  float *red = sh + CMAX * HPL;     // [4][NW]
+  const int b = blockIdx.z, y0 = blockIdx.y * WTY, x0 = blockIdx.x * WTX, tid = threadIdx.x;
   const float *xb = X + (int64_t)b * Cin * H * W;
   const float *hb = Hg + (int64_t)b * Cout * H * W;
-  for (int i = tid; i < Cin * TH * TH; i += 256) {
-    int c = i / (TH * TH), r = (i / TH) % TH, q = i % TH;
-    sx[c][r][q] = ld_pad(xb + (int64_t)c * H * W, H, W, y0 + r - 1, x0 + q - 1);
+  for (int i = tid; i < Cin * (WTY + 2) * (WTX + 2); i += 256) {
+    const int c = i / ((WTY + 2) * (WTX + 2)), rq = i % ((WTY + 2) * (WTX + 2));
+    const int r = rq / (WTX + 2), q = rq % (WTX + 2);
+    sx[c * XPL + rq] = ld_pad(xb + (int64_t)c * H * W, H, W, y0 + r - 1, x0 + q - 1);
   }
-  for (int i = tid; i < Cout * T * T; i += 256) {
-    int c = i / (T * T), r = (i / T) % T, q = i % T;
-    int yy = y0 + r, xx = x0 + q;
-    sh[c][r][q] = (yy < H && xx < W) ? hb[(int64_t)c * H * W + (int64_t)yy * W + xx] : 0.f;
+  for (int i = tid; i < Cout * WTY * WTX; i += 256) {
+    const int c = i / (WTY * WTX), rq = i % (WTY * WTX);
+    const int yy = y0 + rq / WTX, xx = x0 + rq % WTX;
+    sh[c * HPL + rq] = (yy < H && xx < W) ? hb[(int64_t)c * H * W + (int64_t)yy * W + xx] : 0.f;
   }
   __syncthreads();
-  const int nw = Cout * Cin * 9;
-  const int64_t cta = ((int64_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-  for (int w = tid; w < nw; w += 256) {
-    const int co = w / (Cin * 9), ci = (w / 9) % Cin, d = w % 9;
-    const int dy = d / 3, dx = d % 3;
-    float acc = 0.f;
-    for (int r = 0; r < T; r++)
+  const int ci = tid & 15, cg = (tid >> 4) & 3, rg = tid >> 6;  // 16 ci x 4 co-groups x 4 row groups
+  float acc[4][9];
 #pragma unroll
-      for (int q = 0; q < T; q++) acc = fmaf(sh[co][r][q], sx[ci][r + dy][q + dx], acc);
-    part[cta * nw + w] = acc;
+  for (int k = 0; k < 4; k++)
+#pragma unroll
+    for (int d = 0; d < 9; d++) acc[k][d] = 0.f;
+  if (ci < Cin && cg * 4 < Cout) {
+    for (int r = rg * (WTY / 4); r < (rg + 1) * (WTY / 4); r++) {
+      const float *xp = sx + ci * XPL + r * (WTX + 2);
+      float win[3][3];
+#pragma unroll
+      for (int dy = 0; dy < 3; dy++) {
+        win[dy][1] = xp[dy * (WTX + 2) + 0];
+        win[dy][2] = xp[dy * (WTX + 2) + 1];
+      }
+      for (int q = 0; q < WTX; q++) {
+#pragma unroll
+        for (int dy = 0; dy < 3; dy++) {
+          win[dy][0] = win[dy][1];
+          win[dy][1] = win[dy][2];
+          win[dy][2] = xp[dy * (WTX + 2) + q + 2];
+        }
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+          const int co = cg * 4 + k;
+          const float h = co < Cout ? sh[co * HPL + r * WTX + q] : 0.f;
+#pragma unroll
+          for (int d = 0; d < 9; d++) acc[k][d] = fmaf(h, win[d / 3][d % 3], acc[k][d]);
+        }
+      }
+    }
   }
+  const int nw = Cout * Cin * 9;
+  if (ci < Cin) {
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const int co = cg * 4 + k;
+      if (co < Cout)
+#pragma unroll
+        for (int d = 0; d < 9; d++) red[rg * NW + (co * Cin + ci) * 9 + d] = acc[k][d];
+    }
+  }
+  __syncthreads();
+  const int64_t cta = ((int64_t)blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+  for (int w = tid; w < nw; w += 256)
+    part[cta * nw + w] = (red[w] + red[NW + w]) + (red[2 * NW + w] + red[3 * NW + w]);
 }
+
+constexpr size_t WGRAD_SMEM = (size_t)(CMAX * XPL + CMAX * HPL + 4 * NW) * sizeof(float);
 
 // G[w] = sum over CTAs of part[cta][w], in CTA order (reproducible)
 __global__ void k_wgrad_reduce(const float *__restrict__ part, int64_t ncta, int nw, float *__restrict__ G) {
@@ -149,7 +191,29 @@ int conv_args(int B, int Cin, int Cout, int H, int W) {
   return MK_OK;
 }
 
-dim3 conv_grid(int B, int H, int W) { return dim3((W + T - 1) / T, (H + T - 1) / T, B); }
+dim3 wgrad_grid(int B, int H, int W) { return dim3((W + WTX - 1) / WTX, (H + WTY - 1) / WTY, B); }
+
+template <bool ADJ>
+int conv_launch(const float *in, const float *w, float *out, int B, int Cin, int Cout, int H, int W,
+                cudaStream_t st, const char *what) {
+  static bool attr[2][64] = {{false}};
+  int dev = 0;
+  MK_CUDA(cudaGetDevice(&dev));
+  const int nin = ADJ ? Cout : Cin, nout = ADJ ? Cin : Cout;
+  const size_t smem = conv_smem(nin, nout);
+  dim3 g((W + TX - 1) / TX, (H + TY - 1) / TY, B);
+  if (dev >= 0 && dev < 64 && !attr[ADJ][dev]) {
+    const int mx = (int)conv_smem(CMAX, CMAX);
+    MK_CUDA(cudaFuncSetAttribute(k_conv<ADJ, CMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    MK_CUDA(cudaFuncSetAttribute(k_conv<ADJ, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    attr[ADJ][dev] = true;
+  }
+  if (nout == 1)
+    k_conv<ADJ, 1><<<g, 256, smem, st>>>(in, w, out, Cin, Cout, H, W);
+  else
+    k_conv<ADJ, CMAX><<<g, 256, smem, st>>>(in, w, out, Cin, Cout, H, W);
+  return mk::launch_status(what);
+}
 
 }  // namespace
 
@@ -158,8 +222,7 @@ extern "C" int mk_conv3x3_fwd(const float *x, const float *w, float *y, int B, i
   int rc = conv_args(B, Cin, Cout, H, W);
   if (rc) return rc;
   MK_CHECK_ARG(x && w && y && x != y, "mk_conv3x3_fwd: bad pointers");
-  k_conv_fwd<<<conv_grid(B, H, W), 256, 0, mk::as_stream(stream)>>>(x, w, y, Cin, Cout, H, W);
-  return mk::launch_status("mk_conv3x3_fwd");
+  return conv_launch<false>(x, w, y, B, Cin, Cout, H, W, mk::as_stream(stream), "mk_conv3x3_fwd");
 }
 
 extern "C" int mk_conv3x3_adj(const float *y, const float *w, float *x, int B, int Cin, int Cout, int H,
@@ -167,13 +230,12 @@ extern "C" int mk_conv3x3_adj(const float *y, const float *w, float *x, int B, i
   int rc = conv_args(B, Cin, Cout, H, W);
   if (rc) return rc;
   MK_CHECK_ARG(x && w && y && x != y, "mk_conv3x3_adj: bad pointers");
-  k_conv_adj<<<conv_grid(B, H, W), 256, 0, mk::as_stream(stream)>>>(y, w, x, Cin, Cout, H, W);
-  return mk::launch_status("mk_conv3x3_adj");
+  return conv_launch<true>(y, w, x, B, Cin, Cout, H, W, mk::as_stream(stream), "mk_conv3x3_adj");
 }
 
 extern "C" size_t mk_conv3x3_wgrad_scratch_bytes(int B, int Cin, int Cout, int H, int W) {
-  size_t ncta = (size_t)((W + T - 1) / T) * ((H + T - 1) / T) * (size_t)(B > 0 ? B : 0);
-  return ncta * (size_t)Cin * Cout * 9 * sizeof(float);
+  const dim3 g = wgrad_grid(B > 0 ? B : 0, H > 0 ? H : 0, W > 0 ? W : 0);
+  return (size_t)g.x * g.y * g.z * (size_t)Cin * Cout * 9 * sizeof(float);
 }
 
 extern "C" int mk_conv3x3_wgrad(const float *x, const float *h, float *g, int B, int Cin, int Cout, int H,
@@ -183,11 +245,18 @@ extern "C" int mk_conv3x3_wgrad(const float *x, const float *h, float *g, int B,
   MK_CHECK_ARG(x && h && g && scratch, "mk_conv3x3_wgrad: null pointer");
   MK_CHECK_ARG(scratch_bytes >= mk_conv3x3_wgrad_scratch_bytes(B, Cin, Cout, H, W),
                "mk_conv3x3_wgrad: scratch too small");
+  static bool attr[64] = {false};
+  int dev = 0;
+  MK_CUDA(cudaGetDevice(&dev));
+  if (dev >= 0 && dev < 64 && !attr[dev]) {
+    MK_CUDA(cudaFuncSetAttribute(k_conv_wgrad, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)WGRAD_SMEM));
+    attr[dev] = true;
+  }
   cudaStream_t st = mk::as_stream(stream);
-  dim3 grid = conv_grid(B, H, W);
-  k_conv_wgrad<<<grid, 256, 0, st>>>(x, h, (float *)scratch, Cin, Cout, H, W);
-  int nw = Cin * Cout * 9;
-  int64_t ncta = (int64_t)grid.x * grid.y * grid.z;
+  const dim3 grid = wgrad_grid(B, H, W);
+  k_conv_wgrad<<<grid, 256, WGRAD_SMEM, st>>>(x, h, (float *)scratch, Cin, Cout, H, W);
+  const int nw = Cin * Cout * 9;
+  const int64_t ncta = (int64_t)grid.x * grid.y * grid.z;
   k_wgrad_reduce<<<(nw + 127) / 128, 128, 0, st>>>((const float *)scratch, ncta, nw, g);
   return mk::launch_status("mk_conv3x3_wgrad");
 }

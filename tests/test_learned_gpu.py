@@ -25,7 +25,8 @@ def rel(a, b):
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
 
 
-@pytest.mark.parametrize("cin,cout,H,W", [(1, 16, 33, 20), (16, 16, 16, 16), (16, 1, 40, 47), (5, 7, 3, 2)])
+@pytest.mark.parametrize("cin,cout,H,W", [(1, 16, 33, 20), (16, 16, 16, 16), (16, 1, 40, 47), (5, 7, 3, 2),
+                                         (16, 16, 70, 95), (16, 1, 65, 33)])
 def test_conv_kernels_match_oracle(L, cin, cout, H, W):
     rng = np.random.default_rng(cin * 100 + cout)
     x = rng.standard_normal((2, cin, H, W))
