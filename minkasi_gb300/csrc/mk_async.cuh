@@ -62,6 +62,19 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
       : "memory");
 }
 
+// 4-byte global -> shared asynchronous copy; when !valid nothing is read and
+// the destination is zero-filled (src must still be a mapped address)
+__device__ __forceinline__ void cp_async4_zfill(float *dst, const float *src, bool valid) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(dst)), "l"(src),
+               "r"(valid ? 4 : 0)
+               : "memory");
+}
+
+// waits for all of this thread's cp.async copies
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
 // orders this thread's earlier generic-proxy shared-memory accesses before
 // its later async-proxy ones (a bulk copy refilling a consumed stage)
 __device__ __forceinline__ void fence_proxy_async_smem() {

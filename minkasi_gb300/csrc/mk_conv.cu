@@ -11,6 +11,7 @@
 // floats) are read as warp-wide broadcasts; threads are register-blocked
 // (see k_conv and k_conv_wgrad).  conv_wgrad writes one partial per CTA and a
 // second kernel sums the partials in a fixed order (reproducible gradients).
+#include "mk_async.cuh"
 #include "mk_common.cuh"
 
 namespace {
@@ -23,34 +24,52 @@ __device__ __forceinline__ float ld_pad(const float *__restrict__ x, int H, int 
 }
 
 // ---- fwd / adjoint: one kernel, register-blocked ------------------------
-// A CTA owns a 32x32 tile of output pixels; each thread a 1x4 strip of it for
-// every output channel (4 x 16 accumulators), so each shared-memory weight
-// load feeds 4 FMAs.  The input tile plus a 1-pixel halo is staged in shared
-// memory for every input channel.  The adjoint is the same loop with input
-// and output channels swapped and the taps flipped:
+// A CTA owns a TXT x TYT tile of output pixels; each thread a 1x4 strip of it
+// for every output channel (4 x NOUT accumulators), so each shared-memory
+// weight load feeds 4 FMAs.  The input tile plus a 1-pixel halo is staged in
+// shared memory for every input channel with asynchronous 4-byte copies
+// (zero-filled outside the map), all in flight at once.  The adjoint is the
+// same loop with input and output channels swapped and the taps flipped:
 //   adj(o = ci, i = co, d) = W[co][ci][8 - d].
-constexpr int TX = 32, TY = 32, PX = 4;
-constexpr int SXW = TX + 2, SXH = TY + 2;
+// Tiles of 32 x 32 (256 threads) serve large maps; 16 x 16 (64 threads) keep
+// every SM busy on small ones.
+constexpr int PX = 4;
 
-template <bool ADJ, int NOUT>
-__global__ void __launch_bounds__(256) k_conv(const float *__restrict__ In, const float *__restrict__ Wt,
-                                              float *__restrict__ Out, int Cin, int Cout, int H, int W) {
+template <int TXT, int TYT>
+struct Tile {
+  static constexpr int SXW = TXT + 2, SXH = TYT + 2, NT = (TXT / PX) * TYT;
+};
+
+template <int TXT, int TYT>
+size_t conv_smem(int nin, int nout) {
+  return ((size_t)nin * Tile<TXT, TYT>::SXH * Tile<TXT, TYT>::SXW + (size_t)nout * nin * 9) * sizeof(float);
+}
+
+template <bool ADJ, int NOUT, int TXT, int TYT>
+__global__ void __launch_bounds__(Tile<TXT, TYT>::NT) k_conv(const float *__restrict__ In,
+                                                             const float *__restrict__ Wt,
+                                                             float *__restrict__ Out, int Cin, int Cout, int H,
+                                                             int W) {
+  constexpr int SXW = Tile<TXT, TYT>::SXW, SXH = Tile<TXT, TYT>::SXH, NT = Tile<TXT, TYT>::NT;
   extern __shared__ float smem[];
   const int nin = ADJ ? Cout : Cin, nout = ADJ ? Cin : Cout;
   float *sx = smem;
   float *sw = smem + nin * SXH * SXW;
-  const int b = blockIdx.z, y0 = blockIdx.y * TY, x0 = blockIdx.x * TX, tid = threadIdx.x;
-  for (int i = tid; i < nout * nin * 9; i += 256) {
+  const int b = blockIdx.z, y0 = blockIdx.y * TYT, x0 = blockIdx.x * TXT, tid = threadIdx.x;
+  const float *ib = In + (int64_t)b * nin * H * W;
+  for (int i = tid; i < nin * SXH * SXW; i += NT) {
+    const int c = i / (SXH * SXW), r = (i / SXW) % SXH, q = i % SXW;
+    const int yy = y0 + r - 1, xx = x0 + q - 1;
+    const bool ok = yy >= 0 && yy < H && xx >= 0 && xx < W;
+    mk::cp_async4_zfill(sx + i, ok ? ib + (int64_t)c * H * W + (int64_t)yy * W + xx : ib, ok);
+  }
+  for (int i = tid; i < nout * nin * 9; i += NT) {
     const int o = i / (nin * 9), ii = (i / 9) % nin, d = i % 9;
     sw[i] = ADJ ? Wt[(ii * Cin + o) * 9 + (8 - d)] : Wt[(o * Cin + ii) * 9 + d];
   }
-  const float *ib = In + (int64_t)b * nin * H * W;
-  for (int i = tid; i < nin * SXH * SXW; i += 256) {
-    const int c = i / (SXH * SXW), r = (i / SXW) % SXH, q = i % SXW;
-    sx[i] = ld_pad(ib + (int64_t)c * H * W, H, W, y0 + r - 1, x0 + q - 1);
-  }
+  mk::cp_async_wait_all();
   __syncthreads();
-  const int ty = tid / (TX / PX), tx = (tid % (TX / PX)) * PX;
+  const int ty = tid / (TXT / PX), tx = (tid % (TXT / PX)) * PX;
   float acc[PX][NOUT];
 #pragma unroll
   for (int p = 0; p < PX; p++)
@@ -90,8 +109,6 @@ __global__ void __launch_bounds__(256) k_conv(const float *__restrict__ In, cons
   }
 }
 
-size_t conv_smem(int nin, int nout) { return ((size_t)nin * SXH * SXW + (size_t)nout * nin * 9) * sizeof(float); }
-
 // ---- weight gradient -----------------------------------------------------
 // G[co][ci][d] = sum_p H[co, p] X[ci, p + d] over a 16x32 pixel tile per CTA.
 // Thread (rowgroup, co-group, ci) keeps 4 output channels x 9 taps in
@@ -115,14 +132,17 @@ __global__ void __launch_bounds__(256) k_conv_wgrad(const float *__restrict__ X,
   const float *hb = Hg + (int64_t)b * Cout * H * W;
   for (int i = tid; i < Cin * (WTY + 2) * (WTX + 2); i += 256) {
     const int c = i / ((WTY + 2) * (WTX + 2)), rq = i % ((WTY + 2) * (WTX + 2));
-    const int r = rq / (WTX + 2), q = rq % (WTX + 2);
-    sx[c * XPL + rq] = ld_pad(xb + (int64_t)c * H * W, H, W, y0 + r - 1, x0 + q - 1);
+    const int yy = y0 + rq / (WTX + 2) - 1, xx = x0 + rq % (WTX + 2) - 1;
+    const bool ok = yy >= 0 && yy < H && xx >= 0 && xx < W;
+    mk::cp_async4_zfill(sx + c * XPL + rq, ok ? xb + (int64_t)c * H * W + (int64_t)yy * W + xx : xb, ok);
   }
   for (int i = tid; i < Cout * WTY * WTX; i += 256) {
     const int c = i / (WTY * WTX), rq = i % (WTY * WTX);
     const int yy = y0 + rq / WTX, xx = x0 + rq % WTX;
-    sh[c * HPL + rq] = (yy < H && xx < W) ? hb[(int64_t)c * H * W + (int64_t)yy * W + xx] : 0.f;
+    const bool ok = yy < H && xx < W;
+    mk::cp_async4_zfill(sh + c * HPL + rq, ok ? hb + (int64_t)c * H * W + (int64_t)yy * W + xx : hb, ok);
   }
+  mk::cp_async_wait_all();
   __syncthreads();
   const int ci = tid & 15, cg = (tid >> 4) & 3, rg = tid >> 6;  // 16 ci x 4 co-groups x 4 row groups
   float acc[4][9];
@@ -193,26 +213,36 @@ int conv_args(int B, int Cin, int Cout, int H, int W) {
 
 dim3 wgrad_grid(int B, int H, int W) { return dim3((W + WTX - 1) / WTX, (H + WTY - 1) / WTY, B); }
 
-template <bool ADJ>
-int conv_launch(const float *in, const float *w, float *out, int B, int Cin, int Cout, int H, int W,
-                cudaStream_t st, const char *what) {
-  static bool attr[2][64] = {{false}};
+template <bool ADJ, int TXT, int TYT>
+int conv_launch_t(const float *in, const float *w, float *out, int B, int Cin, int Cout, int H, int W,
+                  cudaStream_t st, const char *what) {
+  static bool attr[64] = {false};
   int dev = 0;
   MK_CUDA(cudaGetDevice(&dev));
   const int nin = ADJ ? Cout : Cin, nout = ADJ ? Cin : Cout;
-  const size_t smem = conv_smem(nin, nout);
-  dim3 g((W + TX - 1) / TX, (H + TY - 1) / TY, B);
-  if (dev >= 0 && dev < 64 && !attr[ADJ][dev]) {
-    const int mx = (int)conv_smem(CMAX, CMAX);
-    MK_CUDA(cudaFuncSetAttribute(k_conv<ADJ, CMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    MK_CUDA(cudaFuncSetAttribute(k_conv<ADJ, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    attr[ADJ][dev] = true;
+  const size_t smem = conv_smem<TXT, TYT>(nin, nout);
+  if (dev >= 0 && dev < 64 && !attr[dev]) {
+    const int mx = (int)conv_smem<TXT, TYT>(CMAX, CMAX);
+    MK_CUDA(cudaFuncSetAttribute(k_conv<ADJ, CMAX, TXT, TYT>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    MK_CUDA(cudaFuncSetAttribute(k_conv<ADJ, 1, TXT, TYT>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    attr[dev] = true;
   }
+  dim3 g((W + TXT - 1) / TXT, (H + TYT - 1) / TYT, B);
+  constexpr int NT = Tile<TXT, TYT>::NT;
   if (nout == 1)
-    k_conv<ADJ, 1><<<g, 256, smem, st>>>(in, w, out, Cin, Cout, H, W);
+    k_conv<ADJ, 1, TXT, TYT><<<g, NT, smem, st>>>(in, w, out, Cin, Cout, H, W);
   else
-    k_conv<ADJ, CMAX><<<g, 256, smem, st>>>(in, w, out, Cin, Cout, H, W);
+    k_conv<ADJ, CMAX, TXT, TYT><<<g, NT, smem, st>>>(in, w, out, Cin, Cout, H, W);
   return mk::launch_status(what);
+}
+
+template <bool ADJ>
+int conv_launch(const float *in, const float *w, float *out, int B, int Cin, int Cout, int H, int W,
+                cudaStream_t st, const char *what) {
+  const int64_t big_tiles = (int64_t)((W + 31) / 32) * ((H + 31) / 32) * B;
+  if (big_tiles >= 4LL * mk::sm_count())
+    return conv_launch_t<ADJ, 32, 32>(in, w, out, B, Cin, Cout, H, W, st, what);
+  return conv_launch_t<ADJ, 16, 16>(in, w, out, B, Cin, Cout, H, W, st, what);
 }
 
 }  // namespace
