@@ -25,8 +25,9 @@ __device__ __forceinline__ float ld_pad(const float *__restrict__ x, int H, int 
 
 // ---- fwd / adjoint: one kernel, register-blocked ------------------------
 // A CTA owns a TXT x TYT tile of output pixels; each thread a 1x4 strip of it
-// for every output channel (4 x NOUT accumulators), so each shared-memory
-// weight load feeds 4 FMAs.  The input tile plus a 1-pixel halo is staged in
+// for every output channel (4 x NOUT accumulators).  The weights of one
+// input channel and tap are contiguous over the output channels, so one
+// 16-byte shared-memory load brings 4 of them, each feeding 4 FMAs.  The input tile plus a 1-pixel halo is staged in
 // shared memory for every input channel with asynchronous 4-byte copies
 // (zero-filled outside the map), all in flight at once.  The adjoint is the
 // same loop with input and output channels swapped and the taps flipped:
@@ -40,9 +41,10 @@ struct Tile {
   static constexpr int SXW = TXT + 2, SXH = TYT + 2, NT = (TXT / PX) * TYT;
 };
 
+// input planes, then the weights as [ci][tap][o] with o padded to NOUT
 template <int TXT, int TYT>
-size_t conv_smem(int nin, int nout) {
-  return ((size_t)nin * Tile<TXT, TYT>::SXH * Tile<TXT, TYT>::SXW + (size_t)nout * nin * 9) * sizeof(float);
+size_t conv_smem(int nin, int nout_t) {
+  return ((size_t)nin * Tile<TXT, TYT>::SXH * Tile<TXT, TYT>::SXW + (size_t)nin * 9 * nout_t) * sizeof(float);
 }
 
 template <bool ADJ, int NOUT, int TXT, int TYT>
@@ -63,9 +65,9 @@ __global__ void __launch_bounds__(Tile<TXT, TYT>::NT) k_conv(const float *__rest
     const bool ok = yy >= 0 && yy < H && xx >= 0 && xx < W;
     mk::cp_async4_zfill(sx + i, ok ? ib + (int64_t)c * H * W + (int64_t)yy * W + xx : ib, ok);
   }
-  for (int i = tid; i < nout * nin * 9; i += NT) {
-    const int o = i / (nin * 9), ii = (i / 9) % nin, d = i % 9;
-    sw[i] = ADJ ? Wt[(ii * Cin + o) * 9 + (8 - d)] : Wt[(o * Cin + ii) * 9 + d];
+  for (int i = tid; i < nin * 9 * NOUT; i += NT) {
+    const int o = i % NOUT, d = (i / NOUT) % 9, ii = i / (9 * NOUT);
+    sw[i] = o >= nout ? 0.f : ADJ ? Wt[(ii * Cin + o) * 9 + (8 - d)] : Wt[(o * Cin + ii) * 9 + d];
   }
   mk::cp_async_wait_all();
   __syncthreads();
@@ -82,17 +84,24 @@ __global__ void __launch_bounds__(Tile<TXT, TYT>::NT) k_conv(const float *__rest
     for (int r = 0; r < 3; r++)
 #pragma unroll
       for (int c = 0; c < PX + 2; c++) win[r][c] = sp[r * SXW + c];
-    const float *wc = sw + ci * 9;
+    const float *wc = sw + ci * 9 * NOUT;
 #pragma unroll
     for (int d = 0; d < 9; d++) {
+      float wv[NOUT];
+      if constexpr (NOUT % 4 == 0) {
 #pragma unroll
-      for (int o = 0; o < NOUT; o++) {
-        if (o < nout) {
-          const float wv = wc[o * nin * 9 + d];
-#pragma unroll
-          for (int p = 0; p < PX; p++) acc[p][o] = fmaf(wv, win[d / 3][p + d % 3], acc[p][o]);
+        for (int k = 0; k < NOUT / 4; k++) {
+          const float4 q = reinterpret_cast<const float4 *>(wc + d * NOUT)[k];
+          wv[4 * k] = q.x, wv[4 * k + 1] = q.y, wv[4 * k + 2] = q.z, wv[4 * k + 3] = q.w;
         }
+      } else {
+#pragma unroll
+        for (int o = 0; o < NOUT; o++) wv[o] = wc[d * NOUT + o];
       }
+#pragma unroll
+      for (int o = 0; o < NOUT; o++)
+#pragma unroll
+        for (int p = 0; p < PX; p++) acc[p][o] = fmaf(wv[o], win[d / 3][p + d % 3], acc[p][o]);
     }
   }
   const int yy = y0 + ty;
@@ -220,7 +229,7 @@ int conv_launch_t(const float *in, const float *w, float *out, int B, int Cin, i
   int dev = 0;
   MK_CUDA(cudaGetDevice(&dev));
   const int nin = ADJ ? Cout : Cin, nout = ADJ ? Cin : Cout;
-  const size_t smem = conv_smem<TXT, TYT>(nin, nout);
+  const size_t smem = conv_smem<TXT, TYT>(nin, nout == 1 ? 1 : CMAX);
   if (dev >= 0 && dev < 64 && !attr[dev]) {
     const int mx = (int)conv_smem<TXT, TYT>(CMAX, CMAX);
     MK_CUDA(cudaFuncSetAttribute(k_conv<ADJ, CMAX, TXT, TYT>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));

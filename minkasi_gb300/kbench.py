@@ -170,6 +170,33 @@ def conv_bench(dev, hw: int = 2048, batch: int = 1, c: int = 16) -> dict:
                      ("conv_wgrad", lambda: L.conv_wgrad(x, h))):
         ms = best_ms(fn)
         res[name] = {"ms": ms, "TFLOPs": flops / ms / 1e9, "shape": [batch, c, hw, hw]}
+    res["precon_small"] = precon_bench(dev)
+    return res
+
+
+def precon_bench(dev, hw: int = 256) -> dict:
+    """z = M r of the learned preconditioner on an hw x hw FP64 map (the
+    1 -> 16 -> 16 -> 16 -> 16 network, 8 convolutions), as the PCG runs it:
+    replayed from a CUDA graph.  Also each convolution shape alone."""
+    from . import learned as L
+    net = L.ConvNet.init(seed=0, device=dev)
+    hits = torch.rand((hw, hw), dtype=torch.float64, device=dev) * 100 + 1
+    M = L.LearnedPrecon(hits, net, (hw, hw))
+    r = torch.randn(hw * hw, dtype=torch.float64, device=dev)
+    z = torch.empty_like(r)
+    M.apply(r, z)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        M.apply(r, z)
+    res = {"shape": [hw, hw], "apply_graph_ms": best_ms(g.replay, reps=20),
+           "apply_eager_ms": best_ms(lambda: M.apply(r, z), reps=20)}
+    x1 = torch.randn((1, 1, hw, hw), dtype=torch.float32, device=dev)
+    x16 = torch.randn((1, 16, hw, hw), dtype=torch.float32, device=dev)
+    w0, w1 = net.weights[0], net.weights[1]
+    for name, fn in (("fwd_1_16", lambda: L.conv_fwd(x1, w0)), ("fwd_16_16", lambda: L.conv_fwd(x16, w1)),
+                     ("adj_16_16", lambda: L.conv_adj(x16, w1)), ("adj_16_1", lambda: L.conv_adj(x16, w0))):
+        res[name + "_ms"] = best_ms(fn, reps=20)
     return res
 
 
