@@ -19,40 +19,41 @@ namespace {
 constexpr int CMAX = 16;
 constexpr int NW = CMAX * CMAX * 9;
 
-__device__ __forceinline__ float ld_pad(const float *__restrict__ x, int H, int W, int y, int xx) {
-  return (y >= 0 && y < H && xx >= 0 && xx < W) ? x[(int64_t)y * W + xx] : 0.f;
-}
-
 // ---- fwd / adjoint: one kernel, register-blocked ------------------------
 // A CTA owns a TXT x TYT tile of output pixels; each thread a 1x4 strip of it
-// for every output channel (4 x NOUT accumulators).  The weights of one
-// input channel and tap are contiguous over the output channels, so one
-// 16-byte shared-memory load brings 4 of them, each feeding 4 FMAs.  The input tile plus a 1-pixel halo is staged in
-// shared memory for every input channel with asynchronous 4-byte copies
-// (zero-filled outside the map), all in flight at once.  The adjoint is the
-// same loop with input and output channels swapped and the taps flipped:
-//   adj(o = ci, i = co, d) = W[co][ci][8 - d].
-// Tiles of 32 x 32 (256 threads) serve large maps; 16 x 16 (64 threads) keep
-// every SM busy on small ones.
+// for NOUT / OG of the output channels (OG threads share a strip, one warp
+// all on the same channel group).  The weights of one input channel and tap
+// are contiguous over the output channels, so one 16-byte shared-memory load
+// brings 4 of them, each feeding 4 FMAs.  The input tile plus a 1-pixel halo
+// is staged in shared memory for every input channel with asynchronous
+// 4-byte copies (zero-filled outside the map), all in flight at once.  The
+// adjoint is the same loop with input and output channels swapped and the
+// taps flipped:  adj(o = ci, i = co, d) = W[co][ci][8 - d].
+// Large maps use 32 x 32 tiles with one thread per strip (256 threads);
+// small ones 16 x 16 tiles with 4 channel groups (256 threads), which gives
+// the GPU 4x as many warps for the same work.
 constexpr int PX = 4;
 
-template <int TXT, int TYT>
+template <int TXT, int TYT, int OG>
 struct Tile {
-  static constexpr int SXW = TXT + 2, SXH = TYT + 2, NT = (TXT / PX) * TYT;
+  static constexpr int SXW = TXT + 2, SXH = TYT + 2, NS = (TXT / PX) * TYT, NT = NS * OG;
 };
 
 // input planes, then the weights as [ci][tap][o] with o padded to NOUT
 template <int TXT, int TYT>
 size_t conv_smem(int nin, int nout_t) {
-  return ((size_t)nin * Tile<TXT, TYT>::SXH * Tile<TXT, TYT>::SXW + (size_t)nin * 9 * nout_t) * sizeof(float);
+  return ((size_t)nin * Tile<TXT, TYT, 1>::SXH * Tile<TXT, TYT, 1>::SXW + (size_t)nin * 9 * nout_t) *
+         sizeof(float);
 }
 
-template <bool ADJ, int NOUT, int TXT, int TYT>
-__global__ void __launch_bounds__(Tile<TXT, TYT>::NT) k_conv(const float *__restrict__ In,
-                                                             const float *__restrict__ Wt,
-                                                             float *__restrict__ Out, int Cin, int Cout, int H,
-                                                             int W) {
-  constexpr int SXW = Tile<TXT, TYT>::SXW, SXH = Tile<TXT, TYT>::SXH, NT = Tile<TXT, TYT>::NT;
+template <bool ADJ, int NOUT, int OG, int TXT, int TYT>
+__global__ void __launch_bounds__(Tile<TXT, TYT, OG>::NT) k_conv(const float *__restrict__ In,
+                                                                 const float *__restrict__ Wt,
+                                                                 float *__restrict__ Out, int Cin, int Cout,
+                                                                 int H, int W) {
+  using T = Tile<TXT, TYT, OG>;
+  constexpr int SXW = T::SXW, SXH = T::SXH, NT = T::NT, NO = NOUT / OG;
+  static_assert(NOUT % OG == 0 && (OG == 1 || NO % 4 == 0), "channel groups of 4");
   extern __shared__ float smem[];
   const int nin = ADJ ? Cout : Cin, nout = ADJ ? Cin : Cout;
   float *sx = smem;
@@ -71,12 +72,13 @@ __global__ void __launch_bounds__(Tile<TXT, TYT>::NT) k_conv(const float *__rest
   }
   mk::cp_async_wait_all();
   __syncthreads();
-  const int ty = tid / (TXT / PX), tx = (tid % (TXT / PX)) * PX;
-  float acc[PX][NOUT];
+  const int strip = tid % T::NS, o0 = (tid / T::NS) * NO;
+  const int ty = strip / (TXT / PX), tx = (strip % (TXT / PX)) * PX;
+  float acc[PX][NO];
 #pragma unroll
   for (int p = 0; p < PX; p++)
 #pragma unroll
-    for (int o = 0; o < NOUT; o++) acc[p][o] = 0.f;
+    for (int o = 0; o < NO; o++) acc[p][o] = 0.f;
   for (int ci = 0; ci < nin; ci++) {
     const float *sp = sx + ci * SXH * SXW + ty * SXW + tx;
     float win[3][PX + 2];
@@ -84,22 +86,22 @@ __global__ void __launch_bounds__(Tile<TXT, TYT>::NT) k_conv(const float *__rest
     for (int r = 0; r < 3; r++)
 #pragma unroll
       for (int c = 0; c < PX + 2; c++) win[r][c] = sp[r * SXW + c];
-    const float *wc = sw + ci * 9 * NOUT;
+    const float *wc = sw + ci * 9 * NOUT + o0;
 #pragma unroll
     for (int d = 0; d < 9; d++) {
-      float wv[NOUT];
-      if constexpr (NOUT % 4 == 0) {
+      float wv[NO];
+      if constexpr (NO % 4 == 0) {
 #pragma unroll
-        for (int k = 0; k < NOUT / 4; k++) {
+        for (int k = 0; k < NO / 4; k++) {
           const float4 q = reinterpret_cast<const float4 *>(wc + d * NOUT)[k];
           wv[4 * k] = q.x, wv[4 * k + 1] = q.y, wv[4 * k + 2] = q.z, wv[4 * k + 3] = q.w;
         }
       } else {
 #pragma unroll
-        for (int o = 0; o < NOUT; o++) wv[o] = wc[d * NOUT + o];
+        for (int o = 0; o < NO; o++) wv[o] = wc[d * NOUT + o];
       }
 #pragma unroll
-      for (int o = 0; o < NOUT; o++)
+      for (int o = 0; o < NO; o++)
 #pragma unroll
         for (int p = 0; p < PX; p++) acc[p][o] = fmaf(wv[o], win[d / 3][p + d % 3], acc[p][o]);
     }
@@ -112,8 +114,8 @@ __global__ void __launch_bounds__(Tile<TXT, TYT>::NT) k_conv(const float *__rest
     const int xx = x0 + tx + p;
     if (xx < W) {
 #pragma unroll
-      for (int o = 0; o < NOUT; o++)
-        if (o < nout) ob[(int64_t)o * H * W + xx] = acc[p][o];
+      for (int o = 0; o < NO; o++)
+        if (o0 + o < nout) ob[(int64_t)(o0 + o) * H * W + xx] = acc[p][o];
     }
   }
 }
@@ -222,7 +224,7 @@ int conv_args(int B, int Cin, int Cout, int H, int W) {
 
 dim3 wgrad_grid(int B, int H, int W) { return dim3((W + WTX - 1) / WTX, (H + WTY - 1) / WTY, B); }
 
-template <bool ADJ, int TXT, int TYT>
+template <bool ADJ, int OG, int TXT, int TYT>
 int conv_launch_t(const float *in, const float *w, float *out, int B, int Cin, int Cout, int H, int W,
                   cudaStream_t st, const char *what) {
   static bool attr[64] = {false};
@@ -232,16 +234,16 @@ int conv_launch_t(const float *in, const float *w, float *out, int B, int Cin, i
   const size_t smem = conv_smem<TXT, TYT>(nin, nout == 1 ? 1 : CMAX);
   if (dev >= 0 && dev < 64 && !attr[dev]) {
     const int mx = (int)conv_smem<TXT, TYT>(CMAX, CMAX);
-    MK_CUDA(cudaFuncSetAttribute(k_conv<ADJ, CMAX, TXT, TYT>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    MK_CUDA(cudaFuncSetAttribute(k_conv<ADJ, 1, TXT, TYT>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    MK_CUDA(cudaFuncSetAttribute(k_conv<ADJ, CMAX, OG, TXT, TYT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 mx));
+    MK_CUDA(cudaFuncSetAttribute(k_conv<ADJ, 1, 1, TXT, TYT>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     attr[dev] = true;
   }
   dim3 g((W + TXT - 1) / TXT, (H + TYT - 1) / TYT, B);
-  constexpr int NT = Tile<TXT, TYT>::NT;
   if (nout == 1)
-    k_conv<ADJ, 1, TXT, TYT><<<g, NT, smem, st>>>(in, w, out, Cin, Cout, H, W);
+    k_conv<ADJ, 1, 1, TXT, TYT><<<g, Tile<TXT, TYT, 1>::NT, smem, st>>>(in, w, out, Cin, Cout, H, W);
   else
-    k_conv<ADJ, CMAX, TXT, TYT><<<g, NT, smem, st>>>(in, w, out, Cin, Cout, H, W);
+    k_conv<ADJ, CMAX, OG, TXT, TYT><<<g, Tile<TXT, TYT, OG>::NT, smem, st>>>(in, w, out, Cin, Cout, H, W);
   return mk::launch_status(what);
 }
 
@@ -250,8 +252,8 @@ int conv_launch(const float *in, const float *w, float *out, int B, int Cin, int
                 cudaStream_t st, const char *what) {
   const int64_t big_tiles = (int64_t)((W + 31) / 32) * ((H + 31) / 32) * B;
   if (big_tiles >= 4LL * mk::sm_count())
-    return conv_launch_t<ADJ, 32, 32>(in, w, out, B, Cin, Cout, H, W, st, what);
-  return conv_launch_t<ADJ, 16, 16>(in, w, out, B, Cin, Cout, H, W, st, what);
+    return conv_launch_t<ADJ, 1, 32, 32>(in, w, out, B, Cin, Cout, H, W, st, what);
+  return conv_launch_t<ADJ, 4, 16, 16>(in, w, out, B, Cin, Cout, H, W, st, what);
 }
 
 }  // namespace

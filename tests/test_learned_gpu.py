@@ -25,8 +25,11 @@ def rel(a, b):
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
 
 
+# the last two are large enough (>= 4 x 152 tiles of 32 x 32 over the batch of
+# 2) for the large-map tiling; the others use the small-map one
 @pytest.mark.parametrize("cin,cout,H,W", [(1, 16, 33, 20), (16, 16, 16, 16), (16, 1, 40, 47), (5, 7, 3, 2),
-                                         (16, 16, 70, 95), (16, 1, 65, 33)])
+                                         (16, 16, 70, 95), (16, 1, 65, 33), (7, 16, 521, 611),
+                                         (16, 1, 530, 600)])
 def test_conv_kernels_match_oracle(L, cin, cout, H, W):
     rng = np.random.default_rng(cin * 100 + cout)
     x = rng.standard_normal((2, cin, H, W))
