@@ -397,6 +397,20 @@ size_t mk_conv3x3_wgrad_scratch_bytes(int B, int Cin, int Cout, int H, int W);
 int mk_conv3x3_wgrad(const float *x, const float *h, float *g, int B, int Cin, int Cout, int H,
                      int W, void *scratch, size_t scratch_bytes, void *stream);
 
+/* z = M r for the learned preconditioner on one H x W map, in one call:
+ *   u = dsq * r,  z = dsq * (u + K^T K u),  K = L_n ... L_1,
+ * dsq = D^-1/2 (0 on unhit pixels).  Layer l maps channels[l-1] ->
+ * channels[l] (channels[0] = 1, all <= 16) with weights[l-1] (a host array
+ * of device pointers, each [channels[l]][channels[l-1]][3][3] float32).  The
+ * first and last convolutions form u and z themselves; the 2(n-1) others
+ * run FP32 through `work` (mk_learned_precon_work_bytes).  z, r, dsq are
+ * dtype-typed maps; z may alias r.  Replaces the elementwise `precon * r`
+ * of minkasi/mapmaking/pcg.py:157-158 (no reference counterpart). */
+size_t mk_learned_precon_work_bytes(int H, int W, int nlayer, const int *channels);
+int mk_learned_precon_apply(void *z, const void *r, const void *dsq, int H, int W, int nlayer,
+                            const int *channels, const float *const *weights, float *work,
+                            size_t work_bytes, int dtype, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -83,6 +83,8 @@ SIGNATURES = {
     "mk_conv3x3_adj": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp]),
     "mk_conv3x3_wgrad_scratch_bytes": (_sz, [_i32, _i32, _i32, _i32, _i32]),
     "mk_conv3x3_wgrad": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp, _sz, _vp]),
+    "mk_learned_precon_work_bytes": (_sz, [_i32, _i32, _i32, _vp]),
+    "mk_learned_precon_apply": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp, _sz, _i32, _vp]),
 }
 
 _lib: Optional[ctypes.CDLL] = None

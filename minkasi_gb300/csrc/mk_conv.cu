@@ -46,11 +46,20 @@ size_t conv_smem(int nin, int nout_t) {
          sizeof(float);
 }
 
-template <bool ADJ, int NOUT, int OG, int TXT, int TYT>
-__global__ void __launch_bounds__(Tile<TXT, TYT, OG>::NT) k_conv(const float *__restrict__ In,
-                                                                 const float *__restrict__ Wt,
-                                                                 float *__restrict__ Out, int Cin, int Cout,
-                                                                 int H, int W) {
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+
+// EPI selects what surrounds the convolution (TT = the map type, float or
+// double): 0 plain FP32 in/out; 1 the single input plane is u = dsq * r,
+// formed while staging (In unused); 2 the single output plane is written as
+// z = dsq * (dsq * r + conv) (Out unused).  1 and 2 are the first and last
+// layers of the preconditioner M r = D^-1/2 (u + K^T K u), u = D^-1/2 r.
+template <bool ADJ, int NOUT, int OG, int TXT, int TYT, int EPI = 0, typename TT = float>
+__global__ void __launch_bounds__(Tile<TXT, TYT, OG>::NT)
+    k_conv(const float *__restrict__ In, const float *__restrict__ Wt, float *__restrict__ Out, int Cin, int Cout,
+           int H, int W, const TT *__restrict__ r, const TT *__restrict__ dsq, TT *__restrict__ z) {
   using T = Tile<TXT, TYT, OG>;
   constexpr int SXW = T::SXW, SXH = T::SXH, NT = T::NT, NO = NOUT / OG;
   static_assert(NOUT % OG == 0 && (OG == 1 || NO % 4 == 0), "channel groups of 4");
@@ -59,12 +68,25 @@ __global__ void __launch_bounds__(Tile<TXT, TYT, OG>::NT) k_conv(const float *__
   float *sx = smem;
   float *sw = smem + nin * SXH * SXW;
   const int b = blockIdx.z, y0 = blockIdx.y * TYT, x0 = blockIdx.x * TXT, tid = threadIdx.x;
-  const float *ib = In + (int64_t)b * nin * H * W;
-  for (int i = tid; i < nin * SXH * SXW; i += NT) {
-    const int c = i / (SXH * SXW), r = (i / SXW) % SXH, q = i % SXW;
-    const int yy = y0 + r - 1, xx = x0 + q - 1;
-    const bool ok = yy >= 0 && yy < H && xx >= 0 && xx < W;
-    mk::cp_async4_zfill(sx + i, ok ? ib + (int64_t)c * H * W + (int64_t)yy * W + xx : ib, ok);
+  if constexpr (EPI == 1) {
+    // nin == 1
+    for (int i = tid; i < SXH * SXW; i += NT) {
+      const int yy = y0 + i / SXW - 1, xx = x0 + i % SXW - 1;
+      float v = 0.f;
+      if (yy >= 0 && yy < H && xx >= 0 && xx < W) {
+        const int64_t g = ((int64_t)b * H + yy) * W + xx;
+        v = (float)mul_rn(dsq[g], r[g]);
+      }
+      sx[i] = v;
+    }
+  } else {
+    const float *ib = In + (int64_t)b * nin * H * W;
+    for (int i = tid; i < nin * SXH * SXW; i += NT) {
+      const int c = i / (SXH * SXW), rr = (i / SXW) % SXH, q = i % SXW;
+      const int yy = y0 + rr - 1, xx = x0 + q - 1;
+      const bool ok = yy >= 0 && yy < H && xx >= 0 && xx < W;
+      mk::cp_async4_zfill(sx + i, ok ? ib + (int64_t)c * H * W + (int64_t)yy * W + xx : ib, ok);
+    }
   }
   for (int i = tid; i < nin * 9 * NOUT; i += NT) {
     const int o = i % NOUT, d = (i / NOUT) % 9, ii = i / (9 * NOUT);
@@ -108,6 +130,20 @@ __global__ void __launch_bounds__(Tile<TXT, TYT, OG>::NT) k_conv(const float *__
   }
   const int yy = y0 + ty;
   if (yy >= H) return;
+  if constexpr (EPI == 2) {
+    // nout == 1
+    if (o0 != 0) return;
+#pragma unroll
+    for (int p = 0; p < PX; p++) {
+      const int xx = x0 + tx + p;
+      if (xx < W) {
+        const int64_t g = ((int64_t)b * H + yy) * W + xx;
+        const TT d = dsq[g];
+        z[g] = mul_rn(d, add_rn(mul_rn(d, r[g]), (TT)acc[p][0]));
+      }
+    }
+    return;
+  }
   float *ob = Out + (int64_t)b * nout * H * W + (int64_t)yy * W;
 #pragma unroll
   for (int p = 0; p < PX; p++) {
@@ -224,36 +260,59 @@ int conv_args(int B, int Cin, int Cout, int H, int W) {
 
 dim3 wgrad_grid(int B, int H, int W) { return dim3((W + WTX - 1) / WTX, (H + WTY - 1) / WTY, B); }
 
-template <bool ADJ, int OG, int TXT, int TYT>
+template <bool ADJ, int OG, int TXT, int TYT, int EPI, typename TT>
 int conv_launch_t(const float *in, const float *w, float *out, int B, int Cin, int Cout, int H, int W,
-                  cudaStream_t st, const char *what) {
+                  const TT *r, const TT *dsq, TT *z, cudaStream_t st, const char *what) {
   static bool attr[64] = {false};
   int dev = 0;
   MK_CUDA(cudaGetDevice(&dev));
   const int nin = ADJ ? Cout : Cin, nout = ADJ ? Cin : Cout;
   const size_t smem = conv_smem<TXT, TYT>(nin, nout == 1 ? 1 : CMAX);
+  auto k16 = k_conv<ADJ, CMAX, OG, TXT, TYT, EPI, TT>;
+  auto k1 = k_conv<ADJ, 1, 1, TXT, TYT, EPI, TT>;
   if (dev >= 0 && dev < 64 && !attr[dev]) {
     const int mx = (int)conv_smem<TXT, TYT>(CMAX, CMAX);
-    MK_CUDA(cudaFuncSetAttribute(k_conv<ADJ, CMAX, OG, TXT, TYT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 mx));
-    MK_CUDA(cudaFuncSetAttribute(k_conv<ADJ, 1, 1, TXT, TYT>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    if constexpr (EPI != 2) MK_CUDA(cudaFuncSetAttribute(k16, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    MK_CUDA(cudaFuncSetAttribute(k1, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     attr[dev] = true;
   }
   dim3 g((W + TXT - 1) / TXT, (H + TYT - 1) / TYT, B);
-  if (nout == 1)
-    k_conv<ADJ, 1, 1, TXT, TYT><<<g, Tile<TXT, TYT, 1>::NT, smem, st>>>(in, w, out, Cin, Cout, H, W);
-  else
-    k_conv<ADJ, CMAX, OG, TXT, TYT><<<g, Tile<TXT, TYT, OG>::NT, smem, st>>>(in, w, out, Cin, Cout, H, W);
+  if constexpr (EPI == 2) {
+    k1<<<g, Tile<TXT, TYT, 1>::NT, smem, st>>>(in, w, out, Cin, Cout, H, W, r, dsq, z);
+  } else {
+    if (nout == 1)
+      k1<<<g, Tile<TXT, TYT, 1>::NT, smem, st>>>(in, w, out, Cin, Cout, H, W, r, dsq, z);
+    else
+      k16<<<g, Tile<TXT, TYT, OG>::NT, smem, st>>>(in, w, out, Cin, Cout, H, W, r, dsq, z);
+  }
   return mk::launch_status(what);
 }
 
-template <bool ADJ>
+// 32 x 32 tiles when they give every SM at least 4; 16 x 16 with 4 channel
+// groups otherwise
+template <bool ADJ, int EPI = 0, typename TT = float>
 int conv_launch(const float *in, const float *w, float *out, int B, int Cin, int Cout, int H, int W,
-                cudaStream_t st, const char *what) {
+                cudaStream_t st, const char *what, const TT *r = nullptr, const TT *dsq = nullptr,
+                TT *z = nullptr) {
   const int64_t big_tiles = (int64_t)((W + 31) / 32) * ((H + 31) / 32) * B;
   if (big_tiles >= 4LL * mk::sm_count())
-    return conv_launch_t<ADJ, 1, 32, 32>(in, w, out, B, Cin, Cout, H, W, st, what);
-  return conv_launch_t<ADJ, 4, 16, 16>(in, w, out, B, Cin, Cout, H, W, st, what);
+    return conv_launch_t<ADJ, 1, 32, 32, EPI, TT>(in, w, out, B, Cin, Cout, H, W, r, dsq, z, st, what);
+  return conv_launch_t<ADJ, 4, 16, 16, EPI, TT>(in, w, out, B, Cin, Cout, H, W, r, dsq, z, st, what);
+}
+
+template <typename TT>
+int precon_apply(TT *z, const TT *r, const TT *dsq, int H, int W, int nl, const int *ch, const float *const *wt,
+                 float *work, int maxc, cudaStream_t st) {
+  float *buf[2] = {work, work + (size_t)maxc * H * W};
+  const char *what = "mk_learned_precon_apply";
+  int cur = 0;
+  int rc = conv_launch<false, 1, TT>(nullptr, wt[0], buf[0], 1, 1, ch[1], H, W, st, what, r, dsq, nullptr);
+  for (int l = 1; l < nl && !rc; l++, cur ^= 1)
+    rc = conv_launch<false>(buf[cur], wt[l], buf[cur ^ 1], 1, ch[l], ch[l + 1], H, W, st, what);
+  for (int l = nl - 1; l >= 1 && !rc; l--, cur ^= 1)
+    rc = conv_launch<true>(buf[cur], wt[l], buf[cur ^ 1], 1, ch[l], ch[l + 1], H, W, st, what);
+  if (!rc) rc = conv_launch<true, 2, TT>(buf[cur], wt[0], nullptr, 1, 1, ch[1], H, W, st, what, r, dsq, z);
+  return rc;
 }
 
 }  // namespace
@@ -300,4 +359,37 @@ extern "C" int mk_conv3x3_wgrad(const float *x, const float *h, float *g, int B,
   const int64_t ncta = (int64_t)grid.x * grid.y * grid.z;
   k_wgrad_reduce<<<(nw + 127) / 128, 128, 0, st>>>((const float *)scratch, ncta, nw, g);
   return mk::launch_status("mk_conv3x3_wgrad");
+}
+
+extern "C" size_t mk_learned_precon_work_bytes(int H, int W, int nlayer, const int *channels) {
+  if (H <= 0 || W <= 0 || nlayer < 1 || !channels) return 0;
+  int maxc = 1;
+  for (int l = 0; l <= nlayer; l++) maxc = channels[l] > maxc ? channels[l] : maxc;
+  return 2 * (size_t)maxc * H * W * sizeof(float);
+}
+
+extern "C" int mk_learned_precon_apply(void *z, const void *r, const void *dsq, int H, int W, int nlayer,
+                                       const int *channels, const float *const *weights, float *work,
+                                       size_t work_bytes, int dtype, void *stream) {
+  MK_CHECK_ARG(MK_DTYPE_OK(dtype), "mk_learned_precon_apply: bad dtype %d", dtype);
+  MK_CHECK_ARG(nlayer >= 1 && nlayer <= 16 && channels && weights,
+               "mk_learned_precon_apply: need 1..16 layers with channels and weights (got %d)", nlayer);
+  MK_CHECK_ARG(channels[0] == 1, "mk_learned_precon_apply: the first layer takes 1 channel (got %d)",
+               channels[0]);
+  for (int l = 1; l <= nlayer; l++) {
+    int rc = conv_args(1, channels[l - 1], channels[l], H, W);
+    if (rc) return rc;
+    MK_CHECK_ARG(weights[l - 1] != nullptr, "mk_learned_precon_apply: layer %d has no weights", l);
+  }
+  MK_CHECK_ARG(z && r && dsq && work, "mk_learned_precon_apply: null pointer");
+  MK_CHECK_ARG(work_bytes >= mk_learned_precon_work_bytes(H, W, nlayer, channels),
+               "mk_learned_precon_apply: work too small (%zu bytes)", work_bytes);
+  int maxc = 1;
+  for (int l = 0; l <= nlayer; l++) maxc = channels[l] > maxc ? channels[l] : maxc;
+  cudaStream_t st = mk::as_stream(stream);
+  if (dtype == MK_F64)
+    return precon_apply<double>((double *)z, (const double *)r, (const double *)dsq, H, W, nlayer, channels,
+                                weights, work, maxc, st);
+  return precon_apply<float>((float *)z, (const float *)r, (const float *)dsq, H, W, nlayer, channels, weights,
+                             work, maxc, st);
 }

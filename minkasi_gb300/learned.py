@@ -149,19 +149,22 @@ class LearnedPrecon:
         self.dsq32 = dsq.float().contiguous()
         self.net = net
         self.shape = tuple(shape)
-        self._u = None
+        ws = net.weights
+        self._ch = (ctypes.c_int * (len(ws) + 1))(int(ws[0].shape[1]), *[int(w.shape[0]) for w in ws])
+        nb = int(lib().mk_learned_precon_work_bytes(self.shape[0], self.shape[1], len(ws), self._ch))
+        self._work = torch.empty((nb + 3) // 4, dtype=torch.float32, device=hits.device)
 
     def apply(self, r: torch.Tensor, z: torch.Tensor) -> torch.Tensor:
-        """z = M r for flat maps (float32 or float64)."""
-        dt = r.dtype
-        dsq = self.dsq64 if dt == torch.float64 else self.dsq32
-        u = torch.empty_like(r)
-        K.mul(u, dsq, r)
-        u32 = u if dt == torch.float32 else u.float()
-        kk = self.net.ktk(u32.view(1, 1, *self.shape)).reshape(-1)
-        kk = kk if dt == torch.float32 else kk.double()
-        check(lib().mk_scale_add(_p(z), _p(dsq), _p(u), _p(kk.contiguous()), z.numel(),
-                                 K.dtype_code(z), _stream()), "scale_add")
+        """z = M r for flat maps (float32 or float64): one library call
+        (mk_learned_precon_apply, 2n convolution launches)."""
+        dsq = self.dsq64 if r.dtype == torch.float64 else self.dsq32
+        if z.dtype != r.dtype or r.numel() != dsq.numel() or z.numel() != dsq.numel():
+            raise ValueError("LearnedPrecon.apply: r and z must be maps of one dtype and the map's size")
+        ws = self.net.weights
+        wp = (ctypes.c_void_p * len(ws))(*[w.data_ptr() for w in ws])
+        check(lib().mk_learned_precon_apply(_p(z), _p(r), _p(dsq), self.shape[0], self.shape[1], len(ws),
+                                            self._ch, wp, _p(self._work), self._work.numel() * 4,
+                                            K.dtype_code(z), _stream()), "learned_precon_apply")
         return z
 
     def __mul__(self, mapset):

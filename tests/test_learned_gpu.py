@@ -78,3 +78,45 @@ def test_learned_precon_is_spd_and_reduces_to_jacobi(L):
     Z.apply(a, out)
     jac = torch.where(hits > 0, a / hits.clamp(min=1), torch.zeros_like(a))
     assert torch.allclose(out, jac, rtol=1e-6, atol=1e-12)
+
+
+@pytest.mark.parametrize("shape", [(37, 53), (700, 900)])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_fused_precon_apply(L, shape, dtype):
+    """mk_learned_precon_apply (first and last layers fused with the D^-1/2
+    scalings) against the same operator built from the separate convolution
+    calls (bit-exact), and against the float64 oracle on the small map.
+    (700, 900) is large enough for the 32 x 32 tiling."""
+    rng = np.random.default_rng(shape[0])
+    n = shape[0] * shape[1]
+    hits_np = rng.integers(0, 5, size=n).astype(np.float64)
+    hits = torch.from_numpy(hits_np).to(cuda)
+    net = L.ConvNet.init(seed=2, scale=0.3, device=cuda)
+    M = L.LearnedPrecon(hits, net, shape)
+    r = torch.from_numpy(rng.standard_normal(n)).to(cuda, dtype)
+    z = torch.empty_like(r)
+    M.apply(r, z)
+    dsq = (M.dsq64 if dtype == torch.float64 else M.dsq32)
+    u = dsq * r
+    acts = u.float().view(1, 1, *shape)
+    for w in net.weights:
+        acts = L.conv_fwd(acts, w)
+    for w in reversed(net.weights):
+        acts = L.conv_adj(acts, w)
+    want = dsq * (u + acts.reshape(-1).to(dtype))
+    assert torch.equal(z, want)
+    if shape[0] < 100:
+        d = M.dsq64.cpu().numpy()
+        u64 = d * r.double().cpu().numpy()
+        a = u64.reshape(1, 1, *shape)
+        ws = [w.double().cpu().numpy() for w in net.weights]
+        for w in ws:
+            a = lo.conv_fwd(a, w)
+        for w in reversed(ws):
+            a = lo.conv_adj(a, w)
+        ref = d * (u64 + a.reshape(-1))
+        assert rel(z.double().cpu().numpy(), ref) < 1e-5
+    # z may alias r
+    r2 = r.clone()
+    M.apply(r2, r2)
+    assert torch.equal(r2, z)
