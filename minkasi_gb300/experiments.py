@@ -24,7 +24,9 @@ from x0 = 0 to ||b - A x||/||b|| <= tol with A the FP64 operator:
   learned_f64    : FP64 PCG with the learned preconditioner
 
 Every wall time brackets the solve only (operators, autotuning and training
-happen before), with torch.cuda.synchronize() on both sides.  Map errors are
+happen before), with torch.cuda.synchronize() on both sides; wall_s is the
+second of two identical solves and cold_wall_s the first (graph captures,
+lazy kernel loading).  inner_step_ms is one graph-replayed inner iteration.  Map errors are
 against the truth map with the mean over hit pixels removed (A annihilates
 a constant map, so that mean is undetermined).  Prints one JSON object.
 """
@@ -40,7 +42,7 @@ import torch
 
 from . import learned as L
 from .maps import Mapset
-from .pcg import run_pcg, run_pcg_mixed
+from .pcg import DevicePCG, MixedOp, run_pcg, run_pcg_mixed
 from .projections import jacobi_precon, make_hits
 from .synth import CONFIGS, make_todvec
 
@@ -59,6 +61,31 @@ def timed(fn):
     out = fn()
     torch.cuda.synchronize()
     return out, time.perf_counter() - t0
+
+
+def timed_warm(fn):
+    """(result, warm seconds, cold seconds): the second of two identical
+    calls, and the first (graph captures, lazy kernel loading, plans)."""
+    _, cold = timed(fn)
+    out, warm = timed(fn)
+    return out, warm, cold
+
+
+def inner_step_ms(op32, b: torch.Tensor, M, steps: int = 100) -> float:
+    """Device time of one graph-replayed inner iteration of the mixed solver
+    (FP32 operator, FP64 vectors) with preconditioner M."""
+    st = DevicePCG(MixedOp(op32, b.numel(), b.device), b, torch.zeros_like(b), M, graph=True)
+    st.start()
+    for _ in range(5):
+        st.step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        st.step()
+    e1.record()
+    e1.synchronize()
+    return e0.elapsed_time(e1) / steps
 
 
 def run(config: str = "c1", tol: float = 1e-6, learned: bool = True, pairs: int = 5000,
@@ -87,16 +114,18 @@ def run(config: str = "c1", tol: float = 1e-6, learned: bool = True, pairs: int 
     out["truth"] = {"iters": xt.niter, "wall_s": t_truth}
 
     hist = []
-    xj, tj = timed(lambda: run_pcg(rhs, x0, tv, pre, maxiter=5000, tol=tol, verbose=False,
-                                   history=None))
-    out["jacobi_f64"] = {"iters": xj.niter, "wall_s": tj,
+    xj, tj, tjc = timed_warm(lambda: run_pcg(rhs, x0, tv, pre, maxiter=5000, tol=tol, verbose=False,
+                                             history=None))
+    out["jacobi_f64"] = {"iters": xj.niter, "wall_s": tj, "cold_wall_s": tjc,
                          "map_err": map_error(xj.maps[0].map, truth, hit)}
 
     steps = []
     cb = lambda k, xf, rel: steps.append({"outer": k, "true_rel_residual": rel,
                                           "map_err": map_error(xf, truth, hit)})
-    xm, tm = timed(lambda: run_pcg_mixed(rhs, x0, tv, pre, tol=tol))
-    out["mixed_jacobi"] = {"iters": xm.niter, "fp64_residuals": xm.outer, "wall_s": tm,
+    xm, tm, tmc = timed_warm(lambda: run_pcg_mixed(rhs, x0, tv, pre, tol=tol))
+    out["mixed_jacobi"] = {"iters": xm.niter, "fp64_residuals": xm.outer, "wall_s": tm, "cold_wall_s": tmc,
+                           "inner_step_ms": inner_step_ms(op32, rhs.maps[0].map.reshape(-1),
+                                                          pre.maps[0].map),
                            "true_rel_residual": xm.rel_residual,
                            "map_err": map_error(xm.maps[0].map, truth, hit)}
     run_pcg_mixed(rhs, x0, tv, pre, tol=tol, on_outer=cb)
@@ -136,8 +165,9 @@ def run(config: str = "c1", tol: float = 1e-6, learned: bool = True, pairs: int 
         t_train = time.perf_counter() - t2
         del R, E
         Mlearn = L.LearnedPrecon(hits.map, net, shape)
-        xl, tl = timed(lambda: run_pcg_mixed(rhs, x0, tv, pre, tol=tol, inner_precon=Mlearn))
-        xlf, tlf = timed(lambda: run_pcg(rhs, x0, tv, Mlearn, maxiter=5000, tol=tol, verbose=False))
+        xl, tl, tlc = timed_warm(lambda: run_pcg_mixed(rhs, x0, tv, pre, tol=tol, inner_precon=Mlearn))
+        xlf, tlf, tlfc = timed_warm(lambda: run_pcg(rhs, x0, tv, Mlearn, maxiter=5000, tol=tol,
+                                                    verbose=False))
         # held-out skies: iterations to tol, learned vs Jacobi (FP64 PCG)
         held = []
         for s in range(5):
@@ -149,9 +179,11 @@ def run(config: str = "c1", tol: float = 1e-6, learned: bool = True, pairs: int 
                           "train_s": t_train, "loss_first": hist_loss[0], "loss_last": hist_loss[-1],
                           "epochs": epochs, "held_out": held}
         out["mixed_learned"] = {"iters": xl.niter, "fp64_residuals": xl.outer, "wall_s": tl,
+                                "cold_wall_s": tlc,
+                                "inner_step_ms": inner_step_ms(op32, rhs.maps[0].map.reshape(-1), Mlearn),
                                 "true_rel_residual": xl.rel_residual,
                                 "map_err": map_error(xl.maps[0].map, truth, hit)}
-        out["learned_f64"] = {"iters": xlf.niter, "wall_s": tlf,
+        out["learned_f64"] = {"iters": xlf.niter, "wall_s": tlf, "cold_wall_s": tlfc,
                               "map_err": map_error(xlf.maps[0].map, truth, hit)}
         L.save(net, f"/tmp/mk_learned_{config}.npz")
     out["speedup_mixed_vs_jacobi_f64"] = tj / tm

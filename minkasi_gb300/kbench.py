@@ -171,6 +171,7 @@ def conv_bench(dev, hw: int = 2048, batch: int = 1, c: int = 16) -> dict:
         ms = best_ms(fn)
         res[name] = {"ms": ms, "TFLOPs": flops / ms / 1e9, "shape": [batch, c, hw, hw]}
     res["precon_small"] = precon_bench(dev)
+    res["precon_2048"] = precon_bench(dev, hw=2048)
     return res
 
 
