@@ -283,8 +283,12 @@ int mk_tod2map_fixed_noalloc(void *map, const void *dat, const int32_t *ipix, in
 
 /* Batched unnormalised DCT-I (FFTW REDFT00) of nrow rows of length n >= 2:
  * X_k = x_0 + (-1)^k x_{n-1} + 2 sum_{j=1}^{n-2} x_j cos(pi j k/(n-1)).
- * Computed as a batched cuFFT real-to-complex transform of the even
- * extension (length 2(n-1)); the real part of bins 0..n-1 is the DCT-I.
+ * The DCT-I is the real part of bins 0..n-1 of the DFT of the even
+ * extension (length 2(n-1)).  FP64 plans use a batched cuFFT real-to-complex
+ * transform of the extension.  FP32 plans whose 2(n-1) factors into 2, 3,
+ * 5, 7, 11 (every length minkasi's truncate_tod keeps) use this library's
+ * four-step shared-memory FFT: two kernels per DCT, two rows per complex
+ * transform, the extension formed while loading; other FP32 plans use cuFFT.
  * `in` and `out` are (nrow, n) dtype-typed and may alias.  The plan holds a
  * workspace of mk_dct1_workspace_bytes() bytes that the CALLER provides
  * (device pointer, 256-byte aligned) and keeps alive while the plan is used.
@@ -295,6 +299,14 @@ int mk_dct1_plan_create(mk_dct_plan **plan, int64_t nrow, int64_t n, int dtype,
                         void *workspace, size_t workspace_bytes);
 int mk_dct1_exec(mk_dct_plan *plan, const void *in, void *out, void *stream);
 int mk_dct1_plan_destroy(mk_dct_plan *plan);
+
+/* Transform for DCT / noise plans created after the call: engine 0
+ * (default) as described above, 1 = cuFFT for every plan (for comparisons).
+ * mk_dct1_engine / mk_noise_engine report what a plan uses (0 = four-step
+ * FFT, 1 = cuFFT). */
+int mk_set_dct_engine(int engine);
+int mk_get_dct_engine(void);
+int mk_dct1_engine(const mk_dct_plan *plan);
 
 /* NoiseSmoothedSVD.apply_noise, minkasi/mapmaking/noise.py:680-714:
  *   out = halve_ends( vT . DCT1( mywt[:, :ndata] * DCT1( v . dat ) ) )
@@ -315,6 +327,7 @@ int mk_noise_plan_create(mk_noise_plan **plan, int64_t ndet, int64_t ndata, int 
 int mk_apply_noise(mk_noise_plan *plan, const void *v, const void *vT, const void *mywt,
                    int64_t mywt_ld, const void *dat, void *out, int rot_mode, void *stream);
 int mk_noise_plan_destroy(mk_noise_plan *plan);
+int mk_noise_engine(const mk_noise_plan *plan);
 
 /* The detector rotation alone, R = A . X, for the plan's (ndet, ndata):
  * A (ndet, ndet), X and R (ndet, ndata), dtype-typed, R must not alias X.

@@ -83,6 +83,10 @@ SIGNATURES = {
     "mk_conv3x3_adj": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp]),
     "mk_conv3x3_wgrad_scratch_bytes": (_sz, [_i32, _i32, _i32, _i32, _i32]),
     "mk_conv3x3_wgrad": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _i32, _i32, _vp, _sz, _vp]),
+    "mk_set_dct_engine": (_i32, [_i32]),
+    "mk_get_dct_engine": (_i32, []),
+    "mk_dct1_engine": (_i32, [_vp]),
+    "mk_noise_engine": (_i32, [_vp]),
     "mk_learned_precon_work_bytes": (_sz, [_i32, _i32, _i32, _vp]),
     "mk_learned_precon_apply": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp, _sz, _i32, _vp]),
 }

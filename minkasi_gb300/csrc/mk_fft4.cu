@@ -1,0 +1,414 @@
+// FP32 DCT-I by a four-step FFT in shared memory (see mk_fft4.cuh).
+#include <cmath>
+#include <vector>
+
+#include "mk_common.cuh"
+#include "mk_fft4.cuh"
+
+namespace mk {
+namespace {
+
+constexpr int FB = 8;  // transforms per CTA (consecutive j1 in pass A, k2 in pass B)
+constexpr int NT = 256;
+constexpr int WR3 = 0, WR5 = 3, WR7 = 8, WR11 = 15, WRN = 26;  // offsets into the radix constants
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// -i z
+__device__ __forceinline__ float2 mul_mi(float2 z) { return make_float2(z.y, -z.x); }
+
+// forward DFT of R points in registers: v_q <- sum_r v_r W_R^{rq}
+template <int R>
+struct Dft;
+
+template <>
+struct Dft<2> {
+  __device__ static void run(float2 *v, const float2 *) {
+    const float2 a = v[0], b = v[1];
+    v[0] = cadd(a, b);
+    v[1] = csub(a, b);
+  }
+};
+
+template <>
+struct Dft<4> {
+  __device__ static void run(float2 *v, const float2 *) {
+    const float2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+    const float2 s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
+    v[0] = cadd(s02, s13);
+    v[2] = csub(s02, s13);
+    v[1] = cadd(d02, mul_mi(d13));
+    v[3] = csub(d02, mul_mi(d13));
+  }
+};
+
+template <>
+struct Dft<8> {
+  __device__ static void run(float2 *v, const float2 *) {
+    float2 e[4] = {v[0], v[2], v[4], v[6]}, o[4] = {v[1], v[3], v[5], v[7]};
+    Dft<4>::run(e, nullptr);
+    Dft<4>::run(o, nullptr);
+    const float h = 0.70710678118654752f;
+    // o_k *= W_8^k
+    o[1] = make_float2(h * (o[1].x + o[1].y), h * (o[1].y - o[1].x));
+    o[2] = mul_mi(o[2]);
+    o[3] = make_float2(h * (o[3].y - o[3].x), -h * (o[3].x + o[3].y));
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      v[k] = cadd(e[k], o[k]);
+      v[k + 4] = csub(e[k], o[k]);
+    }
+  }
+};
+
+// odd R: pair r with R - r; wr[t] = W_R^t = (cos 2pi t/R, -sin 2pi t/R)
+template <int R, int OFF>
+struct DftOdd {
+  __device__ static void run(float2 *v, const float2 *wr) {
+    constexpr int H = (R - 1) / 2;
+    float2 s[H + 1], d[H + 1];
+    float2 x0 = v[0];
+#pragma unroll
+    for (int r = 1; r <= H; r++) {
+      s[r] = cadd(v[r], v[R - r]);
+      d[r] = csub(v[r], v[R - r]);
+      x0 = cadd(x0, s[r]);
+    }
+    float2 out[R];
+    out[0] = x0;
+#pragma unroll
+    for (int q = 1; q <= H; q++) {
+      float2 A = v[0], B = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int r = 1; r <= H; r++) {
+        const float2 w = wr[OFF + (r * q) % R];
+        const float c = w.x, sn = -w.y;
+        A.x = fmaf(s[r].x, c, A.x);
+        A.y = fmaf(s[r].y, c, A.y);
+        B.x = fmaf(d[r].x, sn, B.x);
+        B.y = fmaf(d[r].y, sn, B.y);
+      }
+      out[q] = make_float2(A.x + B.y, A.y - B.x);
+      out[R - q] = make_float2(A.x - B.y, A.y + B.x);
+    }
+#pragma unroll
+    for (int q = 0; q < R; q++) v[q] = out[q];
+  }
+};
+template <>
+struct Dft<3> : DftOdd<3, WR3> {};
+template <>
+struct Dft<5> : DftOdd<5, WR5> {};
+template <>
+struct Dft<7> : DftOdd<7, WR7> {};
+template <>
+struct Dft<11> : DftOdd<11, WR11> {};
+
+// one in-place decimation-in-time stage of radix R over `nrows` transforms of
+// length Ls (row pitch `pitch`), after stages whose radices multiply to Ns
+template <int R>
+__device__ __forceinline__ void stage(float2 *buf, int pitch, int nrows, int Ls, int Ns, const float2 *tw,
+                                      const float2 *wr) {
+  const int nq = Ls / R, tstep = Ls / (Ns * R);
+  for (int bf = threadIdx.x; bf < nrows * nq; bf += NT) {
+    const int row = bf / nq, q = bf - row * nq;
+    const int g = q / Ns, k = q - g * Ns;
+    float2 *a = buf + row * pitch + g * Ns * R + k;
+    float2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) v[r] = a[r * Ns];
+    if (Ns > 1) {
+#pragma unroll
+      for (int r = 1; r < R; r++) v[r] = cmul(v[r], __ldg(tw + r * k * tstep));
+    }
+    Dft<R>::run(v, wr);
+#pragma unroll
+    for (int r = 0; r < R; r++) a[r * Ns] = v[r];
+  }
+}
+
+__device__ void run_stages(float2 *buf, int pitch, int nrows, int Ls, int nr, const int *rad, const float2 *tw,
+                           const float2 *wr) {
+  int Ns = 1;
+  for (int s = 0; s < nr; s++) {
+    const int R = rad[s];
+    switch (R) {
+      case 2: stage<2>(buf, pitch, nrows, Ls, Ns, tw, wr); break;
+      case 3: stage<3>(buf, pitch, nrows, Ls, Ns, tw, wr); break;
+      case 4: stage<4>(buf, pitch, nrows, Ls, Ns, tw, wr); break;
+      case 5: stage<5>(buf, pitch, nrows, Ls, Ns, tw, wr); break;
+      case 7: stage<7>(buf, pitch, nrows, Ls, Ns, tw, wr); break;
+      case 8: stage<8>(buf, pitch, nrows, Ls, Ns, tw, wr); break;
+      default: stage<11>(buf, pitch, nrows, Ls, Ns, tw, wr); break;
+    }
+    __syncthreads();
+    Ns *= R;
+  }
+}
+
+struct WrTable {
+  float2 w[WRN];
+};
+
+// pass A: rows (2 pair, 2 pair + 1) of x -> T[pair] (L1 x L2, twiddled)
+__global__ void __launch_bounds__(NT) k_fft4_a(const float *__restrict__ x, int64_t ldx, int64_t nrow,
+                                               float2 *__restrict__ T, const Fft4Dev p, const WrTable wt) {
+  extern __shared__ float2 sbuf[];
+  const int L1 = p.L1, L2 = p.L2, pitch = L2 + 1, tid = threadIdx.x;
+  const int64_t pair = blockIdx.y, r0 = 2 * pair;
+  const bool has2 = r0 + 1 < nrow;
+  const float *x1 = x + r0 * ldx;
+  const float *x2 = has2 ? x1 + ldx : x1;
+  const int j1_0 = blockIdx.x * FB;
+  const int nb = min(FB, L1 - j1_0);
+  for (int idx = tid; idx < FB * L2; idx += NT) {
+    const int b = idx % FB, j2 = idx / FB;
+    if (b < nb) {
+      const int64_t j = (int64_t)(j1_0 + b) + (int64_t)L1 * j2;
+      const int64_t jj = j <= p.m ? j : p.L - j;
+      float2 v;
+      v.x = __ldg(x1 + jj);
+      v.y = has2 ? __ldg(x2 + jj) : 0.f;
+      sbuf[b * pitch + __ldg(p.perm2 + j2)] = v;
+    }
+  }
+  __syncthreads();
+  run_stages(sbuf, pitch, nb, L2, p.nr2, p.r2, p.tw2, wt.w);
+  float2 *Tp = T + pair * p.L;
+  for (int idx = tid; idx < nb * L2; idx += NT) {
+    const int b = idx / L2, k2 = idx - b * L2;
+    const int64_t j1 = j1_0 + b;
+    const int64_t e = j1 * k2;
+    const float2 w = cmul(__ldg(p.twh + e / FFT4_TWS), __ldg(p.twl + e % FFT4_TWS));
+    Tp[j1 * L2 + k2] = cmul(sbuf[b * pitch + k2], w);
+  }
+}
+
+// pass B: T[pair] -> DCT rows 2 pair, 2 pair + 1 of out (k <= m), epilogue
+__global__ void __launch_bounds__(NT) k_fft4_b(const float2 *__restrict__ T, int64_t nrow, float *__restrict__ out,
+                                               int64_t ldo, const float *__restrict__ w, int64_t ldw, int epi,
+                                               const Fft4Dev p, const WrTable wt) {
+  extern __shared__ float2 sbuf[];
+  const int L1 = p.L1, L2 = p.L2, pitch = L1 + 1, tid = threadIdx.x;
+  const int64_t pair = blockIdx.y, r0 = 2 * pair;
+  const bool has2 = r0 + 1 < nrow;
+  const int k2_0 = blockIdx.x * FB;
+  const int nb = min(FB, L2 - k2_0);
+  const float2 *Tp = T + pair * p.L;
+  for (int idx = tid; idx < FB * L1; idx += NT) {
+    const int b = idx % FB, j1 = idx / FB;
+    if (b < nb) sbuf[b * pitch + __ldg(p.perm1 + j1)] = Tp[(int64_t)j1 * L2 + k2_0 + b];
+  }
+  __syncthreads();
+  run_stages(sbuf, pitch, nb, L1, p.nr1, p.r1, p.tw1, wt.w);
+  float *o1 = out + r0 * ldo;
+  float *o2 = o1 + ldo;
+  const float *w1 = epi == FFT4_FILTER ? w + r0 * ldw : nullptr;
+  const float *w2 = epi == FFT4_FILTER ? w1 + ldw : nullptr;
+  for (int idx = tid; idx < FB * L1; idx += NT) {
+    const int b = idx % FB, k1 = idx / FB;
+    if (b >= nb) continue;
+    const int64_t k = k2_0 + b + (int64_t)L2 * k1;
+    if (k > p.m) continue;
+    const float2 F = sbuf[b * pitch + k1];
+    float a = F.x, c = F.y;
+    if (epi == FFT4_FILTER) {
+      a *= __ldcs(w1 + k);
+      if (has2) c *= __ldcs(w2 + k);
+    } else if (epi == FFT4_HALVE && (k == 0 || k == p.m)) {
+      a *= 0.5f;
+      c *= 0.5f;
+    }
+    o1[k] = a;
+    if (has2) o2[k] = c;
+  }
+}
+
+void factor(int64_t L, std::vector<int> &f) {
+  for (int pr : {2, 3, 5, 7, 11})
+    while (L % pr == 0) {
+      f.push_back(pr);
+      L /= pr;
+    }
+  if (L != 1) f.clear();
+}
+
+// radices of a transform of length Ls (a product of 2, 3, 5, 7, 11)
+bool radices(int Ls, int *r, int *nr) {
+  std::vector<int> f;
+  factor(Ls, f);
+  if (f.empty() && Ls != 1) return false;
+  int n2 = 0;
+  std::vector<int> out;
+  for (int x : f) n2 += x == 2;
+  for (; n2 >= 3; n2 -= 3) out.push_back(8);
+  if (n2 == 2) out.push_back(4);
+  if (n2 == 1) out.push_back(2);
+  for (int x : f)
+    if (x != 2) out.push_back(x);
+  if ((int)out.size() > FFT4_MAXR) return false;
+  for (size_t i = 0; i < out.size(); i++) r[i] = out[i];
+  *nr = (int)out.size();
+  return true;
+}
+
+size_t al(size_t x) { return (x + 255) / 256 * 256; }
+
+struct TableLayout {
+  size_t tw1, tw2, perm1, perm2, twl, twh, total;
+};
+
+TableLayout layout(const Fft4Dev &d) {
+  TableLayout t;
+  size_t o = 0;
+  t.tw1 = o;
+  o += al((size_t)d.L1 * sizeof(float2));
+  t.tw2 = o;
+  o += al((size_t)d.L2 * sizeof(float2));
+  t.perm1 = o;
+  o += al((size_t)d.L1 * sizeof(int));
+  t.perm2 = o;
+  o += al((size_t)d.L2 * sizeof(int));
+  t.twl = o;
+  o += al((size_t)FFT4_TWS * sizeof(float2));
+  t.twh = o;
+  o += al((size_t)((d.L + FFT4_TWS - 1) / FFT4_TWS) * sizeof(float2));
+  t.total = o;
+  return t;
+}
+
+float2 unit(double num, double den) {
+  // exp(-2 pi i num / den) in double, rounded
+  const double a = 2.0 * M_PI * num / den;
+  return make_float2((float)std::cos(a), (float)-std::sin(a));
+}
+
+void digit_rev(int Ls, const int *r, int nr, int *P) {
+  std::vector<int> d(nr > 0 ? nr : 1);
+  for (int j = 0; j < Ls; j++) {
+    int q = j;
+    for (int i = nr - 1; i >= 0; i--) {
+      d[i] = q % r[i];
+      q /= r[i];
+    }
+    int pos = 0, span = 1;
+    for (int i = 0; i < nr; i++) {
+      pos += d[i] * span;
+      span *= r[i];
+    }
+    P[j] = pos;
+  }
+}
+
+WrTable radix_constants() {
+  WrTable t;
+  const int rs[4] = {3, 5, 7, 11}, off[4] = {WR3, WR5, WR7, WR11};
+  for (int i = 0; i < 4; i++)
+    for (int k = 0; k < rs[i]; k++) t.w[off[i] + k] = unit(k, rs[i]);
+  return t;
+}
+
+bool g_attr[64] = {false};
+
+}  // namespace
+
+bool fft4_shape(int64_t n, Fft4Dev *d) {
+  if (n < 2) return false;
+  const int64_t m = n - 1, L = 2 * m;
+  std::vector<int> f;
+  factor(L, f);
+  if (f.empty()) return false;
+  // divisors of L; the one closest to sqrt(L) with both parts <= LMAX
+  std::vector<int64_t> ds{1};
+  for (int pr : f) {
+    const size_t k = ds.size();
+    for (size_t i = 0; i < k; i++) {
+      const int64_t v = ds[i] * pr;
+      bool seen = false;
+      for (int64_t u : ds) seen |= (u == v);
+      if (!seen) ds.push_back(v);
+    }
+  }
+  int64_t best = -1;
+  double bc = 1e300;
+  for (int64_t a : ds) {
+    const int64_t b = L / a;
+    if (a > FFT4_LMAX || b > FFT4_LMAX) continue;
+    const double c = std::fabs(std::log((double)a) - std::log((double)b));
+    if (c < bc) {
+      bc = c;
+      best = a;
+    }
+  }
+  if (best < 0) return false;
+  Fft4Dev t{};
+  t.n = n;
+  t.m = m;
+  t.L = L;
+  t.L1 = (int)best;
+  t.L2 = (int)(L / best);
+  if (!radices(t.L1, t.r1, &t.nr1) || !radices(t.L2, t.r2, &t.nr2)) return false;
+  *d = t;
+  return true;
+}
+
+size_t fft4_table_bytes(const Fft4Dev &d) { return layout(d).total; }
+
+size_t fft4_t_bytes(const Fft4Dev &d, int64_t nrow) {
+  return (size_t)((nrow + 1) / 2) * (size_t)d.L * sizeof(float2);
+}
+
+int fft4_init(Fft4Plan *p, int64_t n, void *dev_tables) {
+  MK_CHECK_ARG(fft4_shape(n, &p->d), "fft4: row length %lld has no supported factorisation", (long long)n);
+  Fft4Dev &d = p->d;
+  const TableLayout t = layout(d);
+  std::vector<char> h(t.total, 0);
+  float2 *tw1 = (float2 *)(h.data() + t.tw1), *tw2 = (float2 *)(h.data() + t.tw2);
+  float2 *twl = (float2 *)(h.data() + t.twl), *twh = (float2 *)(h.data() + t.twh);
+  for (int i = 0; i < d.L1; i++) tw1[i] = unit(i, d.L1);
+  for (int i = 0; i < d.L2; i++) tw2[i] = unit(i, d.L2);
+  digit_rev(d.L1, d.r1, d.nr1, (int *)(h.data() + t.perm1));
+  digit_rev(d.L2, d.r2, d.nr2, (int *)(h.data() + t.perm2));
+  for (int i = 0; i < FFT4_TWS; i++) twl[i] = unit(i, (double)d.L);
+  for (int64_t i = 0; i < (d.L + FFT4_TWS - 1) / FFT4_TWS; i++)
+    twh[i] = unit((double)(i * FFT4_TWS % d.L), (double)d.L);
+  MK_CUDA(cudaMemcpy(dev_tables, h.data(), t.total, cudaMemcpyHostToDevice));
+  char *b = (char *)dev_tables;
+  d.tw1 = (const float2 *)(b + t.tw1);
+  d.tw2 = (const float2 *)(b + t.tw2);
+  d.perm1 = (const int *)(b + t.perm1);
+  d.perm2 = (const int *)(b + t.perm2);
+  d.twl = (const float2 *)(b + t.twl);
+  d.twh = (const float2 *)(b + t.twh);
+  p->tables = dev_tables;
+  return MK_OK;
+}
+
+int fft4_dct(const Fft4Plan &p, const float *x, int64_t ldx, int64_t nrow, float2 *T, float *out, int64_t ldo,
+             int epi, const float *w, int64_t ldw, cudaStream_t st) {
+  const Fft4Dev &d = p.d;
+  const int64_t npairs = (nrow + 1) / 2;
+  MK_CHECK_ARG(npairs >= 1 && npairs <= 65535, "fft4: %lld rows out of range", (long long)nrow);
+  MK_CHECK_ARG(ldx >= d.n && ldo >= d.n, "fft4: leading dimensions below the row length");
+  MK_CHECK_ARG(epi != FFT4_FILTER || (w && ldw >= d.n), "fft4: filter weights missing");
+  int dev = 0;
+  MK_CUDA(cudaGetDevice(&dev));
+  if (dev >= 0 && dev < 64 && !g_attr[dev]) {
+    const int mx = FB * (FFT4_LMAX + 1) * (int)sizeof(float2);
+    MK_CUDA(cudaFuncSetAttribute(k_fft4_a, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    MK_CUDA(cudaFuncSetAttribute(k_fft4_b, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    g_attr[dev] = true;
+  }
+  static const WrTable wt = radix_constants();
+  const dim3 ga((d.L1 + FB - 1) / FB, (unsigned)npairs), gb((d.L2 + FB - 1) / FB, (unsigned)npairs);
+  k_fft4_a<<<ga, NT, (size_t)FB * (d.L2 + 1) * sizeof(float2), st>>>(x, ldx, nrow, T, d, wt);
+  int rc = launch_status("fft4 pass A");
+  if (rc) return rc;
+  k_fft4_b<<<gb, NT, (size_t)FB * (d.L1 + 1) * sizeof(float2), st>>>(T, nrow, out, ldo, w, ldw, epi, d, wt);
+  return launch_status("fft4 pass B");
+}
+
+}  // namespace mk

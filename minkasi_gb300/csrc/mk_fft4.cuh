@@ -1,0 +1,61 @@
+// FP32 DCT-I of detector rows by a four-step FFT in shared memory.
+//
+// DCT-I of a row x (length n = m + 1) is the DFT of its even extension
+// e_j = x_{min(j, 2m - j)} (length L = 2m), which is real.  Two rows r, r+1
+// therefore share one complex transform: F = DFT(e_r + i e_{r+1}) gives
+// DCT(x_r)_k = Re F_k and DCT(x_{r+1})_k = Im F_k, k = 0..m.
+//
+// With L = L1 L2 (both <= FFT4_LMAX, factors in {2,3,5,7,11}), j = j1 + L1 j2
+// and k = k2 + L2 k1:
+//   pass A: for each j1, T[j1][k2] = W_L^{j1 k2} sum_j2 e_{j1 + L1 j2} W_L2^{j2 k2}
+//   pass B: for each k2, F[k2 + L2 k1] = sum_j1 T[j1][k2] W_L1^{j1 k1}
+// Each CTA runs 8 transforms of one pass in shared memory (mixed-radix
+// decimation in time, input placed in digit-reversed order, butterflies in
+// place).  Pass A forms the even extension while loading; pass B writes only
+// k <= m and applies the epilogue (plain, times the inverse-spectrum weights,
+// or with columns 0 and m halved).  Twiddles come from tables computed in
+// double precision on the host.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mk {
+
+constexpr int FFT4_LMAX = 2048;  // longest transform of one pass
+constexpr int FFT4_MAXR = 16;    // most radix stages of one pass
+constexpr int FFT4_TWS = 2048;   // split of the four-step twiddle exponent
+
+// device view of a plan (kernel argument)
+struct Fft4Dev {
+  int64_t n, m, L;
+  int L1, L2;
+  int nr1, nr2;
+  int r1[FFT4_MAXR], r2[FFT4_MAXR];
+  const float2 *tw1, *tw2;  // W_L1^t, W_L2^t
+  const int *perm1, *perm2;  // digit-reversed positions
+  const float2 *twh, *twl;  // W_L^(t * TWS), W_L^t (t < TWS)
+};
+
+// epilogues of pass B
+enum { FFT4_PLAIN = 0, FFT4_FILTER = 1, FFT4_HALVE = 2 };
+
+struct Fft4Plan {
+  Fft4Dev d{};
+  void *tables = nullptr;  // device tables inside the caller's workspace
+};
+
+// Split of L = 2(n-1) into L1 x L2, radix lists; false when L has a prime
+// factor above 11 or cannot be split within FFT4_LMAX.
+bool fft4_shape(int64_t n, Fft4Dev *d);
+// bytes of the device tables for that shape
+size_t fft4_table_bytes(const Fft4Dev &d);
+// bytes of the intermediate T for nrow rows
+size_t fft4_t_bytes(const Fft4Dev &d, int64_t nrow);
+// computes the tables on the host and uploads them to `dev_tables`
+int fft4_init(Fft4Plan *p, int64_t n, void *dev_tables);
+// out rows (ld ldo) = DCT-I of x rows (ld ldx) with the given epilogue;
+// T is scratch of fft4_t_bytes; w (ld ldw) only for FFT4_FILTER.
+int fft4_dct(const Fft4Plan &p, const float *x, int64_t ldx, int64_t nrow, float2 *T, float *out,
+             int64_t ldo, int epi, const float *w, int64_t ldw, cudaStream_t st);
+
+}  // namespace mk

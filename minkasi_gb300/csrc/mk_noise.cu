@@ -21,13 +21,22 @@
 // (rot_mode 2) the mirror is written by the first rotation's epilogue and the
 // second rotation reads Re F in place and halves while splitting, so k_mirror
 // and k_real_halve do not run.
+//
+// FP32 plans whose length factors into 2, 3, 5, 7, 11 (every length the
+// reference's truncation produces) use the four-step shared-memory FFT of
+// mk_fft4.cu instead of cuFFT:  E = v . dat;  E = DCT(E) * mywt;
+// E = DCT(E) with columns 0 and n-1 halved;  out = vT . E.  Each DCT is two
+// kernels that form the even extension while loading and apply the weights
+// or the halving while storing, two detector rows per complex transform.
 #include <cublas_v2.h>
 #include <cufft.h>
 
+#include <atomic>
 #include <mutex>
 #include <new>
 
 #include "mk_common.cuh"
+#include "mk_fft4.cuh"
 #include "mk_rot.cuh"
 
 namespace {
@@ -131,9 +140,15 @@ dim3 rows_grid(int64_t n, int64_t nrow) {
 }
 
 // ---- plan object -----------------------------------------------------------
+// 0: four-step FFT for FP32 where the length allows, cuFFT otherwise; 1: cuFFT
+std::atomic<int> g_engine{0};
+
 struct DctCore {
   cufftHandle fft = 0;
   bool have_fft = false;
+  bool own = false;  // four-step FFT (FP32)
+  mk::Fft4Plan f4;
+  float2 *T = nullptr;
   int64_t nrow = 0, n = 0, N = 0;
   int dtype = MK_F64;
   void *E = nullptr, *F = nullptr, *work = nullptr;
@@ -169,11 +184,21 @@ int make_fft(cufftHandle *h, int64_t nrow, int64_t N, int dtype, size_t *work) {
   return MK_OK;
 }
 
+bool use_own(int64_t nrow, int64_t n, int dtype, mk::Fft4Dev *d) {
+  return dtype == MK_F32 && g_engine.load() == 0 && (nrow + 1) / 2 <= 65535 && mk::fft4_shape(n, d);
+}
+
 int core_bytes(int64_t nrow, int64_t n, int dtype, size_t *bytes) {
   MK_CHECK_ARG(bytes, "workspace size: null output");
   MK_CHECK_ARG(MK_DTYPE_OK(dtype), "workspace size: bad dtype %d", dtype);
   MK_CHECK_ARG(nrow >= 1 && n >= 2, "DCT-I needs nrow >= 1 and n >= 2 (got %lld, %lld)",
                (long long)nrow, (long long)n);
+  mk::Fft4Dev d;
+  if (use_own(nrow, n, dtype, &d)) {
+    *bytes = align_up((size_t)nrow * n * sizeof(float)) + align_up(mk::fft4_t_bytes(d, nrow)) +
+             align_up(mk::fft4_table_bytes(d)) + tc_bytes(nrow, dtype);
+    return MK_OK;
+  }
   int64_t N = 2 * (n - 1);
   cufftHandle h;
   size_t work = 0;
@@ -196,6 +221,23 @@ int core_create(DctCore *c, int64_t nrow, int64_t n, int dtype, void *ws, size_t
   c->N = 2 * (n - 1);
   c->dtype = dtype;
   char *p = (char *)ws;
+  mk::Fft4Dev d;
+  if (use_own(nrow, n, dtype, &d)) {
+    c->own = true;
+    c->E = p;
+    p += align_up((size_t)nrow * n * sizeof(float));
+    c->T = (float2 *)p;
+    p += align_up(mk::fft4_t_bytes(d, nrow));
+    rc = mk::fft4_init(&c->f4, n, p);
+    if (rc) return rc;
+    p += align_up(mk::fft4_table_bytes(d));
+    if (tc_bytes(nrow, dtype)) {
+      c->tc_err = (int *)p;
+      c->tc_bimg = p + 256;
+      MK_CUDA(cudaMemset(c->tc_err, 0, sizeof(int)));
+    }
+    return MK_OK;
+  }
   c->E = p;
   p += align_up((size_t)nrow * c->N * elt(dtype));
   c->F = p;
@@ -236,6 +278,9 @@ int core_fft(DctCore *c, cudaStream_t st) {
 
 template <typename T, typename C>
 int dct_exec_t(DctCore *c, const void *in, void *out, cudaStream_t st) {
+  if (c->own)
+    return mk::fft4_dct(c->f4, (const float *)in, c->n, c->nrow, c->T, (float *)out, c->n, mk::FFT4_PLAIN,
+                        nullptr, 0, st);
   dim3 g = rows_grid(c->n, c->nrow);
   k_extend<T><<<g, 256, 0, st>>>((const T *)in, c->n, (T *)c->E, c->n, c->N, c->nrow);
   int rc = mk::launch_status("mk_dct1_exec/extend");
@@ -334,8 +379,16 @@ int apply_noise_t(DctCore *c, const T *v, const T *vT, const T *w, int64_t ldw, 
                   T *out, int rot_mode, cudaStream_t st) {
   const int64_t n = c->n, N = c->N, nd = c->nrow;
   dim3 g = rows_grid(n, nd);
+  int rc;
+  if (c->own) {
+    float *E = (float *)c->E;
+    if ((rc = rotate(c, rot_mode, v, dat, n, E, n, nd, n, st))) return rc;
+    if ((rc = mk::fft4_dct(c->f4, E, n, nd, c->T, E, n, mk::FFT4_FILTER, (const float *)w, ldw, st))) return rc;
+    if ((rc = mk::fft4_dct(c->f4, E, n, nd, c->T, E, n, mk::FFT4_HALVE, nullptr, 0, st))) return rc;
+    return rotate(c, rot_mode, vT, E, n, out, n, nd, n, st);
+  }
   const bool fused_mirror = (rot_mode == 2);  // the tensor-core epilogue writes the extension
-  int rc = rotate(c, rot_mode, v, dat, n, c->E, N, nd, n, st, fused_mirror ? N : 0);
+  rc = rotate(c, rot_mode, v, dat, n, c->E, N, nd, n, st, fused_mirror ? N : 0);
   if (rc) return rc;
   if (!fused_mirror) {
     k_mirror<T><<<g, 256, 0, st>>>((T *)c->E, n, N, nd);
@@ -458,3 +511,15 @@ extern "C" int mk_noise_status(mk_noise_plan *plan, int *code, void *stream) {
   MK_CUDA(cudaStreamSynchronize(st));
   return MK_OK;
 }
+
+extern "C" int mk_set_dct_engine(int engine) {
+  MK_CHECK_ARG(engine == 0 || engine == 1, "mk_set_dct_engine: engine must be 0 or 1 (got %d)", engine);
+  g_engine.store(engine);
+  return MK_OK;
+}
+
+extern "C" int mk_get_dct_engine(void) { return g_engine.load(); }
+
+extern "C" int mk_dct1_engine(const mk_dct_plan *plan) { return plan && plan->core.own ? 0 : 1; }
+
+extern "C" int mk_noise_engine(const mk_noise_plan *plan) { return plan && plan->core.own ? 0 : 1; }

@@ -380,6 +380,17 @@ def _workspace(nbytes: int, device) -> torch.Tensor:
     return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
 
 
+def set_dct_engine(engine: int) -> None:
+    """Transform used by DCT / noise plans created from now on: 0 (default)
+    the four-step shared-memory FFT for FP32 rows whose length factors into
+    2, 3, 5, 7, 11, cuFFT otherwise; 1 cuFFT always."""
+    check(lib().mk_set_dct_engine(int(engine)), "set_dct_engine")
+
+
+def dct_engine() -> int:
+    return int(lib().mk_get_dct_engine())
+
+
 class DCT1:
     """Batched unnormalised DCT-I (REDFT00) of (nrow, n) arrays."""
 
@@ -405,6 +416,11 @@ class DCT1:
             out = torch.empty_like(x)
         check(lib().mk_dct1_exec(self._h, _p(x), _p(out), _stream()), "dct1")
         return out
+
+    @property
+    def engine(self) -> int:
+        """0: four-step FFT, 1: cuFFT."""
+        return int(lib().mk_dct1_engine(self._h))
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -439,6 +455,11 @@ class NoisePlan:
         check(lib().mk_noise_plan_create(ctypes.byref(h), self.ndet, self.ndata, _DT[dtype],
                                          _p(self.ws), self.ws.numel()), "noise plan")
         self._h = h
+
+    @property
+    def engine(self) -> int:
+        """0: four-step FFT, 1: cuFFT."""
+        return int(lib().mk_noise_engine(self._h))
 
     def rotate(self, A: torch.Tensor, X: torch.Tensor, out: Optional[torch.Tensor] = None,
                rot_mode: int = 0) -> torch.Tensor:

@@ -193,6 +193,42 @@ def test_dct1_f32_and_roundtrip(K):
     assert rel(back, x) < 2e-6
 
 
+@pytest.mark.parametrize("nrow,n", [(1, 2), (1, 3), (2, 5), (3, 13), (4, 100), (5, 331), (2, 4097),
+                                    (16, 2311), (9, 694), (8, 600001), (256, 130978)])
+def test_dct1_f32_four_step(K, nrow, n):
+    """FP32 DCT-I through the four-step FFT (every 2(n-1) here factors into
+    2, 3, 5, 7, 11; odd nrow leaves the last row pair half empty) against the
+    FP64 oracle."""
+    x = np.random.default_rng(n).standard_normal((nrow, n))
+    d = K.DCT1(nrow, n, torch.float32)
+    assert d.engine == 0
+    y = d(dev(x, torch.float32)).cpu().numpy()
+    ref = oracle.dct1(x)
+    assert rel(y, ref) < 3e-6
+    assert np.linalg.norm(y - ref) < 2e-6 * np.linalg.norm(ref)
+
+
+def test_dct1_engines_agree_and_fall_back(K):
+    x = np.random.default_rng(9).standard_normal((6, 2311))
+    own = K.DCT1(6, 2311, torch.float32)(dev(x, torch.float32)).cpu().numpy()
+    try:
+        K.set_dct_engine(1)
+        assert K.dct_engine() == 1
+        d = K.DCT1(6, 2311, torch.float32)
+        assert d.engine == 1
+        ref = d(dev(x, torch.float32)).cpu().numpy()
+    finally:
+        K.set_dct_engine(0)
+    assert rel(own, ref) < 3e-6
+    # 2(n-1) = 2 * 27 * 37 has a factor above 11: cuFFT
+    x = np.random.default_rng(10).standard_normal((3, 1000))
+    d = K.DCT1(3, 1000, torch.float32)
+    assert d.engine == 1
+    assert rel(d(dev(x, torch.float32)).cpu().numpy(), oracle.dct1(x)) < 3e-6
+    with pytest.raises(Exception):
+        K.set_dct_engine(2)
+
+
 def test_apply_noise_golden_f64(K, gold):
     g = gold("noise.npz")
     v, vT, w = dev(g["v"]), dev(g["vT"]), dev(g["mywt"])
@@ -219,13 +255,24 @@ def test_apply_noise_prewhitened_by_folding(K, gold):
     assert rel(dd, g["pw_dd"]) < 1e-12
 
 
-def test_apply_noise_f32_close_to_f64(K, gold):
+@pytest.mark.parametrize("engine", [0, 1])
+def test_apply_noise_f32_close_to_f64(K, gold, engine):
     g = gold("noise.npz")
-    x = g["x"]
-    plan = K.NoisePlan(x.shape[0], x.shape[1], torch.float32)
-    dd = plan.apply(dev(g["v"], torch.float32), dev(g["vT"], torch.float32),
-                    dev(g["mywt"], torch.float32), dev(x, torch.float32), rot_mode=1).cpu().numpy()
-    assert rel(dd, g["dd"]) < 1e-5
+    try:
+        K.set_dct_engine(engine)
+        for key_x, key_dd in (("x", "dd"), ("x_short", "dd_short")):
+            x = g[key_x]
+            plan = K.NoisePlan(x.shape[0], x.shape[1], torch.float32)
+            dd = plan.apply(dev(g["v"], torch.float32), dev(g["vT"], torch.float32),
+                            dev(g["mywt"], torch.float32), dev(x, torch.float32), rot_mode=1)
+            assert rel(dd.cpu().numpy(), g[key_dd]) < 1e-5, (engine, key_x, plan.engine)
+            # in place
+            xx = dev(x, torch.float32)
+            plan.apply(dev(g["v"], torch.float32), dev(g["vT"], torch.float32),
+                       dev(g["mywt"], torch.float32), xx, out=xx, rot_mode=1)
+            assert torch.equal(xx, dd)
+    finally:
+        K.set_dct_engine(0)
 
 
 # ---------------------------------------------------------------- map algebra / PCG
