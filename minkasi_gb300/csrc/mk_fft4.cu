@@ -107,16 +107,18 @@ struct Dft<7> : DftOdd<7, WR7> {};
 template <>
 struct Dft<11> : DftOdd<11, WR11> {};
 
-// one in-place decimation-in-time stage of radix R over `nrows` transforms of
-// length Ls (row pitch `pitch`), after stages whose radices multiply to Ns
+// one in-place decimation-in-time stage of radix R over one transform of
+// length Ls held by a warp, after stages whose radices multiply to Ns
 template <int R>
-__device__ __forceinline__ void stage(float2 *buf, int pitch, int nrows, int Ls, int Ns, const float2 *tw,
-                                      const float2 *wr) {
-  const int nq = Ls / R, tstep = Ls / (Ns * R);
-  for (int bf = threadIdx.x; bf < nrows * nq; bf += NT) {
-    const int row = bf / nq, q = bf - row * nq;
-    const int g = q / Ns, k = q - g * Ns;
-    float2 *a = buf + row * pitch + g * Ns * R + k;
+__device__ __forceinline__ void stage(float2 *row, int Ls, int Ns, int tstep, float invNs, const float2 *tw,
+                                     const float2 *wr, int lane) {
+  const int nq = Ls / R;
+  for (int q = lane; q < nq; q += 32) {
+    // q / Ns exactly: q, Ns <= 2048, so (q + 1/2) / Ns is at least 1/(2 Ns)
+    // from an integer, far above the FP32 rounding of the product
+    const int g = __float2int_rz(((float)q + 0.5f) * invNs);
+    const int k = q - g * Ns;
+    float2 *a = row + g * Ns * R + k;
     float2 v[R];
 #pragma unroll
     for (int r = 0; r < R; r++) v[r] = a[r * Ns];
@@ -130,22 +132,22 @@ __device__ __forceinline__ void stage(float2 *buf, int pitch, int nrows, int Ls,
   }
 }
 
-__device__ void run_stages(float2 *buf, int pitch, int nrows, int Ls, int nr, const int *rad, const float2 *tw,
-                           const float2 *wr) {
-  int Ns = 1;
+// all stages of one transform (the calling warp's row)
+__device__ void run_stages(float2 *row, int Ls, int nr, const int *rad, const int *ns, const int *ts,
+                           const float *inv, const float2 *tw, const float2 *wr, int lane) {
   for (int s = 0; s < nr; s++) {
-    const int R = rad[s];
+    const int R = rad[s], Ns = ns[s], tstep = ts[s];
+    const float iv = inv[s];
     switch (R) {
-      case 2: stage<2>(buf, pitch, nrows, Ls, Ns, tw, wr); break;
-      case 3: stage<3>(buf, pitch, nrows, Ls, Ns, tw, wr); break;
-      case 4: stage<4>(buf, pitch, nrows, Ls, Ns, tw, wr); break;
-      case 5: stage<5>(buf, pitch, nrows, Ls, Ns, tw, wr); break;
-      case 7: stage<7>(buf, pitch, nrows, Ls, Ns, tw, wr); break;
-      case 8: stage<8>(buf, pitch, nrows, Ls, Ns, tw, wr); break;
-      default: stage<11>(buf, pitch, nrows, Ls, Ns, tw, wr); break;
+      case 2: stage<2>(row, Ls, Ns, tstep, iv, tw, wr, lane); break;
+      case 3: stage<3>(row, Ls, Ns, tstep, iv, tw, wr, lane); break;
+      case 4: stage<4>(row, Ls, Ns, tstep, iv, tw, wr, lane); break;
+      case 5: stage<5>(row, Ls, Ns, tstep, iv, tw, wr, lane); break;
+      case 7: stage<7>(row, Ls, Ns, tstep, iv, tw, wr, lane); break;
+      case 8: stage<8>(row, Ls, Ns, tstep, iv, tw, wr, lane); break;
+      default: stage<11>(row, Ls, Ns, tstep, iv, tw, wr, lane); break;
     }
-    __syncthreads();
-    Ns *= R;
+    __syncwarp();
   }
 }
 
@@ -164,11 +166,12 @@ __global__ void __launch_bounds__(NT) k_fft4_a(const float *__restrict__ x, int6
   const float *x2 = has2 ? x1 + ldx : x1;
   const int j1_0 = blockIdx.x * FB;
   const int nb = min(FB, L1 - j1_0);
+  const int m = (int)p.m, L = (int)p.L;
   for (int idx = tid; idx < FB * L2; idx += NT) {
     const int b = idx % FB, j2 = idx / FB;
     if (b < nb) {
-      const int64_t j = (int64_t)(j1_0 + b) + (int64_t)L1 * j2;
-      const int64_t jj = j <= p.m ? j : p.L - j;
+      const int j = j1_0 + b + L1 * j2;
+      const int jj = j <= m ? j : L - j;
       float2 v;
       v.x = __ldg(x1 + jj);
       v.y = has2 ? __ldg(x2 + jj) : 0.f;
@@ -176,12 +179,15 @@ __global__ void __launch_bounds__(NT) k_fft4_a(const float *__restrict__ x, int6
     }
   }
   __syncthreads();
-  run_stages(sbuf, pitch, nb, L2, p.nr2, p.r2, p.tw2, wt.w);
+  const int warp = tid >> 5, lane = tid & 31;
+  if (warp < nb)
+    run_stages(sbuf + warp * pitch, L2, p.nr2, p.r2, p.ns2, p.ts2, p.inv2, p.tw2, wt.w, lane);
+  __syncthreads();
   float2 *Tp = T + pair * p.L;
   for (int idx = tid; idx < nb * L2; idx += NT) {
     const int b = idx / L2, k2 = idx - b * L2;
-    const int64_t j1 = j1_0 + b;
-    const int64_t e = j1 * k2;
+    const int j1 = j1_0 + b;
+    const int e = j1 * k2;
     const float2 w = cmul(__ldg(p.twh + e / FFT4_TWS), __ldg(p.twl + e % FFT4_TWS));
     Tp[j1 * L2 + k2] = cmul(sbuf[b * pitch + k2], w);
   }
@@ -200,25 +206,29 @@ __global__ void __launch_bounds__(NT) k_fft4_b(const float2 *__restrict__ T, int
   const float2 *Tp = T + pair * p.L;
   for (int idx = tid; idx < FB * L1; idx += NT) {
     const int b = idx % FB, j1 = idx / FB;
-    if (b < nb) sbuf[b * pitch + __ldg(p.perm1 + j1)] = Tp[(int64_t)j1 * L2 + k2_0 + b];
+    if (b < nb) sbuf[b * pitch + __ldg(p.perm1 + j1)] = Tp[j1 * L2 + k2_0 + b];
   }
   __syncthreads();
-  run_stages(sbuf, pitch, nb, L1, p.nr1, p.r1, p.tw1, wt.w);
+  const int warp = tid >> 5, lane = tid & 31;
+  if (warp < nb)
+    run_stages(sbuf + warp * pitch, L1, p.nr1, p.r1, p.ns1, p.ts1, p.inv1, p.tw1, wt.w, lane);
+  __syncthreads();
   float *o1 = out + r0 * ldo;
   float *o2 = o1 + ldo;
   const float *w1 = epi == FFT4_FILTER ? w + r0 * ldw : nullptr;
   const float *w2 = epi == FFT4_FILTER ? w1 + ldw : nullptr;
+  const int m = (int)p.m;
   for (int idx = tid; idx < FB * L1; idx += NT) {
     const int b = idx % FB, k1 = idx / FB;
     if (b >= nb) continue;
-    const int64_t k = k2_0 + b + (int64_t)L2 * k1;
-    if (k > p.m) continue;
+    const int k = k2_0 + b + L2 * k1;
+    if (k > m) continue;
     const float2 F = sbuf[b * pitch + k1];
     float a = F.x, c = F.y;
     if (epi == FFT4_FILTER) {
       a *= __ldcs(w1 + k);
       if (has2) c *= __ldcs(w2 + k);
-    } else if (epi == FFT4_HALVE && (k == 0 || k == p.m)) {
+    } else if (epi == FFT4_HALVE && (k == 0 || k == m)) {
       a *= 0.5f;
       c *= 0.5f;
     }
@@ -316,7 +326,7 @@ bool g_attr[64] = {false};
 }  // namespace
 
 bool fft4_shape(int64_t n, Fft4Dev *d) {
-  if (n < 2) return false;
+  if (n < 2 || n > (int64_t)FFT4_LMAX * FFT4_LMAX / 2) return false;
   const int64_t m = n - 1, L = 2 * m;
   std::vector<int> f;
   factor(L, f);
@@ -351,6 +361,19 @@ bool fft4_shape(int64_t n, Fft4Dev *d) {
   t.L1 = (int)best;
   t.L2 = (int)(L / best);
   if (!radices(t.L1, t.r1, &t.nr1) || !radices(t.L2, t.r2, &t.nr2)) return false;
+  for (int pass = 0; pass < 2; pass++) {
+    const int Ls = pass ? t.L2 : t.L1, nr = pass ? t.nr2 : t.nr1;
+    const int *r = pass ? t.r2 : t.r1;
+    int *ns = pass ? t.ns2 : t.ns1, *ts = pass ? t.ts2 : t.ts1;
+    float *inv = pass ? t.inv2 : t.inv1;
+    int span = 1;
+    for (int s = 0; s < nr; s++) {
+      ns[s] = span;
+      ts[s] = Ls / (span * r[s]);
+      inv[s] = 1.0f / (float)span;
+      span *= r[s];
+    }
+  }
   *d = t;
   return true;
 }

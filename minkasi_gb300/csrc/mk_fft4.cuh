@@ -9,11 +9,12 @@
 // and k = k2 + L2 k1:
 //   pass A: for each j1, T[j1][k2] = W_L^{j1 k2} sum_j2 e_{j1 + L1 j2} W_L2^{j2 k2}
 //   pass B: for each k2, F[k2 + L2 k1] = sum_j1 T[j1][k2] W_L1^{j1 k1}
-// Each CTA runs 8 transforms of one pass in shared memory (mixed-radix
-// decimation in time, input placed in digit-reversed order, butterflies in
-// place).  Pass A forms the even extension while loading; pass B writes only
-// k <= m and applies the epilogue (plain, times the inverse-spectrum weights,
-// or with columns 0 and m halved).  Twiddles come from tables computed in
+// Each CTA runs 8 transforms of one pass in shared memory, one per warp
+// (mixed-radix decimation in time, input placed in digit-reversed order,
+// butterflies in place, warp barriers between stages).  Pass A forms the
+// even extension while loading; pass B writes only k <= m and applies the
+// epilogue (plain, times the inverse-spectrum weights, or with columns 0 and
+// m halved).  Twiddles come from tables computed in
 // double precision on the host.
 #pragma once
 #include <cuda_runtime.h>
@@ -31,6 +32,9 @@ struct Fft4Dev {
   int L1, L2;
   int nr1, nr2;
   int r1[FFT4_MAXR], r2[FFT4_MAXR];
+  // per stage: span Ns of the earlier stages, twiddle stride Ls / (Ns R), 1 / Ns
+  int ns1[FFT4_MAXR], ns2[FFT4_MAXR], ts1[FFT4_MAXR], ts2[FFT4_MAXR];
+  float inv1[FFT4_MAXR], inv2[FFT4_MAXR];
   const float2 *tw1, *tw2;  // W_L1^t, W_L2^t
   const int *perm1, *perm2;  // digit-reversed positions
   const float2 *twh, *twl;  // W_L^(t * TWS), W_L^t (t < TWS)
