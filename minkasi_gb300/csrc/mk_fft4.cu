@@ -2,6 +2,7 @@
 #include <cmath>
 #include <vector>
 
+#include "mk_async.cuh"
 #include "mk_common.cuh"
 #include "mk_fft4.cuh"
 
@@ -151,6 +152,16 @@ __device__ void run_stages(float2 *row, int Ls, int nr, const int *rad, const in
   }
 }
 
+// 4- and 8-byte asynchronous global -> shared copies; !valid zero-fills
+// (src must still be a mapped address)
+__device__ __forceinline__ void cp4(void *dst, const void *src, bool valid) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(valid ? 4 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp8(void *dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+
 struct WrTable {
   float2 w[WRN];
 };
@@ -167,17 +178,19 @@ __global__ void __launch_bounds__(NT) k_fft4_a(const float *__restrict__ x, int6
   const int j1_0 = blockIdx.x * FB;
   const int nb = min(FB, L1 - j1_0);
   const int m = (int)p.m, L = (int)p.L;
+  // every copy of the tile in flight at once
+#pragma unroll 4
   for (int idx = tid; idx < FB * L2; idx += NT) {
     const int b = idx % FB, j2 = idx / FB;
     if (b < nb) {
       const int j = j1_0 + b + L1 * j2;
       const int jj = j <= m ? j : L - j;
-      float2 v;
-      v.x = __ldg(x1 + jj);
-      v.y = has2 ? __ldg(x2 + jj) : 0.f;
-      sbuf[b * pitch + __ldg(p.perm2 + j2)] = v;
+      float2 *dst = sbuf + b * pitch + __ldg(p.perm2 + j2);
+      cp4(&dst->x, x1 + jj, true);
+      cp4(&dst->y, x2 + jj, has2);
     }
   }
+  cp_async_wait_all();
   __syncthreads();
   const int warp = tid >> 5, lane = tid & 31;
   if (warp < nb)
@@ -204,10 +217,23 @@ __global__ void __launch_bounds__(NT) k_fft4_b(const float2 *__restrict__ T, int
   const int k2_0 = blockIdx.x * FB;
   const int nb = min(FB, L2 - k2_0);
   const float2 *Tp = T + pair * p.L;
+  const int m = (int)p.m;
+  // the weights of this tile's outputs, [k1][b][row], prefetched with the tile
+  float *sw = reinterpret_cast<float *>(sbuf + FB * pitch);
+  const float *w1 = epi == FFT4_FILTER ? w + r0 * ldw : nullptr;
+  const float *w2 = epi == FFT4_FILTER && has2 ? w1 + ldw : w1;
+#pragma unroll 4
   for (int idx = tid; idx < FB * L1; idx += NT) {
     const int b = idx % FB, j1 = idx / FB;
-    if (b < nb) sbuf[b * pitch + __ldg(p.perm1 + j1)] = Tp[j1 * L2 + k2_0 + b];
+    if (b < nb) cp8(sbuf + b * pitch + __ldg(p.perm1 + j1), Tp + j1 * L2 + k2_0 + b);
+    if (epi == FFT4_FILTER) {
+      const int k = k2_0 + b + L2 * j1;  // j1 plays k1 here
+      const bool ok = b < nb && k <= m;
+      cp4(sw + 2 * idx, ok ? w1 + k : w1, ok);
+      cp4(sw + 2 * idx + 1, ok ? w2 + k : w1, ok && has2);
+    }
   }
+  cp_async_wait_all();
   __syncthreads();
   const int warp = tid >> 5, lane = tid & 31;
   if (warp < nb)
@@ -215,9 +241,6 @@ __global__ void __launch_bounds__(NT) k_fft4_b(const float2 *__restrict__ T, int
   __syncthreads();
   float *o1 = out + r0 * ldo;
   float *o2 = o1 + ldo;
-  const float *w1 = epi == FFT4_FILTER ? w + r0 * ldw : nullptr;
-  const float *w2 = epi == FFT4_FILTER ? w1 + ldw : nullptr;
-  const int m = (int)p.m;
   for (int idx = tid; idx < FB * L1; idx += NT) {
     const int b = idx % FB, k1 = idx / FB;
     if (b >= nb) continue;
@@ -226,8 +249,8 @@ __global__ void __launch_bounds__(NT) k_fft4_b(const float2 *__restrict__ T, int
     const float2 F = sbuf[b * pitch + k1];
     float a = F.x, c = F.y;
     if (epi == FFT4_FILTER) {
-      a *= __ldcs(w1 + k);
-      if (has2) c *= __ldcs(w2 + k);
+      a *= sw[2 * idx];
+      c *= sw[2 * idx + 1];
     } else if (epi == FFT4_HALVE && (k == 0 || k == m)) {
       a *= 0.5f;
       c *= 0.5f;
@@ -420,7 +443,7 @@ int fft4_dct(const Fft4Plan &p, const float *x, int64_t ldx, int64_t nrow, float
   int dev = 0;
   MK_CUDA(cudaGetDevice(&dev));
   if (dev >= 0 && dev < 64 && !g_attr[dev]) {
-    const int mx = FB * (FFT4_LMAX + 1) * (int)sizeof(float2);
+    const int mx = FB * (FFT4_LMAX + 1) * (int)sizeof(float2) + FB * FFT4_LMAX * 2 * (int)sizeof(float);
     MK_CUDA(cudaFuncSetAttribute(k_fft4_a, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     MK_CUDA(cudaFuncSetAttribute(k_fft4_b, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     g_attr[dev] = true;
@@ -430,7 +453,9 @@ int fft4_dct(const Fft4Plan &p, const float *x, int64_t ldx, int64_t nrow, float
   k_fft4_a<<<ga, NT, (size_t)FB * (d.L2 + 1) * sizeof(float2), st>>>(x, ldx, nrow, T, d, wt);
   int rc = launch_status("fft4 pass A");
   if (rc) return rc;
-  k_fft4_b<<<gb, NT, (size_t)FB * (d.L1 + 1) * sizeof(float2), st>>>(T, nrow, out, ldo, w, ldw, epi, d, wt);
+  const size_t smem_b = (size_t)FB * (d.L1 + 1) * sizeof(float2) +
+                        (epi == FFT4_FILTER ? (size_t)FB * d.L1 * 2 * sizeof(float) : 0);
+  k_fft4_b<<<gb, NT, smem_b, st>>>(T, nrow, out, ldo, w, ldw, epi, d, wt);
   return launch_status("fft4 pass B");
 }
 

@@ -22,7 +22,7 @@
 
 namespace mk {
 
-constexpr int FFT4_LMAX = 2048;  // longest transform of one pass
+constexpr int FFT4_LMAX = 1536;  // longest transform of one pass
 constexpr int FFT4_MAXR = 16;    // most radix stages of one pass
 constexpr int FFT4_TWS = 2048;   // split of the four-step twiddle exponent
 
