@@ -11,7 +11,7 @@ namespace {
 
 constexpr int FB = 8;  // transforms per CTA (consecutive j1 in pass A, k2 in pass B)
 constexpr int NT = 256;
-constexpr int WR3 = 0, WR5 = 3, WR7 = 8, WR11 = 15, WRN = 26;  // offsets into the radix constants
+constexpr int WR3 = 0, WR5 = 3, WR7 = 8, WR9 = 15, WR11 = 24, WRN = 35;  // offsets into the radix constants
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -106,12 +106,16 @@ struct Dft<5> : DftOdd<5, WR5> {};
 template <>
 struct Dft<7> : DftOdd<7, WR7> {};
 template <>
+struct Dft<9> : DftOdd<9, WR9> {};
+template <>
 struct Dft<11> : DftOdd<11, WR11> {};
 
 // one in-place decimation-in-time stage of radix R over one transform of
-// length Ls held by a warp, after stages whose radices multiply to Ns
+// length Ls held by a warp, after stages whose radices multiply to Ns; its
+// twiddles W_{Ns R}^{r k} are at stw[(r - 1) Ns + k] (consecutive k of
+// neighbouring lanes are neighbouring entries)
 template <int R>
-__device__ __forceinline__ void stage(float2 *row, int Ls, int Ns, int tstep, float invNs, const float2 *tw,
+__device__ __forceinline__ void stage(float2 *row, int Ls, int Ns, float invNs, const float2 *stw,
                                      const float2 *wr, int lane) {
   const int nq = Ls / R;
   for (int q = lane; q < nq; q += 32) {
@@ -125,7 +129,7 @@ __device__ __forceinline__ void stage(float2 *row, int Ls, int Ns, int tstep, fl
     for (int r = 0; r < R; r++) v[r] = a[r * Ns];
     if (Ns > 1) {
 #pragma unroll
-      for (int r = 1; r < R; r++) v[r] = cmul(v[r], __ldg(tw + r * k * tstep));
+      for (int r = 1; r < R; r++) v[r] = cmul(v[r], __ldg(stw + (r - 1) * Ns + k));
     }
     Dft<R>::run(v, wr);
 #pragma unroll
@@ -134,19 +138,21 @@ __device__ __forceinline__ void stage(float2 *row, int Ls, int Ns, int tstep, fl
 }
 
 // all stages of one transform (the calling warp's row)
-__device__ void run_stages(float2 *row, int Ls, int nr, const int *rad, const int *ns, const int *ts,
-                           const float *inv, const float2 *tw, const float2 *wr, int lane) {
+__device__ void run_stages(float2 *row, int Ls, int nr, const int *rad, const int *ns, const int *to,
+                           const float *inv, const float2 *stw, const float2 *wr, int lane) {
   for (int s = 0; s < nr; s++) {
-    const int R = rad[s], Ns = ns[s], tstep = ts[s];
+    const int R = rad[s], Ns = ns[s];
     const float iv = inv[s];
+    const float2 *t = stw + to[s];
     switch (R) {
-      case 2: stage<2>(row, Ls, Ns, tstep, iv, tw, wr, lane); break;
-      case 3: stage<3>(row, Ls, Ns, tstep, iv, tw, wr, lane); break;
-      case 4: stage<4>(row, Ls, Ns, tstep, iv, tw, wr, lane); break;
-      case 5: stage<5>(row, Ls, Ns, tstep, iv, tw, wr, lane); break;
-      case 7: stage<7>(row, Ls, Ns, tstep, iv, tw, wr, lane); break;
-      case 8: stage<8>(row, Ls, Ns, tstep, iv, tw, wr, lane); break;
-      default: stage<11>(row, Ls, Ns, tstep, iv, tw, wr, lane); break;
+      case 2: stage<2>(row, Ls, Ns, iv, t, wr, lane); break;
+      case 3: stage<3>(row, Ls, Ns, iv, t, wr, lane); break;
+      case 4: stage<4>(row, Ls, Ns, iv, t, wr, lane); break;
+      case 5: stage<5>(row, Ls, Ns, iv, t, wr, lane); break;
+      case 7: stage<7>(row, Ls, Ns, iv, t, wr, lane); break;
+      case 8: stage<8>(row, Ls, Ns, iv, t, wr, lane); break;
+      case 9: stage<9>(row, Ls, Ns, iv, t, wr, lane); break;
+      default: stage<11>(row, Ls, Ns, iv, t, wr, lane); break;
     }
     __syncwarp();
   }
@@ -192,17 +198,18 @@ __global__ void __launch_bounds__(NT) k_fft4_a(const float *__restrict__ x, int6
   }
   cp_async_wait_all();
   __syncthreads();
+  // warp b transforms row b, twiddles it by W_L^{j1 k2} and stores it
   const int warp = tid >> 5, lane = tid & 31;
-  if (warp < nb)
-    run_stages(sbuf + warp * pitch, L2, p.nr2, p.r2, p.ns2, p.ts2, p.inv2, p.tw2, wt.w, lane);
-  __syncthreads();
-  float2 *Tp = T + pair * p.L;
-  for (int idx = tid; idx < nb * L2; idx += NT) {
-    const int b = idx / L2, k2 = idx - b * L2;
-    const int j1 = j1_0 + b;
-    const int e = j1 * k2;
-    const float2 w = cmul(__ldg(p.twh + e / FFT4_TWS), __ldg(p.twl + e % FFT4_TWS));
-    Tp[j1 * L2 + k2] = cmul(sbuf[b * pitch + k2], w);
+  if (warp >= nb) return;
+  float2 *row = sbuf + warp * pitch;
+  run_stages(row, L2, p.nr2, p.r2, p.ns2, p.to2, p.inv2, p.stw2, wt.w, lane);
+  const int j1 = j1_0 + warp;
+  const float2 tl = __ldg(p.tlane + 32 * j1 + lane);
+  const float2 *tb = p.tblk + j1 * p.nb32;
+  float2 *Tp = T + pair * p.L + j1 * L2;
+  for (int i = 0; i < p.nb32; i++) {
+    const int k2 = 32 * i + lane;
+    if (k2 < L2) Tp[k2] = cmul(row[k2], cmul(__ldg(tb + i), tl));
   }
 }
 
@@ -236,8 +243,7 @@ __global__ void __launch_bounds__(NT) k_fft4_b(const float2 *__restrict__ T, int
   cp_async_wait_all();
   __syncthreads();
   const int warp = tid >> 5, lane = tid & 31;
-  if (warp < nb)
-    run_stages(sbuf + warp * pitch, L1, p.nr1, p.r1, p.ns1, p.ts1, p.inv1, p.tw1, wt.w, lane);
+  if (warp < nb) run_stages(sbuf + warp * pitch, L1, p.nr1, p.r1, p.ns1, p.to1, p.inv1, p.stw1, wt.w, lane);
   __syncthreads();
   float *o1 = out + r0 * ldo;
   float *o2 = o1 + ldo;
@@ -269,19 +275,24 @@ void factor(int64_t L, std::vector<int> &f) {
   if (L != 1) f.clear();
 }
 
-// radices of a transform of length Ls (a product of 2, 3, 5, 7, 11)
+// radices of a transform of length Ls (a product of 2, 3, 5, 7, 11): odd
+// ones first (the stride-1 first stage is then free of bank conflicts), 3 x 3
+// as 9, powers of 2 as 8, 4, 2
 bool radices(int Ls, int *r, int *nr) {
   std::vector<int> f;
   factor(Ls, f);
   if (f.empty() && Ls != 1) return false;
-  int n2 = 0;
+  int c[12] = {0};
+  for (int x : f) c[x]++;
   std::vector<int> out;
-  for (int x : f) n2 += x == 2;
-  for (; n2 >= 3; n2 -= 3) out.push_back(8);
-  if (n2 == 2) out.push_back(4);
-  if (n2 == 1) out.push_back(2);
-  for (int x : f)
-    if (x != 2) out.push_back(x);
+  for (int i = 0; i < c[11]; i++) out.push_back(11);
+  for (; c[3] >= 2; c[3] -= 2) out.push_back(9);
+  for (int i = 0; i < c[7]; i++) out.push_back(7);
+  for (int i = 0; i < c[5]; i++) out.push_back(5);
+  if (c[3]) out.push_back(3);
+  for (; c[2] >= 3; c[2] -= 3) out.push_back(8);
+  if (c[2] == 2) out.push_back(4);
+  if (c[2] == 1) out.push_back(2);
   if ((int)out.size() > FFT4_MAXR) return false;
   for (size_t i = 0; i < out.size(); i++) r[i] = out[i];
   *nr = (int)out.size();
@@ -291,24 +302,24 @@ bool radices(int Ls, int *r, int *nr) {
 size_t al(size_t x) { return (x + 255) / 256 * 256; }
 
 struct TableLayout {
-  size_t tw1, tw2, perm1, perm2, twl, twh, total;
+  size_t stw1, stw2, perm1, perm2, tlane, tblk, total;
 };
 
 TableLayout layout(const Fft4Dev &d) {
   TableLayout t;
   size_t o = 0;
-  t.tw1 = o;
+  t.stw1 = o;
   o += al((size_t)d.L1 * sizeof(float2));
-  t.tw2 = o;
+  t.stw2 = o;
   o += al((size_t)d.L2 * sizeof(float2));
   t.perm1 = o;
   o += al((size_t)d.L1 * sizeof(int));
   t.perm2 = o;
   o += al((size_t)d.L2 * sizeof(int));
-  t.twl = o;
-  o += al((size_t)FFT4_TWS * sizeof(float2));
-  t.twh = o;
-  o += al((size_t)((d.L + FFT4_TWS - 1) / FFT4_TWS) * sizeof(float2));
+  t.tlane = o;
+  o += al((size_t)d.L1 * 32 * sizeof(float2));
+  t.tblk = o;
+  o += al((size_t)d.L1 * d.nb32 * sizeof(float2));
   t.total = o;
   return t;
 }
@@ -338,8 +349,8 @@ void digit_rev(int Ls, const int *r, int nr, int *P) {
 
 WrTable radix_constants() {
   WrTable t;
-  const int rs[4] = {3, 5, 7, 11}, off[4] = {WR3, WR5, WR7, WR11};
-  for (int i = 0; i < 4; i++)
+  const int rs[5] = {3, 5, 7, 9, 11}, off[5] = {WR3, WR5, WR7, WR9, WR11};
+  for (int i = 0; i < 5; i++)
     for (int k = 0; k < rs[i]; k++) t.w[off[i] + k] = unit(k, rs[i]);
   return t;
 }
@@ -384,16 +395,18 @@ bool fft4_shape(int64_t n, Fft4Dev *d) {
   t.L1 = (int)best;
   t.L2 = (int)(L / best);
   if (!radices(t.L1, t.r1, &t.nr1) || !radices(t.L2, t.r2, &t.nr2)) return false;
+  t.nb32 = (t.L2 + 31) / 32;
   for (int pass = 0; pass < 2; pass++) {
-    const int Ls = pass ? t.L2 : t.L1, nr = pass ? t.nr2 : t.nr1;
+    const int nr = pass ? t.nr2 : t.nr1;
     const int *r = pass ? t.r2 : t.r1;
-    int *ns = pass ? t.ns2 : t.ns1, *ts = pass ? t.ts2 : t.ts1;
+    int *ns = pass ? t.ns2 : t.ns1, *to = pass ? t.to2 : t.to1;
     float *inv = pass ? t.inv2 : t.inv1;
-    int span = 1;
+    int span = 1, off = 0;
     for (int s = 0; s < nr; s++) {
       ns[s] = span;
-      ts[s] = Ls / (span * r[s]);
+      to[s] = off;
       inv[s] = 1.0f / (float)span;
+      off += (r[s] - 1) * span;
       span *= r[s];
     }
   }
@@ -412,23 +425,29 @@ int fft4_init(Fft4Plan *p, int64_t n, void *dev_tables) {
   Fft4Dev &d = p->d;
   const TableLayout t = layout(d);
   std::vector<char> h(t.total, 0);
-  float2 *tw1 = (float2 *)(h.data() + t.tw1), *tw2 = (float2 *)(h.data() + t.tw2);
-  float2 *twl = (float2 *)(h.data() + t.twl), *twh = (float2 *)(h.data() + t.twh);
-  for (int i = 0; i < d.L1; i++) tw1[i] = unit(i, d.L1);
-  for (int i = 0; i < d.L2; i++) tw2[i] = unit(i, d.L2);
+  for (int pass = 0; pass < 2; pass++) {
+    const int nr = pass ? d.nr2 : d.nr1;
+    const int *r = pass ? d.r2 : d.r1, *ns = pass ? d.ns2 : d.ns1, *to = pass ? d.to2 : d.to1;
+    float2 *stw = (float2 *)(h.data() + (pass ? t.stw2 : t.stw1));
+    for (int s = 0; s < nr; s++)
+      for (int rr = 1; rr < r[s]; rr++)
+        for (int k = 0; k < ns[s]; k++) stw[to[s] + (rr - 1) * ns[s] + k] = unit((double)rr * k, (double)ns[s] * r[s]);
+  }
   digit_rev(d.L1, d.r1, d.nr1, (int *)(h.data() + t.perm1));
   digit_rev(d.L2, d.r2, d.nr2, (int *)(h.data() + t.perm2));
-  for (int i = 0; i < FFT4_TWS; i++) twl[i] = unit(i, (double)d.L);
-  for (int64_t i = 0; i < (d.L + FFT4_TWS - 1) / FFT4_TWS; i++)
-    twh[i] = unit((double)(i * FFT4_TWS % d.L), (double)d.L);
+  float2 *tlane = (float2 *)(h.data() + t.tlane), *tblk = (float2 *)(h.data() + t.tblk);
+  for (int64_t j1 = 0; j1 < d.L1; j1++) {
+    for (int l = 0; l < 32; l++) tlane[32 * j1 + l] = unit((double)(j1 * l % d.L), (double)d.L);
+    for (int i = 0; i < d.nb32; i++) tblk[j1 * d.nb32 + i] = unit((double)(j1 * 32 * i % d.L), (double)d.L);
+  }
   MK_CUDA(cudaMemcpy(dev_tables, h.data(), t.total, cudaMemcpyHostToDevice));
   char *b = (char *)dev_tables;
-  d.tw1 = (const float2 *)(b + t.tw1);
-  d.tw2 = (const float2 *)(b + t.tw2);
+  d.stw1 = (const float2 *)(b + t.stw1);
+  d.stw2 = (const float2 *)(b + t.stw2);
   d.perm1 = (const int *)(b + t.perm1);
   d.perm2 = (const int *)(b + t.perm2);
-  d.twl = (const float2 *)(b + t.twl);
-  d.twh = (const float2 *)(b + t.twh);
+  d.tlane = (const float2 *)(b + t.tlane);
+  d.tblk = (const float2 *)(b + t.tblk);
   p->tables = dev_tables;
   return MK_OK;
 }

@@ -24,20 +24,21 @@ namespace mk {
 
 constexpr int FFT4_LMAX = 1536;  // longest transform of one pass
 constexpr int FFT4_MAXR = 16;    // most radix stages of one pass
-constexpr int FFT4_TWS = 2048;   // split of the four-step twiddle exponent
 
 // device view of a plan (kernel argument)
 struct Fft4Dev {
   int64_t n, m, L;
-  int L1, L2;
+  int L1, L2, nb32;  // nb32 = ceil(L2 / 32)
   int nr1, nr2;
   int r1[FFT4_MAXR], r2[FFT4_MAXR];
-  // per stage: span Ns of the earlier stages, twiddle stride Ls / (Ns R), 1 / Ns
-  int ns1[FFT4_MAXR], ns2[FFT4_MAXR], ts1[FFT4_MAXR], ts2[FFT4_MAXR];
+  // per stage: span Ns of the earlier stages, 1 / Ns, offset of its twiddles
+  int ns1[FFT4_MAXR], ns2[FFT4_MAXR], to1[FFT4_MAXR], to2[FFT4_MAXR];
   float inv1[FFT4_MAXR], inv2[FFT4_MAXR];
-  const float2 *tw1, *tw2;  // W_L1^t, W_L2^t
+  // stage twiddles W_{Ns R}^{r k} at [to + (r - 1) Ns + k]
+  const float2 *stw1, *stw2;
   const int *perm1, *perm2;  // digit-reversed positions
-  const float2 *twh, *twl;  // W_L^(t * TWS), W_L^t (t < TWS)
+  // four-step twiddle W_L^{j1 k2} = tblk[j1 nb32 + k2 / 32] * tlane[32 j1 + k2 % 32]
+  const float2 *tlane, *tblk;
 };
 
 // epilogues of pass B
