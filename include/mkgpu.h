@@ -289,9 +289,15 @@ int mk_tod2map_fixed_noalloc(void *map, const void *dat, const int32_t *ipix, in
  * 5, 7, 11 (every length minkasi's truncate_tod keeps) use this library's
  * four-step shared-memory FFT: two kernels per DCT, two rows per complex
  * transform, the extension formed while loading; other FP32 plans use cuFFT.
- * `in` and `out` are (nrow, n) dtype-typed and may alias.  The plan holds a
+ * `in` and `out` are (nrow, n) dtype-typed and may alias.  The plan uses a
  * workspace of mk_dct1_workspace_bytes() bytes that the CALLER provides
  * (device pointer, 256-byte aligned) and keeps alive while the plan is used.
+ * The workspace holds only scratch of one call, so plans of any shapes may
+ * share one (sized for the largest) when their calls are stream-ordered.
+ * What a plan keeps between calls (cuFFT's plan data; the four-step
+ * engine's twiddle and permutation tables, at most a few hundred KB; the
+ * tensor-core status word) is device memory the plan allocates at creation
+ * and frees on destroy.
  * Replaces many_fft_r2r_1d / many_fftf_r2r_1d, minkasi/lib/mkfftw.c:174-254. */
 typedef struct mk_dct_plan mk_dct_plan;
 int mk_dct1_workspace_bytes(int64_t nrow, int64_t n, int dtype, size_t *bytes);

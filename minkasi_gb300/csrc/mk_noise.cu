@@ -153,15 +153,34 @@ struct DctCore {
   int dtype = MK_F64;
   void *E = nullptr, *F = nullptr, *work = nullptr;
   size_t work_bytes = 0;
-  // tensor-core rotation scratch (FP32 plans): status word, then operand image
+  // tensor-core rotation (FP32 plans): status word (plan-owned), operand
+  // image (workspace: rebuilt by every rotation)
   int *tc_err = nullptr;
   void *tc_bimg = nullptr;
+  // device memory the plan owns: the status word, then the four-step tables.
+  // Never in the workspace, which plans of different shapes may share.
+  void *owned = nullptr;
 };
 
-// workspace bytes of the tensor-core rotation scratch: 256 B status + image
+// workspace bytes of the tensor-core rotation's operand image
 size_t tc_bytes(int64_t nrow, int dtype) {
   if (dtype != MK_F32 || !mk::rot_tc_supported(nrow)) return 0;
-  return 256 + ((mk::rot_tc_bimg_bytes(nrow) + 255) / 256) * 256;
+  return align_up(mk::rot_tc_bimg_bytes(nrow));
+}
+
+void core_free(DctCore *c) {
+  if (c->have_fft) cufftDestroy(c->fft);
+  c->have_fft = false;
+  if (c->owned) cudaFree(c->owned);
+  c->owned = nullptr;
+}
+
+// plan-owned device memory: 256 B (status word) + `extra`
+int own_alloc(DctCore *c, size_t extra) {
+  MK_CUDA(cudaMalloc(&c->owned, 256 + extra));
+  MK_CUDA(cudaMemset(c->owned, 0, 256));
+  c->tc_err = (int *)c->owned;
+  return MK_OK;
 }
 
 size_t elt(int dtype) { return dtype == MK_F64 ? 8 : 4; }
@@ -196,7 +215,7 @@ int core_bytes(int64_t nrow, int64_t n, int dtype, size_t *bytes) {
   mk::Fft4Dev d;
   if (use_own(nrow, n, dtype, &d)) {
     *bytes = align_up((size_t)nrow * n * sizeof(float)) + align_up(mk::fft4_t_bytes(d, nrow)) +
-             align_up(mk::fft4_table_bytes(d)) + tc_bytes(nrow, dtype);
+             tc_bytes(nrow, dtype);
     return MK_OK;
   }
   int64_t N = 2 * (n - 1);
@@ -228,13 +247,11 @@ int core_create(DctCore *c, int64_t nrow, int64_t n, int dtype, void *ws, size_t
     p += align_up((size_t)nrow * n * sizeof(float));
     c->T = (float2 *)p;
     p += align_up(mk::fft4_t_bytes(d, nrow));
-    rc = mk::fft4_init(&c->f4, n, p);
-    if (rc) return rc;
-    p += align_up(mk::fft4_table_bytes(d));
-    if (tc_bytes(nrow, dtype)) {
-      c->tc_err = (int *)p;
-      c->tc_bimg = p + 256;
-      MK_CUDA(cudaMemset(c->tc_err, 0, sizeof(int)));
+    if (tc_bytes(nrow, dtype)) c->tc_bimg = p;
+    if ((rc = own_alloc(c, mk::fft4_table_bytes(d))) ||
+        (rc = mk::fft4_init(&c->f4, n, (char *)c->owned + 256))) {
+      core_free(c);
+      return rc;
     }
     return MK_OK;
   }
@@ -245,22 +262,17 @@ int core_create(DctCore *c, int64_t nrow, int64_t n, int dtype, void *ws, size_t
   c->work = p;
   rc = make_fft(&c->fft, nrow, c->N, dtype, &c->work_bytes);
   if (rc) return rc;
+  c->have_fft = true;
   if (tc_bytes(nrow, dtype)) {
-    char *q = (char *)c->work + align_up(c->work_bytes);
-    c->tc_err = (int *)q;
-    c->tc_bimg = q + 256;
-    cudaError_t e = cudaMemset(c->tc_err, 0, sizeof(int));
-    if (e != cudaSuccess) {
-      cufftDestroy(c->fft);
-      mk::set_error("workspace status init failed: %s", cudaGetErrorString(e));
-      return MK_ERR_CUDA;
+    c->tc_bimg = (char *)c->work + align_up(c->work_bytes);
+    if ((rc = own_alloc(c, 0))) {
+      core_free(c);
+      return rc;
     }
   }
-  c->have_fft = true;
   cufftResult r = cufftSetWorkArea(c->fft, c->work);
   if (r != CUFFT_SUCCESS) {
-    cufftDestroy(c->fft);
-    c->have_fft = false;
+    core_free(c);
     mk::set_error("cufftSetWorkArea failed: %s", cufft_str(r));
     return MK_ERR_CUFFT;
   }
@@ -445,7 +457,7 @@ extern "C" int mk_dct1_exec(mk_dct_plan *plan, const void *in, void *out, void *
 
 extern "C" int mk_dct1_plan_destroy(mk_dct_plan *plan) {
   if (!plan) return MK_OK;
-  if (plan->core.have_fft) cufftDestroy(plan->core.fft);
+  core_free(&plan->core);
   delete plan;
   return MK_OK;
 }
@@ -488,7 +500,7 @@ extern "C" int mk_apply_noise(mk_noise_plan *plan, const void *v, const void *vT
 
 extern "C" int mk_noise_plan_destroy(mk_noise_plan *plan) {
   if (!plan) return MK_OK;
-  if (plan->core.have_fft) cufftDestroy(plan->core.fft);
+  core_free(&plan->core);
   delete plan;
   return MK_OK;
 }

@@ -229,6 +229,35 @@ def test_dct1_engines_agree_and_fall_back(K):
         K.set_dct_engine(2)
 
 
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_noise_plans_sharing_one_workspace(K, dtype):
+    """Plans of different shapes on one workspace (as the batched operator
+    builds them), used alternately: each gives what it gives on a workspace
+    of its own.  Plan state (transform tables, status word) must not live in
+    the shared workspace."""
+    shapes = [(16, 3529), (16, 4236), (32, 4097)]
+    ws_bytes = max(K.noise_workspace_bytes(nd, n, dtype) for nd, n in shapes)
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+    rng = np.random.default_rng(11)
+    cases = []
+    for nd, n in shapes:
+        A = np.linalg.qr(rng.standard_normal((nd, nd)))[0]
+        cases.append((dev(A, dtype), dev(A.T, dtype), dev(rng.random((nd, n)), dtype),
+                      dev(rng.standard_normal((nd, n)), dtype)))
+    shared = [K.NoisePlan(nd, n, dtype, workspace=ws) for nd, n in shapes]
+    alone = [K.NoisePlan(nd, n, dtype) for nd, n in shapes]
+    for _ in range(2):
+        for p_s, p_a, (v, vT, w, x) in zip(shared, alone, cases):
+            # the tensor-core rotation (its operand image is workspace too)
+            # where the shape allows it
+            mode = 2 if dtype == torch.float32 and x.shape[0] in (32, 64, 128, 256) else 1
+            a = p_s.apply(v, vT, w, x, rot_mode=mode)
+            b = p_a.apply(v, vT, w, x, rot_mode=mode)
+            assert torch.equal(a, b)
+    for p_s in shared:
+        assert p_s.status() == 0
+
+
 def test_apply_noise_golden_f64(K, gold):
     g = gold("noise.npz")
     v, vT, w = dev(g["v"]), dev(g["vT"]), dev(g["mywt"])
