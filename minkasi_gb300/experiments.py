@@ -208,6 +208,11 @@ def hit_density(hits: torch.Tensor) -> float:
     return float(len(pts) / max(int(inside.sum()), 1))
 
 
+def _compact(hist: list) -> list:
+    """(iteration, recursive residual, true FP64 residual, restarted) per replacement."""
+    return [[h["iter"], h["recursive_rel"], h["true_rel_residual"], h.get("restart", False)] for h in hist]
+
+
 def run_large(config: str = "c4", tol: float = 1e-6, max_iter: int = 3000, wall_limit_s: float = 900.0,
               learned: bool = False, pair_skies=(1000, 1001), pair_iters: int = 240, n_white: int = 64,
               epochs: int = 12, batch: int = 4, log=print) -> dict:
@@ -287,9 +292,9 @@ def run_large(config: str = "c4", tol: float = 1e-6, max_iter: int = 3000, wall_
     t1 = time.perf_counter()
     budget = max(50, min(max_iter, int(wall_limit_s * 1e3 / max(msmx * 1.3, 1e-3))))
     xs, tm = timed(lambda: run_pcg_mixed(b, x0, tv, pre_ms, tol=tol, max_iter=budget, history=hist))
-    out["mixed_solve"] = {"iters": xs.niter, "fp64_residuals": xs.outer, "wall_s": tm,
-                          "true_rel_residual": xs.rel_residual, "reached_tol": xs.rel_residual <= tol,
-                          "iteration_budget": budget}
+    out["mixed_solve"] = {"iters": xs.niter, "fp64_residuals": xs.outer, "restarts": xs.restarts,
+                          "wall_s": tm, "true_rel_residual": xs.rel_residual, "reached_tol": xs.rel_residual <= tol,
+                          "iteration_budget": budget, "replacements": _compact(hist)}
     out["jacobi_f64_projected_s"] = xs.niter * ms64 / 1e3
     out["projected_speedup_mixed_vs_jacobi_f64"] = out["jacobi_f64_projected_s"] / tm
     if learned:
@@ -320,8 +325,9 @@ def run_large(config: str = "c4", tol: float = 1e-6, max_iter: int = 3000, wall_
                                              inner_precon=mlearn))
         out["learned"] = {"pairs": npairs, "pair_gen_s": t_pairs, "train_s": t_train, "epochs": epochs,
                           "loss_first": hist_loss[0], "loss_last": hist_loss[-1]}
-        out["mixed_learned_solve"] = {"iters": xl.niter, "fp64_residuals": xl.outer, "wall_s": tl,
-                                      "true_rel_residual": xl.rel_residual, "reached_tol": xl.rel_residual <= tol}
+        out["mixed_learned_solve"] = {"iters": xl.niter, "fp64_residuals": xl.outer, "restarts": xl.restarts,
+                                      "wall_s": tl, "true_rel_residual": xl.rel_residual,
+                                      "reached_tol": xl.rel_residual <= tol, "replacements": _compact(hist_l)}
         out["projected_speedup_mixed_learned_vs_jacobi_f64"] = out["jacobi_f64_projected_s"] / tl
         L.save(net, f"/tmp/mk_learned_{config}.npz")
     return out

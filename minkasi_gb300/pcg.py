@@ -245,10 +245,11 @@ class MixedOp:
 
 
 def run_pcg_mixed(b: Mapset, x0: Mapset, tods: TodVec, precon=None, tol: float = 1e-6,
-                  max_iter: int = 5000, replace_every: int = 50, graph: bool = True,
+                  max_iter: int = 5000, replace_every: int = 200, graph: bool = True,
                   verbose: bool = False, history: Optional[list] = None,
                   inner_precon=None, on_outer=None, mode: str = "reliable",
-                  inner_iters: int = 20, max_outer: int = 500) -> Mapset:
+                  inner_iters: int = 20, max_outer: int = 500,
+                  restart_drift: float = 1.2) -> Mapset:
     """Mixed-precision PCG to an FP64 true residual ||b - A x||/||b|| <= tol.
 
     mode="reliable" (default): PCG whose vectors, dot products and scalars are
@@ -256,9 +257,14 @@ def run_pcg_mixed(b: Mapset, x0: Mapset, tods: TodVec, precon=None, tol: float =
     DCT/filter, 3xTF32 tensor-core rotations); every ``replace_every``
     iterations, and whenever the recursive residual claims convergence, the
     residual is replaced by the FP64 true residual b - A64 x (an FP64
-    operator application).  Those replacements are the iterative-refinement
+    operator application, as costly as 10-25 FP32 iterations on GB300; the
+    recursive residual tracks the true one to ~6 digits over 200 iterations
+    on the benchmark maps, hence the default).  Those replacements are the iterative-refinement
     steps: the FP64 residual corrects the drift of the FP32 operator while the
-    Krylov space is kept.
+    Krylov space is kept.  When a replacement finds the recursive residual
+    off from the true one by more than ``restart_drift`` (either way), the
+    search direction restarts from z = M r: continuing with the old one
+    after a large correction can diverge.
 
     mode="refine": classic iterative refinement -- each outer step solves
     A32 e = r64 with ``inner_iters`` FP32 PCG iterations from zero and updates
@@ -285,7 +291,8 @@ def run_pcg_mixed(b: Mapset, x0: Mapset, tods: TodVec, precon=None, tol: float =
     ptmp = torch.empty_like(bf)
 
     def replace() -> float:
-        # r = b - A64 x; z = M r; zr = r.z  (p kept)
+        # r = b - A64 x; z = M r; zr = r.z  (p kept; the caller restarts it
+        # when the recursive residual had drifted)
         op64.apply(xf, ax)
         K.pcg_init(st.r, st.z, ptmp, bf, ax, st.M, st.s, st.red)
         if st.Mop is not None:
@@ -297,6 +304,7 @@ def run_pcg_mixed(b: Mapset, x0: Mapset, tods: TodVec, precon=None, tol: float =
     rel = math.sqrt(max(float(st.s[MK_S_RR]), 0.0)) / bnorm
     k = 0
     outer = 0
+    restarts = 0
     since = 0
     while k < max_iter:
         st.step()
@@ -313,8 +321,16 @@ def run_pcg_mixed(b: Mapset, x0: Mapset, tods: TodVec, precon=None, tol: float =
             rel = replace()
             outer += 1
             since = 0
+            # the recursive residual had drifted from the true one (the FP32
+            # operator's rounding): the kept search direction no longer fits
+            # the replaced residual, so restart it (p = z)
+            restart = rel > restart_drift * rec or rec > restart_drift * rel
+            if restart:
+                st.p.copy_(st.z)
+                restarts += 1
             if history is not None:
-                history.append({"iter": k, "recursive_rel": rec, "true_rel_residual": rel})
+                history.append({"iter": k, "recursive_rel": rec, "true_rel_residual": rel,
+                                "restart": restart})
             if verbose:
                 print(f"iter {k}: true FP64 residual {rel:.3e} (recursive {rec:.3e})")
             if on_outer is not None:
@@ -323,6 +339,7 @@ def run_pcg_mixed(b: Mapset, x0: Mapset, tods: TodVec, precon=None, tol: float =
                 break
     x.niter = k
     x.outer = outer
+    x.restarts = restarts
     x.rel_residual = rel
     return x
 

@@ -163,6 +163,28 @@ def test_jacobi_and_mixed_reach_1e6_checked_by_oracle(mk):
     assert np.linalg.norm(a - c) / np.linalg.norm(a) < 1e-3
 
 
+def test_mixed_replacement_policies_converge(mk):
+    """Every residual-replacement interval, including replacing only when the
+    recursive residual claims convergence, reaches the FP64 tolerance; a
+    replacement that finds the recursive residual drifted restarts the
+    search direction instead of diverging."""
+    from minkasi_gb300 import synth
+    tv, m = synth.make_todvec(synth.CONFIGS["tiny"])
+    mapset = mk.Mapset()
+    mapset.add_map(m)
+    rhs = mapset.copy()
+    tv.make_rhs(rhs)
+    x0 = rhs.copy()
+    x0.clear()
+    pre = mk.jacobi_precon(mk.make_hits(tv, m))
+    for every in (10, 200, 10 ** 9):
+        hist = []
+        x = mk.run_pcg_mixed(rhs, x0, tv, pre, tol=1e-6, replace_every=every, history=hist)
+        assert x.rel_residual <= 1e-6, every
+        assert hist[-1]["true_rel_residual"] <= 1e-6
+        assert x.outer == len(hist) and x.restarts == sum(h["restart"] for h in hist)
+
+
 def test_tod2map_from_pinned_host_through_api(mk, gold):
     """SkyMap.tod2map on a pinned host timestream: chunked copies on a copy
     stream overlapped with the scatter (a small chunk makes the two-buffer
