@@ -158,14 +158,11 @@ __device__ void run_stages(float2 *row, int Ls, int nr, const int *rad, const in
   }
 }
 
-// 4- and 8-byte asynchronous global -> shared copies; !valid zero-fills
+// 4-byte asynchronous global -> shared copy; !valid zero-fills
 // (src must still be a mapped address)
 __device__ __forceinline__ void cp4(void *dst, const void *src, bool valid) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(valid ? 4 : 0)
                : "memory");
-}
-__device__ __forceinline__ void cp8(void *dst, const void *src) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
 }
 
 struct WrTable {
@@ -213,57 +210,141 @@ __global__ void __launch_bounds__(NT) k_fft4_a(const float *__restrict__ x, int6
   }
 }
 
+// ---- pass B ------------------------------------------------------------
+// The CTA's 8 transforms (8 consecutive k2) are interleaved over the threads:
+// butterfly bf of a stage belongs to row b = bf % 8, so the 8 lanes of a row
+// group read or write 8 consecutive columns of T / of the output.  The first
+// stage reads its inputs straight from T (natural order: position g R0 + r of
+// the digit-reversed layout holds index iperm[g R0] + (L1 / R0) r), and the
+// last stage writes its outputs straight to the DCT rows with the epilogue.
+struct PassB {
+  const float2 *Tp;  // this pair's T (L1 x L2)
+  int L2, k2_0, nb, m, epi;
+  bool has2;
+  float *o1, *o2;
+  const float *sw;  // prefetched weights, [k1][b][row]
+  const int *iperm;
+};
+
+template <int R, bool FIRST, bool LAST>
+__device__ __forceinline__ void bstage(float2 *sbuf, int pitch, int Ls, int Ns, float invNs, const float2 *stw,
+                                       const float2 *wr, const PassB &pb) {
+  const int nq = Ls / R;
+  for (int bf = threadIdx.x; bf < FB * nq; bf += NT) {
+    const int b = bf % FB, q = bf / FB;
+    if (b >= pb.nb) continue;
+    const int g = __float2int_rz(((float)q + 0.5f) * invNs);
+    const int k = q - g * Ns;
+    float2 v[R];
+    if (FIRST) {  // Ns == 1: g == q, k == 0
+      const int jg = __ldg(pb.iperm + q * R);
+#pragma unroll
+      for (int r = 0; r < R; r++) v[r] = pb.Tp[(jg + (Ls / R) * r) * pb.L2 + pb.k2_0 + b];
+    } else {
+      const float2 *a = sbuf + b * pitch + g * Ns * R + k;
+#pragma unroll
+      for (int r = 0; r < R; r++) v[r] = a[r * Ns];
+      if (Ns > 1) {
+#pragma unroll
+        for (int r = 1; r < R; r++) v[r] = cmul(v[r], __ldg(stw + (r - 1) * Ns + k));
+      }
+    }
+    Dft<R>::run(v, wr);
+    if (LAST) {
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        const int k1 = g * Ns * R + k + r * Ns;
+        const int kk = pb.k2_0 + b + pb.L2 * k1;
+        if (kk > pb.m) continue;
+        float a = v[r].x, c = v[r].y;
+        if (pb.epi == FFT4_FILTER) {
+          a *= pb.sw[2 * (k1 * FB + b)];
+          c *= pb.sw[2 * (k1 * FB + b) + 1];
+        } else if (pb.epi == FFT4_HALVE && (kk == 0 || kk == pb.m)) {
+          a *= 0.5f;
+          c *= 0.5f;
+        }
+        pb.o1[kk] = a;
+        if (pb.has2) pb.o2[kk] = c;
+      }
+    } else {
+      float2 *a = sbuf + b * pitch + g * Ns * R + k;
+#pragma unroll
+      for (int r = 0; r < R; r++) a[r * Ns] = v[r];
+    }
+  }
+}
+
+template <bool FIRST, bool LAST>
+__device__ __forceinline__ void bstage_r(int R, float2 *sbuf, int pitch, int Ls, int Ns, float invNs,
+                                         const float2 *stw, const float2 *wr, const PassB &pb) {
+  switch (R) {
+    case 2: bstage<2, FIRST, LAST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
+    case 3: bstage<3, FIRST, LAST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
+    case 4: bstage<4, FIRST, LAST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
+    case 5: bstage<5, FIRST, LAST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
+    case 7: bstage<7, FIRST, LAST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
+    case 8: bstage<8, FIRST, LAST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
+    case 9: bstage<9, FIRST, LAST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
+    default: bstage<11, FIRST, LAST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
+  }
+}
+
+// row pitch (float2) of the pass-B tile: odd, so the 8 interleaved rows fall
+// in distinct shared-memory banks
+__host__ __device__ __forceinline__ int pitch_b(int L1) { return L1 | 1; }
+
 // pass B: T[pair] -> DCT rows 2 pair, 2 pair + 1 of out (k <= m), epilogue
 __global__ void __launch_bounds__(NT) k_fft4_b(const float2 *__restrict__ T, int64_t nrow, float *__restrict__ out,
                                                int64_t ldo, const float *__restrict__ w, int64_t ldw, int epi,
                                                const Fft4Dev p, const WrTable wt) {
   extern __shared__ float2 sbuf[];
-  const int L1 = p.L1, L2 = p.L2, pitch = L1 + 1, tid = threadIdx.x;
+  const int L1 = p.L1, L2 = p.L2, pitch = pitch_b(L1), tid = threadIdx.x;
   const int64_t pair = blockIdx.y, r0 = 2 * pair;
-  const bool has2 = r0 + 1 < nrow;
-  const int k2_0 = blockIdx.x * FB;
-  const int nb = min(FB, L2 - k2_0);
-  const float2 *Tp = T + pair * p.L;
-  const int m = (int)p.m;
-  // the weights of this tile's outputs, [k1][b][row], prefetched with the tile
+  PassB pb;
+  pb.has2 = r0 + 1 < nrow;
+  pb.k2_0 = blockIdx.x * FB;
+  pb.nb = min(FB, L2 - pb.k2_0);
+  pb.Tp = T + pair * p.L;
+  pb.L2 = L2;
+  pb.m = (int)p.m;
+  pb.epi = epi;
+  pb.o1 = out + r0 * ldo;
+  pb.o2 = pb.o1 + ldo;
+  pb.iperm = p.iperm1;
+  // the weights of this tile's outputs, [k1][b][row], prefetched during the
+  // first stages
   float *sw = reinterpret_cast<float *>(sbuf + FB * pitch);
-  const float *w1 = epi == FFT4_FILTER ? w + r0 * ldw : nullptr;
-  const float *w2 = epi == FFT4_FILTER && has2 ? w1 + ldw : w1;
+  pb.sw = sw;
+  if (epi == FFT4_FILTER) {
+    const float *w1 = w + r0 * ldw;
+    const float *w2 = pb.has2 ? w1 + ldw : w1;
 #pragma unroll 4
-  for (int idx = tid; idx < FB * L1; idx += NT) {
-    const int b = idx % FB, j1 = idx / FB;
-    if (b < nb) cp8(sbuf + b * pitch + __ldg(p.perm1 + j1), Tp + j1 * L2 + k2_0 + b);
-    if (epi == FFT4_FILTER) {
-      const int k = k2_0 + b + L2 * j1;  // j1 plays k1 here
-      const bool ok = b < nb && k <= m;
+    for (int idx = tid; idx < FB * L1; idx += NT) {
+      const int b = idx % FB, k1 = idx / FB;
+      const int k = pb.k2_0 + b + L2 * k1;
+      const bool ok = b < pb.nb && k <= pb.m;
       cp4(sw + 2 * idx, ok ? w1 + k : w1, ok);
-      cp4(sw + 2 * idx + 1, ok ? w2 + k : w1, ok && has2);
+      cp4(sw + 2 * idx + 1, ok ? w2 + k : w1, ok && pb.has2);
     }
+  }
+  const int S = p.nr1;
+  if (S == 1) {
+    cp_async_wait_all();
+    __syncthreads();
+    bstage_r<true, true>(p.r1[0], sbuf, pitch, L1, 1, 1.0f, p.stw1, wt.w, pb);
+    return;
+  }
+  bstage_r<true, false>(p.r1[0], sbuf, pitch, L1, 1, 1.0f, p.stw1, wt.w, pb);
+  __syncthreads();
+  for (int s = 1; s < S - 1; s++) {
+    bstage_r<false, false>(p.r1[s], sbuf, pitch, L1, p.ns1[s], p.inv1[s], p.stw1 + p.to1[s], wt.w, pb);
+    __syncthreads();
   }
   cp_async_wait_all();
   __syncthreads();
-  const int warp = tid >> 5, lane = tid & 31;
-  if (warp < nb) run_stages(sbuf + warp * pitch, L1, p.nr1, p.r1, p.ns1, p.to1, p.inv1, p.stw1, wt.w, lane);
-  __syncthreads();
-  float *o1 = out + r0 * ldo;
-  float *o2 = o1 + ldo;
-  for (int idx = tid; idx < FB * L1; idx += NT) {
-    const int b = idx % FB, k1 = idx / FB;
-    if (b >= nb) continue;
-    const int k = k2_0 + b + L2 * k1;
-    if (k > m) continue;
-    const float2 F = sbuf[b * pitch + k1];
-    float a = F.x, c = F.y;
-    if (epi == FFT4_FILTER) {
-      a *= sw[2 * idx];
-      c *= sw[2 * idx + 1];
-    } else if (epi == FFT4_HALVE && (k == 0 || k == m)) {
-      a *= 0.5f;
-      c *= 0.5f;
-    }
-    o1[k] = a;
-    if (has2) o2[k] = c;
-  }
+  bstage_r<false, true>(p.r1[S - 1], sbuf, pitch, L1, p.ns1[S - 1], p.inv1[S - 1], p.stw1 + p.to1[S - 1], wt.w,
+                        pb);
 }
 
 void factor(int64_t L, std::vector<int> &f) {
@@ -302,7 +383,7 @@ bool radices(int Ls, int *r, int *nr) {
 size_t al(size_t x) { return (x + 255) / 256 * 256; }
 
 struct TableLayout {
-  size_t stw1, stw2, perm1, perm2, tlane, tblk, total;
+  size_t stw1, stw2, perm1, perm2, iperm1, tlane, tblk, total;
 };
 
 TableLayout layout(const Fft4Dev &d) {
@@ -316,6 +397,8 @@ TableLayout layout(const Fft4Dev &d) {
   o += al((size_t)d.L1 * sizeof(int));
   t.perm2 = o;
   o += al((size_t)d.L2 * sizeof(int));
+  t.iperm1 = o;
+  o += al((size_t)d.L1 * sizeof(int));
   t.tlane = o;
   o += al((size_t)d.L1 * 32 * sizeof(float2));
   t.tblk = o;
@@ -380,7 +463,7 @@ bool fft4_shape(int64_t n, Fft4Dev *d) {
   double bc = 1e300;
   for (int64_t a : ds) {
     const int64_t b = L / a;
-    if (a > FFT4_LMAX || b > FFT4_LMAX) continue;
+    if (a > FFT4_LMAX || b > FFT4_LMAX || a == 1) continue;  // pass B needs at least one stage
     const double c = std::fabs(std::log((double)a) - std::log((double)b));
     if (c < bc) {
       bc = c;
@@ -435,6 +518,11 @@ int fft4_init(Fft4Plan *p, int64_t n, void *dev_tables) {
   }
   digit_rev(d.L1, d.r1, d.nr1, (int *)(h.data() + t.perm1));
   digit_rev(d.L2, d.r2, d.nr2, (int *)(h.data() + t.perm2));
+  {
+    const int *P1 = (const int *)(h.data() + t.perm1);
+    int *I1 = (int *)(h.data() + t.iperm1);
+    for (int j = 0; j < d.L1; j++) I1[P1[j]] = j;
+  }
   float2 *tlane = (float2 *)(h.data() + t.tlane), *tblk = (float2 *)(h.data() + t.tblk);
   for (int64_t j1 = 0; j1 < d.L1; j1++) {
     for (int l = 0; l < 32; l++) tlane[32 * j1 + l] = unit((double)(j1 * l % d.L), (double)d.L);
@@ -446,6 +534,7 @@ int fft4_init(Fft4Plan *p, int64_t n, void *dev_tables) {
   d.stw2 = (const float2 *)(b + t.stw2);
   d.perm1 = (const int *)(b + t.perm1);
   d.perm2 = (const int *)(b + t.perm2);
+  d.iperm1 = (const int *)(b + t.iperm1);
   d.tlane = (const float2 *)(b + t.tlane);
   d.tblk = (const float2 *)(b + t.tblk);
   p->tables = dev_tables;
@@ -472,7 +561,7 @@ int fft4_dct(const Fft4Plan &p, const float *x, int64_t ldx, int64_t nrow, float
   k_fft4_a<<<ga, NT, (size_t)FB * (d.L2 + 1) * sizeof(float2), st>>>(x, ldx, nrow, T, d, wt);
   int rc = launch_status("fft4 pass A");
   if (rc) return rc;
-  const size_t smem_b = (size_t)FB * (d.L1 + 1) * sizeof(float2) +
+  const size_t smem_b = (size_t)FB * pitch_b(d.L1) * sizeof(float2) +
                         (epi == FFT4_FILTER ? (size_t)FB * d.L1 * 2 * sizeof(float) : 0);
   k_fft4_b<<<gb, NT, smem_b, st>>>(T, nrow, out, ldo, w, ldw, epi, d, wt);
   return launch_status("fft4 pass B");
