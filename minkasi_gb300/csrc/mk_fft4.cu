@@ -110,54 +110,6 @@ struct Dft<9> : DftOdd<9, WR9> {};
 template <>
 struct Dft<11> : DftOdd<11, WR11> {};
 
-// one in-place decimation-in-time stage of radix R over one transform of
-// length Ls held by a warp, after stages whose radices multiply to Ns; its
-// twiddles W_{Ns R}^{r k} are at stw[(r - 1) Ns + k] (consecutive k of
-// neighbouring lanes are neighbouring entries)
-template <int R>
-__device__ __forceinline__ void stage(float2 *row, int Ls, int Ns, float invNs, const float2 *stw,
-                                     const float2 *wr, int lane) {
-  const int nq = Ls / R;
-  for (int q = lane; q < nq; q += 32) {
-    // q / Ns exactly: q, Ns <= 2048, so (q + 1/2) / Ns is at least 1/(2 Ns)
-    // from an integer, far above the FP32 rounding of the product
-    const int g = __float2int_rz(((float)q + 0.5f) * invNs);
-    const int k = q - g * Ns;
-    float2 *a = row + g * Ns * R + k;
-    float2 v[R];
-#pragma unroll
-    for (int r = 0; r < R; r++) v[r] = a[r * Ns];
-    if (Ns > 1) {
-#pragma unroll
-      for (int r = 1; r < R; r++) v[r] = cmul(v[r], __ldg(stw + (r - 1) * Ns + k));
-    }
-    Dft<R>::run(v, wr);
-#pragma unroll
-    for (int r = 0; r < R; r++) a[r * Ns] = v[r];
-  }
-}
-
-// all stages of one transform (the calling warp's row)
-__device__ void run_stages(float2 *row, int Ls, int nr, const int *rad, const int *ns, const int *to,
-                           const float *inv, const float2 *stw, const float2 *wr, int lane) {
-  for (int s = 0; s < nr; s++) {
-    const int R = rad[s], Ns = ns[s];
-    const float iv = inv[s];
-    const float2 *t = stw + to[s];
-    switch (R) {
-      case 2: stage<2>(row, Ls, Ns, iv, t, wr, lane); break;
-      case 3: stage<3>(row, Ls, Ns, iv, t, wr, lane); break;
-      case 4: stage<4>(row, Ls, Ns, iv, t, wr, lane); break;
-      case 5: stage<5>(row, Ls, Ns, iv, t, wr, lane); break;
-      case 7: stage<7>(row, Ls, Ns, iv, t, wr, lane); break;
-      case 8: stage<8>(row, Ls, Ns, iv, t, wr, lane); break;
-      case 9: stage<9>(row, Ls, Ns, iv, t, wr, lane); break;
-      default: stage<11>(row, Ls, Ns, iv, t, wr, lane); break;
-    }
-    __syncwarp();
-  }
-}
-
 // 4-byte asynchronous global -> shared copy; !valid zero-fills
 // (src must still be a mapped address)
 __device__ __forceinline__ void cp4(void *dst, const void *src, bool valid) {
@@ -169,38 +121,108 @@ struct WrTable {
   float2 w[WRN];
 };
 
+// ---- pass A ------------------------------------------------------------
+// The 8 transforms of the CTA (8 consecutive j1) are interleaved over the
+// threads for the stages (row b = bf % 8): the first stage reads its inputs
+// straight from the detector rows (8 lanes, 8 consecutive samples), forming
+// the even extension; the stages run in shared memory with CTA barriers.
+// Then warp b twiddles row b by W_L^{j1 k2} and stores it to T.
+struct PassA {
+  const float *x1, *x2;
+  bool has2;
+  int L1, j1_0, nb, m, L;
+  const int *iperm;
+};
+
+template <int R, bool FIRST>
+__device__ __forceinline__ void astage(float2 *sbuf, int pitch, int Ls, int Ns, float invNs, const float2 *stw,
+                                       const float2 *wr, const PassA &pa) {
+  const int nq = Ls / R;
+  for (int bf = threadIdx.x; bf < FB * nq; bf += NT) {
+    const int b = bf % FB, q = bf / FB;
+    if (b >= pa.nb) continue;
+    const int g = __float2int_rz(((float)q + 0.5f) * invNs);
+    const int k = q - g * Ns;
+    float2 v[R];
+    float2 *a = sbuf + b * pitch + g * Ns * R + k;
+    if (FIRST) {  // Ns == 1
+      const int jg = __ldg(pa.iperm + q * R);
+#pragma unroll
+      for (int r = 0; r < R; r++) {
+        const int j = pa.j1_0 + b + pa.L1 * (jg + (Ls / R) * r);
+        const int jj = j <= pa.m ? j : pa.L - j;
+        v[r].x = __ldg(pa.x1 + jj);
+        v[r].y = pa.has2 ? __ldg(pa.x2 + jj) : 0.f;
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < R; r++) v[r] = a[r * Ns];
+      if (Ns > 1) {
+#pragma unroll
+        for (int r = 1; r < R; r++) v[r] = cmul(v[r], __ldg(stw + (r - 1) * Ns + k));
+      }
+    }
+    Dft<R>::run(v, wr);
+#pragma unroll
+    for (int r = 0; r < R; r++) a[r * Ns] = v[r];
+  }
+}
+
+template <bool FIRST>
+__device__ __forceinline__ void astage_r(int R, float2 *sbuf, int pitch, int Ls, int Ns, float invNs,
+                                         const float2 *stw, const float2 *wr, const PassA &pa) {
+  switch (R) {
+    case 2: astage<2, FIRST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
+    case 3: astage<3, FIRST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
+    case 4: astage<4, FIRST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
+    case 5: astage<5, FIRST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
+    case 7: astage<7, FIRST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
+    case 8: astage<8, FIRST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
+    case 9: astage<9, FIRST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
+    default: astage<11, FIRST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
+  }
+}
+
+// row pitch (float2) of a tile of 8 interleaved transforms: odd, so the 8
+// rows fall in distinct shared-memory banks
+__host__ __device__ __forceinline__ int pitch_odd(int Ls) { return Ls | 1; }
+
 // pass A: rows (2 pair, 2 pair + 1) of x -> T[pair] (L1 x L2, twiddled)
 __global__ void __launch_bounds__(NT) k_fft4_a(const float *__restrict__ x, int64_t ldx, int64_t nrow,
                                                float2 *__restrict__ T, const Fft4Dev p, const WrTable wt) {
   extern __shared__ float2 sbuf[];
-  const int L1 = p.L1, L2 = p.L2, pitch = L2 + 1, tid = threadIdx.x;
+  const int L1 = p.L1, L2 = p.L2, pitch = pitch_odd(L2), tid = threadIdx.x;
   const int64_t pair = blockIdx.y, r0 = 2 * pair;
-  const bool has2 = r0 + 1 < nrow;
-  const float *x1 = x + r0 * ldx;
-  const float *x2 = has2 ? x1 + ldx : x1;
-  const int j1_0 = blockIdx.x * FB;
-  const int nb = min(FB, L1 - j1_0);
-  const int m = (int)p.m, L = (int)p.L;
-  // every copy of the tile in flight at once
-#pragma unroll 4
-  for (int idx = tid; idx < FB * L2; idx += NT) {
-    const int b = idx % FB, j2 = idx / FB;
-    if (b < nb) {
-      const int j = j1_0 + b + L1 * j2;
-      const int jj = j <= m ? j : L - j;
-      float2 *dst = sbuf + b * pitch + __ldg(p.perm2 + j2);
-      cp4(&dst->x, x1 + jj, true);
-      cp4(&dst->y, x2 + jj, has2);
+  PassA pa;
+  pa.has2 = r0 + 1 < nrow;
+  pa.x1 = x + r0 * ldx;
+  pa.x2 = pa.has2 ? pa.x1 + ldx : pa.x1;
+  pa.L1 = L1;
+  pa.j1_0 = blockIdx.x * FB;
+  pa.nb = min(FB, L1 - pa.j1_0);
+  pa.m = (int)p.m;
+  pa.L = (int)p.L;
+  pa.iperm = p.iperm2;
+  const int S = p.nr2;
+  if (S == 0) {  // L2 == 1: the column is its own transform
+    if (tid < pa.nb) {
+      const int j = pa.j1_0 + tid;
+      const int jj = j <= pa.m ? j : pa.L - j;
+      sbuf[tid * pitch] = make_float2(__ldg(pa.x1 + jj), pa.has2 ? __ldg(pa.x2 + jj) : 0.f);
+    }
+  } else {
+    astage_r<true>(p.r2[0], sbuf, pitch, L2, 1, 1.0f, p.stw2, wt.w, pa);
+    for (int s = 1; s < S; s++) {
+      __syncthreads();
+      astage_r<false>(p.r2[s], sbuf, pitch, L2, p.ns2[s], p.inv2[s], p.stw2 + p.to2[s], wt.w, pa);
     }
   }
-  cp_async_wait_all();
   __syncthreads();
-  // warp b transforms row b, twiddles it by W_L^{j1 k2} and stores it
+  // warp b twiddles row b by W_L^{j1 k2} and stores it
   const int warp = tid >> 5, lane = tid & 31;
-  if (warp >= nb) return;
-  float2 *row = sbuf + warp * pitch;
-  run_stages(row, L2, p.nr2, p.r2, p.ns2, p.to2, p.inv2, p.stw2, wt.w, lane);
-  const int j1 = j1_0 + warp;
+  if (warp >= pa.nb) return;
+  const float2 *row = sbuf + warp * pitch;
+  const int j1 = pa.j1_0 + warp;
   const float2 tl = __ldg(p.tlane + 32 * j1 + lane);
   const float2 *tb = p.tblk + j1 * p.nb32;
   float2 *Tp = T + pair * p.L + j1 * L2;
@@ -290,16 +312,12 @@ __device__ __forceinline__ void bstage_r(int R, float2 *sbuf, int pitch, int Ls,
   }
 }
 
-// row pitch (float2) of the pass-B tile: odd, so the 8 interleaved rows fall
-// in distinct shared-memory banks
-__host__ __device__ __forceinline__ int pitch_b(int L1) { return L1 | 1; }
-
 // pass B: T[pair] -> DCT rows 2 pair, 2 pair + 1 of out (k <= m), epilogue
 __global__ void __launch_bounds__(NT) k_fft4_b(const float2 *__restrict__ T, int64_t nrow, float *__restrict__ out,
                                                int64_t ldo, const float *__restrict__ w, int64_t ldw, int epi,
                                                const Fft4Dev p, const WrTable wt) {
   extern __shared__ float2 sbuf[];
-  const int L1 = p.L1, L2 = p.L2, pitch = pitch_b(L1), tid = threadIdx.x;
+  const int L1 = p.L1, L2 = p.L2, pitch = pitch_odd(L1), tid = threadIdx.x;
   const int64_t pair = blockIdx.y, r0 = 2 * pair;
   PassB pb;
   pb.has2 = r0 + 1 < nrow;
@@ -383,7 +401,7 @@ bool radices(int Ls, int *r, int *nr) {
 size_t al(size_t x) { return (x + 255) / 256 * 256; }
 
 struct TableLayout {
-  size_t stw1, stw2, perm1, perm2, iperm1, tlane, tblk, total;
+  size_t stw1, stw2, iperm1, iperm2, tlane, tblk, total;
 };
 
 TableLayout layout(const Fft4Dev &d) {
@@ -393,12 +411,10 @@ TableLayout layout(const Fft4Dev &d) {
   o += al((size_t)d.L1 * sizeof(float2));
   t.stw2 = o;
   o += al((size_t)d.L2 * sizeof(float2));
-  t.perm1 = o;
-  o += al((size_t)d.L1 * sizeof(int));
-  t.perm2 = o;
-  o += al((size_t)d.L2 * sizeof(int));
   t.iperm1 = o;
   o += al((size_t)d.L1 * sizeof(int));
+  t.iperm2 = o;
+  o += al((size_t)d.L2 * sizeof(int));
   t.tlane = o;
   o += al((size_t)d.L1 * 32 * sizeof(float2));
   t.tblk = o;
@@ -516,12 +532,13 @@ int fft4_init(Fft4Plan *p, int64_t n, void *dev_tables) {
       for (int rr = 1; rr < r[s]; rr++)
         for (int k = 0; k < ns[s]; k++) stw[to[s] + (rr - 1) * ns[s] + k] = unit((double)rr * k, (double)ns[s] * r[s]);
   }
-  digit_rev(d.L1, d.r1, d.nr1, (int *)(h.data() + t.perm1));
-  digit_rev(d.L2, d.r2, d.nr2, (int *)(h.data() + t.perm2));
   {
-    const int *P1 = (const int *)(h.data() + t.perm1);
-    int *I1 = (int *)(h.data() + t.iperm1);
+    std::vector<int> P1(d.L1), P2(d.L2);
+    digit_rev(d.L1, d.r1, d.nr1, P1.data());
+    digit_rev(d.L2, d.r2, d.nr2, P2.data());
+    int *I1 = (int *)(h.data() + t.iperm1), *I2 = (int *)(h.data() + t.iperm2);
     for (int j = 0; j < d.L1; j++) I1[P1[j]] = j;
+    for (int j = 0; j < d.L2; j++) I2[P2[j]] = j;
   }
   float2 *tlane = (float2 *)(h.data() + t.tlane), *tblk = (float2 *)(h.data() + t.tblk);
   for (int64_t j1 = 0; j1 < d.L1; j1++) {
@@ -532,9 +549,8 @@ int fft4_init(Fft4Plan *p, int64_t n, void *dev_tables) {
   char *b = (char *)dev_tables;
   d.stw1 = (const float2 *)(b + t.stw1);
   d.stw2 = (const float2 *)(b + t.stw2);
-  d.perm1 = (const int *)(b + t.perm1);
-  d.perm2 = (const int *)(b + t.perm2);
   d.iperm1 = (const int *)(b + t.iperm1);
+  d.iperm2 = (const int *)(b + t.iperm2);
   d.tlane = (const float2 *)(b + t.tlane);
   d.tblk = (const float2 *)(b + t.tblk);
   p->tables = dev_tables;
@@ -558,10 +574,10 @@ int fft4_dct(const Fft4Plan &p, const float *x, int64_t ldx, int64_t nrow, float
   }
   static const WrTable wt = radix_constants();
   const dim3 ga((d.L1 + FB - 1) / FB, (unsigned)npairs), gb((d.L2 + FB - 1) / FB, (unsigned)npairs);
-  k_fft4_a<<<ga, NT, (size_t)FB * (d.L2 + 1) * sizeof(float2), st>>>(x, ldx, nrow, T, d, wt);
+  k_fft4_a<<<ga, NT, (size_t)FB * pitch_odd(d.L2) * sizeof(float2), st>>>(x, ldx, nrow, T, d, wt);
   int rc = launch_status("fft4 pass A");
   if (rc) return rc;
-  const size_t smem_b = (size_t)FB * pitch_b(d.L1) * sizeof(float2) +
+  const size_t smem_b = (size_t)FB * pitch_odd(d.L1) * sizeof(float2) +
                         (epi == FFT4_FILTER ? (size_t)FB * d.L1 * 2 * sizeof(float) : 0);
   k_fft4_b<<<gb, NT, smem_b, st>>>(T, nrow, out, ldo, w, ldw, epi, d, wt);
   return launch_status("fft4 pass B");

@@ -10,12 +10,12 @@
 //   pass A: for each j1, T[j1][k2] = W_L^{j1 k2} sum_j2 e_{j1 + L1 j2} W_L2^{j2 k2}
 //   pass B: for each k2, F[k2 + L2 k1] = sum_j1 T[j1][k2] W_L1^{j1 k1}
 // Each CTA runs 8 transforms of one pass in shared memory (mixed-radix
-// decimation in time, butterflies in place).  Pass A: one transform per warp,
-// input staged in digit-reversed order, warp barriers between stages; it
-// forms the even extension while loading.  Pass B: the 8 transforms
-// interleaved over the CTA; its first stage reads T directly and its last
-// stage writes only k <= m straight to the rows with the epilogue (plain,
-// times the inverse-spectrum weights, or with columns 0 and m halved).  Twiddles come from tables computed in
+// decimation in time, butterflies in place), interleaved over its threads.
+// The first stage of each pass reads its inputs straight from global memory
+// (pass A forms the even extension there); pass A's rows are then twiddled
+// and stored one per warp; pass B's last stage writes only k <= m straight
+// to the rows with the epilogue (plain, times the inverse-spectrum weights,
+// or with columns 0 and m halved).  Twiddles come from tables computed in
 // double precision on the host.
 #pragma once
 #include <cuda_runtime.h>
@@ -37,8 +37,7 @@ struct Fft4Dev {
   float inv1[FFT4_MAXR], inv2[FFT4_MAXR];
   // stage twiddles W_{Ns R}^{r k} at [to + (r - 1) Ns + k]
   const float2 *stw1, *stw2;
-  const int *perm1, *perm2;  // digit-reversed positions
-  const int *iperm1;          // natural index at each digit-reversed position of pass B
+  const int *iperm1, *iperm2;  // natural index at each digit-reversed (DIT input) position
   // four-step twiddle W_L^{j1 k2} = tblk[j1 nb32 + k2 / 32] * tlane[32 j1 + k2 % 32]
   const float2 *tlane, *tblk;
 };
