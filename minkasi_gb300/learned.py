@@ -349,15 +349,23 @@ def loss_and_grad(net: ConvNet, dsq: torch.Tensor, mask: torch.Tensor, R: torch.
 
 
 def train(net: ConvNet, hits: torch.Tensor, shape, R: torch.Tensor, E: torch.Tensor,
-          epochs: int = 30, batch: int = 64, lr: float = 3e-3, seed: int = 0, log=None) -> List[float]:
-    """Adam on the relative error loss; returns the per-epoch mean loss."""
+          epochs: int = 30, batch: int = 64, lr: float = 3e-3, seed: int = 0, log=None,
+          eps: float = 1e-30) -> List[float]:
+    """Adam on the relative error loss; returns the per-epoch mean loss.
+
+    The loss is invariant to the units of r and e, but the weight gradients
+    are not: K^T K is of degree 8 in the weights, and at the small initial
+    weights the gradients are ~1e-10 on the benchmark maps (smaller still with
+    more hits per pixel).  Adam's usual eps = 1e-8 would then dominate the
+    step and stall training, so eps defaults to a negligible value and the
+    steps scale with lr alone."""
     dev = R.device
     h = hits.reshape(-1).float()
     dsq = torch.where(h > 0, 1.0 / torch.sqrt(h.clamp(min=1e-30)), torch.zeros_like(h))
     mask = (h > 0).float()
     m = [torch.zeros_like(w) for w in net.weights]
     v = [torch.zeros_like(w) for w in net.weights]
-    b1, b2, eps = 0.9, 0.999, 1e-8
+    b1, b2 = 0.9, 0.999
     t = 0
     gen = torch.Generator(device="cpu").manual_seed(seed)
     hist = []
