@@ -324,7 +324,8 @@ def run_large(config: str = "c4", tol: float = 1e-6, max_iter: int = 3000, wall_
         xl, tl = timed(lambda: run_pcg_mixed(b, x0, tv, pre_ms, tol=tol, max_iter=budget, history=hist_l,
                                              inner_precon=mlearn))
         out["learned"] = {"pairs": npairs, "pair_gen_s": t_pairs, "train_s": t_train, "epochs": epochs,
-                          "loss_first": hist_loss[0], "loss_last": hist_loss[-1]}
+                          "loss_first": hist_loss[0], "loss_last": hist_loss[-1],
+                          "weight_rms": [float(w.pow(2).mean().sqrt()) for w in net.weights]}
         out["mixed_learned_solve"] = {"iters": xl.niter, "fp64_residuals": xl.outer, "restarts": xl.restarts,
                                       "wall_s": tl, "true_rel_residual": xl.rel_residual,
                                       "reached_tol": xl.rel_residual <= tol, "replacements": _compact(hist_l)}
