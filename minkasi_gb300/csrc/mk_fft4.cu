@@ -121,6 +121,12 @@ struct WrTable {
   float2 w[WRN];
 };
 
+// Stage indexing shared by both passes: butterfly q of a stage with span Ns
+// is group g = q / Ns, offset k = q % Ns.  The division is done as
+// trunc((q + 1/2) / Ns) in FP32: q < 1536 and Ns <= 1536, so (q + 1/2) / Ns
+// lies at least 1/(2 Ns) from an integer, far above the rounding error of
+// the product (checked exhaustively for all q, Ns < 2048).
+
 // ---- pass A ------------------------------------------------------------
 // The 8 transforms of the CTA (8 consecutive j1) are interleaved over the
 // threads for the stages (row b = bf % 8): the first stage reads its inputs
