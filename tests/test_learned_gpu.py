@@ -40,17 +40,19 @@ def test_conv_kernels_match_oracle(L, cin, cout, H, W):
     assert rel(L.conv_wgrad(t(x), t(y)).cpu().numpy(), lo.conv_wgrad(x, y)) < 1e-5
 
 
-def test_training_gradient_matches_oracle(L):
+# (400, 780) with a batch of 2 gives 650 tiles of 32 x 32, so the
+# convolutions take the large-map tiling
+@pytest.mark.parametrize("shape,B", [((24, 20), 4), ((400, 780), 2)])
+def test_training_gradient_matches_oracle(L, shape, B):
     rng = np.random.default_rng(7)
-    shape = (24, 20)
     n = shape[0] * shape[1]
     ws = [rng.standard_normal((co, ci, 3, 3)) * 0.2
           for ci, co in zip(L.CHANNELS[:-1], L.CHANNELS[1:])]
     hits = rng.integers(0, 6, size=n).astype(float)
     mask = (hits > 0).astype(float)
     dsq = np.where(hits > 0, 1 / np.sqrt(np.maximum(hits, 1)), 0)
-    R = rng.standard_normal((4, n))
-    E = rng.standard_normal((4, n))
+    R = rng.standard_normal((B, n))
+    E = rng.standard_normal((B, n))
     Lref, gref = lo.loss_grad(ws, dsq, mask, R, E, shape)
     net = L.ConvNet([t(w) for w in ws])
     loss, grads = L.loss_and_grad(net, t(dsq), t(mask), t(R), t(E), shape)
