@@ -1,4 +1,6 @@
 // FP32 DCT-I by a four-step FFT in shared memory (see mk_fft4.cuh).
+#include <cufft.h>
+
 #include <cmath>
 #include <vector>
 
@@ -133,14 +135,29 @@ struct WrTable {
 // straight from the detector rows (8 lanes, 8 consecutive samples), forming
 // the even extension; the stages run in shared memory with CTA barriers.
 // Then warp b twiddles row b by W_L^{j1 k2} and stores it to T.
+// what pass A's first stage reads: the rows' even extension (DCT), the same
+// times the Bluestein chirp (zero past 2m), or a complex sequence (U)
+enum { AM_DCT = 0, AM_BLUE = 1, AM_CPLX = 2 };
+
 struct PassA {
   const float *x1, *x2;
+  const float2 *U;  // AM_CPLX: this pair's sequence
+  const float2 *chirp;
   bool has2;
-  int L1, j1_0, nb, m, L;
+  int L1, j1_0, nb, m, Lx;
   const int *iperm;
 };
 
-template <int R, bool FIRST>
+template <int AM>
+__device__ __forceinline__ float2 a_input(const PassA &pa, int j) {
+  if (AM == AM_CPLX) return pa.U[j];
+  if (AM == AM_BLUE && j >= pa.Lx) return make_float2(0.f, 0.f);
+  const int jj = j <= pa.m ? j : pa.Lx - j;
+  const float2 z = make_float2(__ldg(pa.x1 + jj), pa.has2 ? __ldg(pa.x2 + jj) : 0.f);
+  return AM == AM_BLUE ? cmul(z, __ldg(pa.chirp + j)) : z;
+}
+
+template <int R, bool FIRST, int AM>
 __device__ __forceinline__ void astage(float2 *sbuf, int pitch, int Ls, int Ns, float invNs, const float2 *stw,
                                        const float2 *wr, const PassA &pa) {
   const int nq = Ls / R;
@@ -154,12 +171,7 @@ __device__ __forceinline__ void astage(float2 *sbuf, int pitch, int Ls, int Ns, 
     if (FIRST) {  // Ns == 1
       const int jg = __ldg(pa.iperm + q * R);
 #pragma unroll
-      for (int r = 0; r < R; r++) {
-        const int j = pa.j1_0 + b + pa.L1 * (jg + (Ls / R) * r);
-        const int jj = j <= pa.m ? j : pa.L - j;
-        v[r].x = __ldg(pa.x1 + jj);
-        v[r].y = pa.has2 ? __ldg(pa.x2 + jj) : 0.f;
-      }
+      for (int r = 0; r < R; r++) v[r] = a_input<AM>(pa, pa.j1_0 + b + pa.L1 * (jg + (Ls / R) * r));
     } else {
 #pragma unroll
       for (int r = 0; r < R; r++) v[r] = a[r * Ns];
@@ -174,18 +186,18 @@ __device__ __forceinline__ void astage(float2 *sbuf, int pitch, int Ls, int Ns, 
   }
 }
 
-template <bool FIRST>
+template <bool FIRST, int AM>
 __device__ __forceinline__ void astage_r(int R, float2 *sbuf, int pitch, int Ls, int Ns, float invNs,
                                          const float2 *stw, const float2 *wr, const PassA &pa) {
   switch (R) {
-    case 2: astage<2, FIRST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
-    case 3: astage<3, FIRST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
-    case 4: astage<4, FIRST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
-    case 5: astage<5, FIRST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
-    case 7: astage<7, FIRST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
-    case 8: astage<8, FIRST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
-    case 9: astage<9, FIRST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
-    default: astage<11, FIRST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
+    case 2: astage<2, FIRST, AM>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
+    case 3: astage<3, FIRST, AM>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
+    case 4: astage<4, FIRST, AM>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
+    case 5: astage<5, FIRST, AM>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
+    case 7: astage<7, FIRST, AM>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
+    case 8: astage<8, FIRST, AM>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
+    case 9: astage<9, FIRST, AM>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
+    default: astage<11, FIRST, AM>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pa); break;
   }
 }
 
@@ -193,34 +205,35 @@ __device__ __forceinline__ void astage_r(int R, float2 *sbuf, int pitch, int Ls,
 // rows fall in distinct shared-memory banks
 __host__ __device__ __forceinline__ int pitch_odd(int Ls) { return Ls | 1; }
 
-// pass A: rows (2 pair, 2 pair + 1) of x -> T[pair] (L1 x L2, twiddled)
-__global__ void __launch_bounds__(NT) k_fft4_a(const float *__restrict__ x, int64_t ldx, int64_t nrow,
-                                               float2 *__restrict__ T, const Fft4Dev p, const WrTable wt) {
+// pass A: rows (2 pair, 2 pair + 1) of x (or the pair's U) -> T[pair]
+// (L1 x L2, twiddled)
+template <int AM>
+__global__ void __launch_bounds__(NT) k_fft4_a(const float *__restrict__ x, int64_t ldx, const float2 *__restrict__ U,
+                                               int64_t nrow, float2 *__restrict__ T, const Fft4Dev p,
+                                               const WrTable wt) {
   extern __shared__ float2 sbuf[];
   const int L1 = p.L1, L2 = p.L2, pitch = pitch_odd(L2), tid = threadIdx.x;
   const int64_t pair = blockIdx.y, r0 = 2 * pair;
   PassA pa;
   pa.has2 = r0 + 1 < nrow;
-  pa.x1 = x + r0 * ldx;
-  pa.x2 = pa.has2 ? pa.x1 + ldx : pa.x1;
+  pa.x1 = AM == AM_CPLX ? nullptr : x + r0 * ldx;
+  pa.x2 = AM == AM_CPLX ? nullptr : pa.has2 ? pa.x1 + ldx : pa.x1;
+  pa.U = AM == AM_CPLX ? U + pair * p.L : nullptr;
+  pa.chirp = p.chirp;
   pa.L1 = L1;
   pa.j1_0 = blockIdx.x * FB;
   pa.nb = min(FB, L1 - pa.j1_0);
   pa.m = (int)p.m;
-  pa.L = (int)p.L;
+  pa.Lx = (int)p.Lx;
   pa.iperm = p.iperm2;
   const int S = p.nr2;
   if (S == 0) {  // L2 == 1: the column is its own transform
-    if (tid < pa.nb) {
-      const int j = pa.j1_0 + tid;
-      const int jj = j <= pa.m ? j : pa.L - j;
-      sbuf[tid * pitch] = make_float2(__ldg(pa.x1 + jj), pa.has2 ? __ldg(pa.x2 + jj) : 0.f);
-    }
+    if (tid < pa.nb) sbuf[tid * pitch] = a_input<AM>(pa, pa.j1_0 + tid);
   } else {
-    astage_r<true>(p.r2[0], sbuf, pitch, L2, 1, 1.0f, p.stw2, wt.w, pa);
+    astage_r<true, AM>(p.r2[0], sbuf, pitch, L2, 1, 1.0f, p.stw2, wt.w, pa);
     for (int s = 1; s < S; s++) {
       __syncthreads();
-      astage_r<false>(p.r2[s], sbuf, pitch, L2, p.ns2[s], p.inv2[s], p.stw2 + p.to2[s], wt.w, pa);
+      astage_r<false, AM>(p.r2[s], sbuf, pitch, L2, p.ns2[s], p.inv2[s], p.stw2 + p.to2[s], wt.w, pa);
     }
   }
   __syncthreads();
@@ -245,8 +258,15 @@ __global__ void __launch_bounds__(NT) k_fft4_a(const float *__restrict__ x, int6
 // stage reads its inputs straight from T (natural order: position g R0 + r of
 // the digit-reversed layout holds index iperm[g R0] + (L1 / R0) r), and the
 // last stage writes its outputs straight to the DCT rows with the epilogue.
+// what pass B's last stage writes: DCT rows (k <= m, epilogue), the
+// Bluestein product U = conj(F B^) (all k), or the Bluestein result
+// c_k conj(F_k) as DCT rows
+enum { BM_DCT = 0, BM_MUL = 1, BM_BLUE = 2 };
+
 struct PassB {
   const float2 *Tp;  // this pair's T (L1 x L2)
+  float2 *U;         // BM_MUL: this pair's output sequence
+  const float2 *bhat, *chirp;
   int L2, k2_0, nb, m, epi;
   bool has2;
   float *o1, *o2;
@@ -254,7 +274,7 @@ struct PassB {
   const int *iperm;
 };
 
-template <int R, bool FIRST, bool LAST>
+template <int R, bool FIRST, bool LAST, int BM>
 __device__ __forceinline__ void bstage(float2 *sbuf, int pitch, int Ls, int Ns, float invNs, const float2 *stw,
                                        const float2 *wr, const PassB &pb) {
   const int nq = Ls / R;
@@ -283,7 +303,13 @@ __device__ __forceinline__ void bstage(float2 *sbuf, int pitch, int Ls, int Ns, 
       for (int r = 0; r < R; r++) {
         const int k1 = g * Ns * R + k + r * Ns;
         const int kk = pb.k2_0 + b + pb.L2 * k1;
+        if (BM == BM_MUL) {
+          const float2 f = cmul(v[r], __ldg(pb.bhat + kk));
+          pb.U[kk] = make_float2(f.x, -f.y);
+          continue;
+        }
         if (kk > pb.m) continue;
+        if (BM == BM_BLUE) v[r] = cmul(make_float2(v[r].x, -v[r].y), __ldg(pb.chirp + kk));
         float a = v[r].x, c = v[r].y;
         if (pb.epi == FFT4_FILTER) {
           a *= pb.sw[2 * (k1 * FB + b)];
@@ -303,25 +329,27 @@ __device__ __forceinline__ void bstage(float2 *sbuf, int pitch, int Ls, int Ns, 
   }
 }
 
-template <bool FIRST, bool LAST>
+template <bool FIRST, bool LAST, int BM>
 __device__ __forceinline__ void bstage_r(int R, float2 *sbuf, int pitch, int Ls, int Ns, float invNs,
                                          const float2 *stw, const float2 *wr, const PassB &pb) {
   switch (R) {
-    case 2: bstage<2, FIRST, LAST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
-    case 3: bstage<3, FIRST, LAST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
-    case 4: bstage<4, FIRST, LAST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
-    case 5: bstage<5, FIRST, LAST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
-    case 7: bstage<7, FIRST, LAST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
-    case 8: bstage<8, FIRST, LAST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
-    case 9: bstage<9, FIRST, LAST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
-    default: bstage<11, FIRST, LAST>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
+    case 2: bstage<2, FIRST, LAST, BM>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
+    case 3: bstage<3, FIRST, LAST, BM>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
+    case 4: bstage<4, FIRST, LAST, BM>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
+    case 5: bstage<5, FIRST, LAST, BM>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
+    case 7: bstage<7, FIRST, LAST, BM>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
+    case 8: bstage<8, FIRST, LAST, BM>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
+    case 9: bstage<9, FIRST, LAST, BM>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
+    default: bstage<11, FIRST, LAST, BM>(sbuf, pitch, Ls, Ns, invNs, stw, wr, pb); break;
   }
 }
 
-// pass B: T[pair] -> DCT rows 2 pair, 2 pair + 1 of out (k <= m), epilogue
+// pass B: T[pair] -> DCT rows 2 pair, 2 pair + 1 of out (k <= m) with the
+// epilogue, or (BM_MUL) -> the pair's U
+template <int BM>
 __global__ void __launch_bounds__(NT) k_fft4_b(const float2 *__restrict__ T, int64_t nrow, float *__restrict__ out,
-                                               int64_t ldo, const float *__restrict__ w, int64_t ldw, int epi,
-                                               const Fft4Dev p, const WrTable wt) {
+                                               int64_t ldo, float2 *__restrict__ U, const float *__restrict__ w,
+                                               int64_t ldw, int epi, const Fft4Dev p, const WrTable wt) {
   extern __shared__ float2 sbuf[];
   const int L1 = p.L1, L2 = p.L2, pitch = pitch_odd(L1), tid = threadIdx.x;
   const int64_t pair = blockIdx.y, r0 = 2 * pair;
@@ -330,17 +358,20 @@ __global__ void __launch_bounds__(NT) k_fft4_b(const float2 *__restrict__ T, int
   pb.k2_0 = blockIdx.x * FB;
   pb.nb = min(FB, L2 - pb.k2_0);
   pb.Tp = T + pair * p.L;
+  pb.U = BM == BM_MUL ? U + pair * p.L : nullptr;
+  pb.bhat = p.bhat;
+  pb.chirp = p.chirp;
   pb.L2 = L2;
   pb.m = (int)p.m;
   pb.epi = epi;
-  pb.o1 = out + r0 * ldo;
-  pb.o2 = pb.o1 + ldo;
+  pb.o1 = BM == BM_MUL ? nullptr : out + r0 * ldo;
+  pb.o2 = BM == BM_MUL ? nullptr : pb.o1 + ldo;
   pb.iperm = p.iperm1;
   // the weights of this tile's outputs, [k1][b][row], prefetched during the
   // first stages
   float *sw = reinterpret_cast<float *>(sbuf + FB * pitch);
   pb.sw = sw;
-  if (epi == FFT4_FILTER) {
+  if (BM != BM_MUL && epi == FFT4_FILTER) {
     const float *w1 = w + r0 * ldw;
     const float *w2 = pb.has2 ? w1 + ldw : w1;
 #pragma unroll 4
@@ -356,19 +387,19 @@ __global__ void __launch_bounds__(NT) k_fft4_b(const float2 *__restrict__ T, int
   if (S == 1) {
     cp_async_wait_all();
     __syncthreads();
-    bstage_r<true, true>(p.r1[0], sbuf, pitch, L1, 1, 1.0f, p.stw1, wt.w, pb);
+    bstage_r<true, true, BM>(p.r1[0], sbuf, pitch, L1, 1, 1.0f, p.stw1, wt.w, pb);
     return;
   }
-  bstage_r<true, false>(p.r1[0], sbuf, pitch, L1, 1, 1.0f, p.stw1, wt.w, pb);
+  bstage_r<true, false, BM>(p.r1[0], sbuf, pitch, L1, 1, 1.0f, p.stw1, wt.w, pb);
   __syncthreads();
   for (int s = 1; s < S - 1; s++) {
-    bstage_r<false, false>(p.r1[s], sbuf, pitch, L1, p.ns1[s], p.inv1[s], p.stw1 + p.to1[s], wt.w, pb);
+    bstage_r<false, false, BM>(p.r1[s], sbuf, pitch, L1, p.ns1[s], p.inv1[s], p.stw1 + p.to1[s], wt.w, pb);
     __syncthreads();
   }
   cp_async_wait_all();
   __syncthreads();
-  bstage_r<false, true>(p.r1[S - 1], sbuf, pitch, L1, p.ns1[S - 1], p.inv1[S - 1], p.stw1 + p.to1[S - 1], wt.w,
-                        pb);
+  bstage_r<false, true, BM>(p.r1[S - 1], sbuf, pitch, L1, p.ns1[S - 1], p.inv1[S - 1], p.stw1 + p.to1[S - 1],
+                            wt.w, pb);
 }
 
 void factor(int64_t L, std::vector<int> &f) {
@@ -407,7 +438,7 @@ bool radices(int Ls, int *r, int *nr) {
 size_t al(size_t x) { return (x + 255) / 256 * 256; }
 
 struct TableLayout {
-  size_t stw1, stw2, iperm1, iperm2, tlane, tblk, total;
+  size_t stw1, stw2, iperm1, iperm2, tlane, tblk, chirp, bhat, total;
 };
 
 TableLayout layout(const Fft4Dev &d) {
@@ -425,6 +456,10 @@ TableLayout layout(const Fft4Dev &d) {
   o += al((size_t)d.L1 * 32 * sizeof(float2));
   t.tblk = o;
   o += al((size_t)d.L1 * d.nb32 * sizeof(float2));
+  t.chirp = o;
+  o += d.blue ? al((size_t)d.Lx * sizeof(float2)) : 0;
+  t.bhat = o;
+  o += d.blue ? al((size_t)d.L * sizeof(float2)) : 0;
   t.total = o;
   return t;
 }
@@ -464,13 +499,13 @@ bool g_attr[64] = {false};
 
 }  // namespace
 
-bool fft4_shape(int64_t n, Fft4Dev *d) {
-  if (n < 2 || n > (int64_t)FFT4_LMAX * FFT4_LMAX / 2) return false;
-  const int64_t m = n - 1, L = 2 * m;
+// L1 x L2 split of a transform of length L (the divisor pair closest to
+// sqrt(L) with both parts <= LMAX and L1 > 1), radices and stage constants
+static bool split_len(int64_t L, Fft4Dev *t) {
+  if (L < 2 || L > (int64_t)FFT4_LMAX * FFT4_LMAX) return false;
   std::vector<int> f;
   factor(L, f);
   if (f.empty()) return false;
-  // divisors of L; the one closest to sqrt(L) with both parts <= LMAX
   std::vector<int64_t> ds{1};
   for (int pr : f) {
     const size_t k = ds.size();
@@ -493,19 +528,16 @@ bool fft4_shape(int64_t n, Fft4Dev *d) {
     }
   }
   if (best < 0) return false;
-  Fft4Dev t{};
-  t.n = n;
-  t.m = m;
-  t.L = L;
-  t.L1 = (int)best;
-  t.L2 = (int)(L / best);
-  if (!radices(t.L1, t.r1, &t.nr1) || !radices(t.L2, t.r2, &t.nr2)) return false;
-  t.nb32 = (t.L2 + 31) / 32;
+  t->L = L;
+  t->L1 = (int)best;
+  t->L2 = (int)(L / best);
+  if (!radices(t->L1, t->r1, &t->nr1) || !radices(t->L2, t->r2, &t->nr2)) return false;
+  t->nb32 = (t->L2 + 31) / 32;
   for (int pass = 0; pass < 2; pass++) {
-    const int nr = pass ? t.nr2 : t.nr1;
-    const int *r = pass ? t.r2 : t.r1;
-    int *ns = pass ? t.ns2 : t.ns1, *to = pass ? t.to2 : t.to1;
-    float *inv = pass ? t.inv2 : t.inv1;
+    const int nr = pass ? t->nr2 : t->nr1;
+    const int *r = pass ? t->r2 : t->r1;
+    int *ns = pass ? t->ns2 : t->ns1, *to = pass ? t->to2 : t->to1;
+    float *inv = pass ? t->inv2 : t->inv1;
     int span = 1, off = 0;
     for (int s = 0; s < nr; s++) {
       ns[s] = span;
@@ -515,18 +547,71 @@ bool fft4_shape(int64_t n, Fft4Dev *d) {
       span *= r[s];
     }
   }
-  *d = t;
   return true;
+}
+
+bool fft4_shape(int64_t n, Fft4Dev *d, bool bluestein) {
+  if (n < 2 || n > (int64_t)FFT4_LMAX * FFT4_LMAX / 2) return false;
+  Fft4Dev t{};
+  t.n = n;
+  t.m = n - 1;
+  t.Lx = 2 * t.m;
+  if (split_len(t.Lx, &t)) {
+    t.blue = false;
+    *d = t;
+    return true;
+  }
+  if (!bluestein) return false;
+  for (int64_t M = 2 * t.Lx - 1; M <= (int64_t)FFT4_LMAX * FFT4_LMAX; M++) {
+    if (split_len(M, &t)) {
+      t.blue = true;
+      *d = t;
+      return true;
+    }
+  }
+  return false;
 }
 
 size_t fft4_table_bytes(const Fft4Dev &d) { return layout(d).total; }
 
 size_t fft4_t_bytes(const Fft4Dev &d, int64_t nrow) {
-  return (size_t)((nrow + 1) / 2) * (size_t)d.L * sizeof(float2);
+  return (d.blue ? 2 : 1) * (size_t)((nrow + 1) / 2) * (size_t)d.L * sizeof(float2);
 }
 
-int fft4_init(Fft4Plan *p, int64_t n, void *dev_tables) {
-  MK_CHECK_ARG(fft4_shape(n, &p->d), "fft4: row length %lld has no supported factorisation", (long long)n);
+// B^ = DFT_M(b) / M with b_t = conj(c_t) at t mod M for |t| < Lx, in double
+// precision through a cuFFT Z2Z transform, rounded to float
+static int bluestein_bhat(const Fft4Dev &d, float2 *out) {
+  const int64_t M = d.L, Lx = d.Lx;
+  std::vector<cufftDoubleComplex> b((size_t)M);
+  for (auto &v : b) v.x = v.y = 0.0;
+  for (int64_t t = 0; t < Lx; t++) {
+    const double a = M_PI * (double)((t * t) % (2 * Lx)) / (double)Lx;  // conj(c_t) = exp(+i a)
+    b[(size_t)t].x = std::cos(a);
+    b[(size_t)t].y = std::sin(a);
+    if (t > 0) b[(size_t)(M - t)] = b[(size_t)t];
+  }
+  cufftDoubleComplex *db = nullptr;
+  MK_CUDA(cudaMalloc(&db, (size_t)M * sizeof(cufftDoubleComplex)));
+  int rc = MK_OK;
+  cufftHandle h = 0;
+  if (cudaMemcpy(db, b.data(), (size_t)M * sizeof(cufftDoubleComplex), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cufftPlan1d(&h, (int)M, CUFFT_Z2Z, 1) != CUFFT_SUCCESS ||
+      cufftExecZ2Z(h, db, db, CUFFT_FORWARD) != CUFFT_SUCCESS ||
+      cudaMemcpy(b.data(), db, (size_t)M * sizeof(cufftDoubleComplex), cudaMemcpyDeviceToHost) != cudaSuccess) {
+    set_error("fft4: Bluestein kernel transform (M = %lld) failed", (long long)M);
+    rc = MK_ERR_CUFFT;
+  }
+  if (h) cufftDestroy(h);
+  cudaFree(db);
+  if (rc) return rc;
+  for (int64_t k = 0; k < M; k++)
+    out[k] = make_float2((float)(b[(size_t)k].x / (double)M), (float)(b[(size_t)k].y / (double)M));
+  return MK_OK;
+}
+
+int fft4_init(Fft4Plan *p, int64_t n, void *dev_tables, bool bluestein) {
+  MK_CHECK_ARG(fft4_shape(n, &p->d, bluestein), "fft4: row length %lld has no supported factorisation",
+               (long long)n);
   Fft4Dev &d = p->d;
   const TableLayout t = layout(d);
   std::vector<char> h(t.total, 0);
@@ -551,6 +636,12 @@ int fft4_init(Fft4Plan *p, int64_t n, void *dev_tables) {
     for (int l = 0; l < 32; l++) tlane[32 * j1 + l] = unit((double)(j1 * l % d.L), (double)d.L);
     for (int i = 0; i < d.nb32; i++) tblk[j1 * d.nb32 + i] = unit((double)(j1 * 32 * i % d.L), (double)d.L);
   }
+  if (d.blue) {
+    float2 *chirp = (float2 *)(h.data() + t.chirp);
+    for (int64_t j = 0; j < d.Lx; j++) chirp[j] = unit((double)((j * j) % (2 * d.Lx)), 2.0 * (double)d.Lx);
+    const int rc = bluestein_bhat(d, (float2 *)(h.data() + t.bhat));
+    if (rc) return rc;
+  }
   MK_CUDA(cudaMemcpy(dev_tables, h.data(), t.total, cudaMemcpyHostToDevice));
   char *b = (char *)dev_tables;
   d.stw1 = (const float2 *)(b + t.stw1);
@@ -559,6 +650,8 @@ int fft4_init(Fft4Plan *p, int64_t n, void *dev_tables) {
   d.iperm2 = (const int *)(b + t.iperm2);
   d.tlane = (const float2 *)(b + t.tlane);
   d.tblk = (const float2 *)(b + t.tblk);
+  d.chirp = d.blue ? (const float2 *)(b + t.chirp) : nullptr;
+  d.bhat = d.blue ? (const float2 *)(b + t.bhat) : nullptr;
   p->tables = dev_tables;
   return MK_OK;
 }
@@ -574,19 +667,35 @@ int fft4_dct(const Fft4Plan &p, const float *x, int64_t ldx, int64_t nrow, float
   MK_CUDA(cudaGetDevice(&dev));
   if (dev >= 0 && dev < 64 && !g_attr[dev]) {
     const int mx = FB * (FFT4_LMAX + 1) * (int)sizeof(float2) + FB * FFT4_LMAX * 2 * (int)sizeof(float);
-    MK_CUDA(cudaFuncSetAttribute(k_fft4_a, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    MK_CUDA(cudaFuncSetAttribute(k_fft4_b, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    MK_CUDA(cudaFuncSetAttribute(k_fft4_a<AM_DCT>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    MK_CUDA(cudaFuncSetAttribute(k_fft4_a<AM_BLUE>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    MK_CUDA(cudaFuncSetAttribute(k_fft4_a<AM_CPLX>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    MK_CUDA(cudaFuncSetAttribute(k_fft4_b<BM_DCT>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    MK_CUDA(cudaFuncSetAttribute(k_fft4_b<BM_MUL>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    MK_CUDA(cudaFuncSetAttribute(k_fft4_b<BM_BLUE>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     g_attr[dev] = true;
   }
   static const WrTable wt = radix_constants();
   const dim3 ga((d.L1 + FB - 1) / FB, (unsigned)npairs), gb((d.L2 + FB - 1) / FB, (unsigned)npairs);
-  k_fft4_a<<<ga, NT, (size_t)FB * pitch_odd(d.L2) * sizeof(float2), st>>>(x, ldx, nrow, T, d, wt);
-  int rc = launch_status("fft4 pass A");
-  if (rc) return rc;
-  const size_t smem_b = (size_t)FB * pitch_odd(d.L1) * sizeof(float2) +
-                        (epi == FFT4_FILTER ? (size_t)FB * d.L1 * 2 * sizeof(float) : 0);
-  k_fft4_b<<<gb, NT, smem_b, st>>>(T, nrow, out, ldo, w, ldw, epi, d, wt);
-  return launch_status("fft4 pass B");
+  const size_t smem_a = (size_t)FB * pitch_odd(d.L2) * sizeof(float2);
+  const size_t smem_b = (size_t)FB * pitch_odd(d.L1) * sizeof(float2);
+  const size_t smem_w = epi == FFT4_FILTER ? (size_t)FB * d.L1 * 2 * sizeof(float) : 0;
+  int rc;
+  if (!d.blue) {
+    k_fft4_a<AM_DCT><<<ga, NT, smem_a, st>>>(x, ldx, nullptr, nrow, T, d, wt);
+    if ((rc = launch_status("fft4 pass A"))) return rc;
+    k_fft4_b<BM_DCT><<<gb, NT, smem_b + smem_w, st>>>(T, nrow, out, ldo, nullptr, w, ldw, epi, d, wt);
+    return launch_status("fft4 pass B");
+  }
+  float2 *U = T + npairs * d.L;
+  k_fft4_a<AM_BLUE><<<ga, NT, smem_a, st>>>(x, ldx, nullptr, nrow, T, d, wt);
+  if ((rc = launch_status("fft4 Bluestein pass A"))) return rc;
+  k_fft4_b<BM_MUL><<<gb, NT, smem_b, st>>>(T, nrow, nullptr, 0, U, nullptr, 0, FFT4_PLAIN, d, wt);
+  if ((rc = launch_status("fft4 Bluestein pass B"))) return rc;
+  k_fft4_a<AM_CPLX><<<ga, NT, smem_a, st>>>(nullptr, 0, U, nrow, T, d, wt);
+  if ((rc = launch_status("fft4 Bluestein pass A (second)"))) return rc;
+  k_fft4_b<BM_BLUE><<<gb, NT, smem_b + smem_w, st>>>(T, nrow, out, ldo, nullptr, w, ldw, epi, d, wt);
+  return launch_status("fft4 Bluestein pass B (second)");
 }
 
 }  // namespace mk

@@ -17,6 +17,15 @@
 // to the rows with the epilogue (plain, times the inverse-spectrum weights,
 // or with columns 0 and m halved).  Twiddles come from tables computed in
 // double precision on the host.
+//
+// Lengths whose 2m has a prime factor above 11 (minkasi's truncate_tod leaves
+// some) go through Bluestein's algorithm on the same passes: with the chirp
+// c_j = exp(-i pi j^2 / L), DFT(z)_k = c_k (a (*) b)_k, a_j = z_j c_j (zero
+// past L), b_t = conj(c_t) for |t| < L, a circular convolution of a smooth
+// length M >= 2L - 1:  pass A forms a from the rows; pass B multiplies by
+// B^ = DFT_M(b) / M and stores U = conj(DFT(a) B^); pass A and pass B run
+// again on U, and the last stage writes c_k conj(DFT(U)_k) for k <= m with the
+// usual epilogue.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -28,7 +37,9 @@ constexpr int FFT4_MAXR = 16;    // most radix stages of one pass
 
 // device view of a plan (kernel argument)
 struct Fft4Dev {
-  int64_t n, m, L;
+  int64_t n, m, L;  // row length, m = n - 1, transform length (2m, or M for Bluestein)
+  int64_t Lx;       // even-extension length 2m
+  bool blue;        // Bluestein: L = M, chirp and bhat set
   int L1, L2, nb32;  // nb32 = ceil(L2 / 32)
   int nr1, nr2;
   int r1[FFT4_MAXR], r2[FFT4_MAXR];
@@ -40,6 +51,8 @@ struct Fft4Dev {
   const int *iperm1, *iperm2;  // natural index at each digit-reversed (DIT input) position
   // four-step twiddle W_L^{j1 k2} = tblk[j1 nb32 + k2 / 32] * tlane[32 j1 + k2 % 32]
   const float2 *tlane, *tblk;
+  const float2 *chirp;  // Bluestein: c_j, j < Lx
+  const float2 *bhat;   // Bluestein: DFT_M(b) / M
 };
 
 // epilogues of pass B
@@ -47,18 +60,21 @@ enum { FFT4_PLAIN = 0, FFT4_FILTER = 1, FFT4_HALVE = 2 };
 
 struct Fft4Plan {
   Fft4Dev d{};
-  void *tables = nullptr;  // device tables inside the caller's workspace
+  void *tables = nullptr;  // device tables (plan-owned memory)
 };
 
-// Split of L = 2(n-1) into L1 x L2, radix lists; false when L has a prime
-// factor above 11 or cannot be split within FFT4_LMAX.
-bool fft4_shape(int64_t n, Fft4Dev *d);
+// The transform for rows of length n: L = 2(n-1) split into L1 x L2 with
+// radix lists, or, when 2(n-1) has a prime factor above 11 and `bluestein`
+// is set, the smallest splittable M >= 4(n-1) - 1; false when neither fits
+// within FFT4_LMAX x FFT4_LMAX.
+bool fft4_shape(int64_t n, Fft4Dev *d, bool bluestein = true);
 // bytes of the device tables for that shape
 size_t fft4_table_bytes(const Fft4Dev &d);
-// bytes of the intermediate T for nrow rows
+// bytes of the scratch (T, and U for Bluestein) for nrow rows
 size_t fft4_t_bytes(const Fft4Dev &d, int64_t nrow);
-// computes the tables on the host and uploads them to `dev_tables`
-int fft4_init(Fft4Plan *p, int64_t n, void *dev_tables);
+// computes the tables on the host (B^ with a double-precision cuFFT
+// transform) and uploads them to `dev_tables`
+int fft4_init(Fft4Plan *p, int64_t n, void *dev_tables, bool bluestein = true);
 // out rows (ld ldo) = DCT-I of x rows (ld ldx) with the given epilogue;
 // T is scratch of fft4_t_bytes; w (ld ldw) only for FFT4_FILTER.
 int fft4_dct(const Fft4Plan &p, const float *x, int64_t ldx, int64_t nrow, float2 *T, float *out,

@@ -22,11 +22,13 @@
 // second rotation reads Re F in place and halves while splitting, so k_mirror
 // and k_real_halve do not run.
 //
-// FP32 plans whose length factors into 2, 3, 5, 7, 11 (every length the
-// reference's truncation produces) use the four-step shared-memory FFT of
-// mk_fft4.cu instead of cuFFT:  E = v . dat;  E = DCT(E) * mywt;
-// E = DCT(E) with columns 0 and n-1 halved;  out = vT . E.  Each DCT is two
-// kernels that form the even extension while loading and apply the weights
+// FP32 plans use the four-step shared-memory FFT of mk_fft4.cu instead of
+// cuFFT (directly when 2(n-1) factors into 2, 3, 5, 7, 11; through
+// Bluestein's algorithm otherwise, up to its length limit):
+//   E = v . dat;  E = DCT(E) * mywt;  E = DCT(E) with columns 0 and n-1
+//   halved;  out = vT . E.
+// Each DCT is two kernels (four with Bluestein) that form the even
+// extension while loading and apply the weights
 // or the halving while storing, two detector rows per complex transform.
 #include <cublas_v2.h>
 #include <cufft.h>
@@ -140,7 +142,8 @@ dim3 rows_grid(int64_t n, int64_t nrow) {
 }
 
 // ---- plan object -----------------------------------------------------------
-// 0: four-step FFT for FP32 where the length allows, cuFFT otherwise; 1: cuFFT
+// 0: four-step FFT for FP32 (Bluestein on it for lengths with a prime factor
+// above 11), cuFFT otherwise; 1: cuFFT; 2: four-step for smooth lengths only
 std::atomic<int> g_engine{0};
 
 struct DctCore {
@@ -203,8 +206,10 @@ int make_fft(cufftHandle *h, int64_t nrow, int64_t N, int dtype, size_t *work) {
   return MK_OK;
 }
 
-bool use_own(int64_t nrow, int64_t n, int dtype, mk::Fft4Dev *d) {
-  return dtype == MK_F32 && g_engine.load() == 0 && (nrow + 1) / 2 <= 65535 && mk::fft4_shape(n, d);
+bool use_own(int64_t nrow, int64_t n, int dtype, mk::Fft4Dev *d, bool *blue_ok) {
+  const int e = g_engine.load();
+  *blue_ok = e == 0;
+  return dtype == MK_F32 && e != 1 && (nrow + 1) / 2 <= 65535 && mk::fft4_shape(n, d, *blue_ok);
 }
 
 int core_bytes(int64_t nrow, int64_t n, int dtype, size_t *bytes) {
@@ -213,7 +218,8 @@ int core_bytes(int64_t nrow, int64_t n, int dtype, size_t *bytes) {
   MK_CHECK_ARG(nrow >= 1 && n >= 2, "DCT-I needs nrow >= 1 and n >= 2 (got %lld, %lld)",
                (long long)nrow, (long long)n);
   mk::Fft4Dev d;
-  if (use_own(nrow, n, dtype, &d)) {
+  bool blue_ok;
+  if (use_own(nrow, n, dtype, &d, &blue_ok)) {
     *bytes = align_up((size_t)nrow * n * sizeof(float)) + align_up(mk::fft4_t_bytes(d, nrow)) +
              tc_bytes(nrow, dtype);
     return MK_OK;
@@ -241,7 +247,8 @@ int core_create(DctCore *c, int64_t nrow, int64_t n, int dtype, void *ws, size_t
   c->dtype = dtype;
   char *p = (char *)ws;
   mk::Fft4Dev d;
-  if (use_own(nrow, n, dtype, &d)) {
+  bool blue_ok;
+  if (use_own(nrow, n, dtype, &d, &blue_ok)) {
     c->own = true;
     c->E = p;
     p += align_up((size_t)nrow * n * sizeof(float));
@@ -249,7 +256,7 @@ int core_create(DctCore *c, int64_t nrow, int64_t n, int dtype, void *ws, size_t
     p += align_up(mk::fft4_t_bytes(d, nrow));
     if (tc_bytes(nrow, dtype)) c->tc_bimg = p;
     if ((rc = own_alloc(c, mk::fft4_table_bytes(d))) ||
-        (rc = mk::fft4_init(&c->f4, n, (char *)c->owned + 256))) {
+        (rc = mk::fft4_init(&c->f4, n, (char *)c->owned + 256, blue_ok))) {
       core_free(c);
       return rc;
     }
@@ -525,13 +532,15 @@ extern "C" int mk_noise_status(mk_noise_plan *plan, int *code, void *stream) {
 }
 
 extern "C" int mk_set_dct_engine(int engine) {
-  MK_CHECK_ARG(engine == 0 || engine == 1, "mk_set_dct_engine: engine must be 0 or 1 (got %d)", engine);
+  MK_CHECK_ARG(engine >= 0 && engine <= 2, "mk_set_dct_engine: engine must be 0, 1 or 2 (got %d)", engine);
   g_engine.store(engine);
   return MK_OK;
 }
 
 extern "C" int mk_get_dct_engine(void) { return g_engine.load(); }
 
-extern "C" int mk_dct1_engine(const mk_dct_plan *plan) { return plan && plan->core.own ? 0 : 1; }
+static int engine_of(const DctCore &c) { return !c.own ? 1 : c.f4.d.blue ? 2 : 0; }
 
-extern "C" int mk_noise_engine(const mk_noise_plan *plan) { return plan && plan->core.own ? 0 : 1; }
+extern "C" int mk_dct1_engine(const mk_dct_plan *plan) { return plan ? engine_of(plan->core) : 1; }
+
+extern "C" int mk_noise_engine(const mk_noise_plan *plan) { return plan ? engine_of(plan->core) : 1; }

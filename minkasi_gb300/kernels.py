@@ -382,8 +382,10 @@ def _workspace(nbytes: int, device) -> torch.Tensor:
 
 def set_dct_engine(engine: int) -> None:
     """Transform used by DCT / noise plans created from now on: 0 (default)
-    the four-step shared-memory FFT for FP32 rows whose length factors into
-    2, 3, 5, 7, 11, cuFFT otherwise; 1 cuFFT always."""
+    the four-step shared-memory FFT for FP32 rows (through Bluestein's
+    algorithm when 2(n-1) has a prime factor above 11), cuFFT for FP64;
+    1 cuFFT always; 2 the four-step FFT only where 2(n-1) factors into
+    2, 3, 5, 7, 11."""
     check(lib().mk_set_dct_engine(int(engine)), "set_dct_engine")
 
 
@@ -419,7 +421,7 @@ class DCT1:
 
     @property
     def engine(self) -> int:
-        """0: four-step FFT, 1: cuFFT."""
+        """0: four-step FFT, 2: four-step FFT through Bluestein, 1: cuFFT."""
         return int(lib().mk_dct1_engine(self._h))
 
     def __del__(self):
@@ -458,7 +460,7 @@ class NoisePlan:
 
     @property
     def engine(self) -> int:
-        """0: four-step FFT, 1: cuFFT."""
+        """0: four-step FFT, 2: four-step FFT through Bluestein, 1: cuFFT."""
         return int(lib().mk_noise_engine(self._h))
 
     def rotate(self, A: torch.Tensor, X: torch.Tensor, out: Optional[torch.Tensor] = None,

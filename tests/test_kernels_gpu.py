@@ -208,25 +208,41 @@ def test_dct1_f32_four_step(K, nrow, n):
     assert np.linalg.norm(y - ref) < 2e-6 * np.linalg.norm(ref)
 
 
+@pytest.mark.parametrize("nrow,n", [(3, 38), (3, 1000), (4, 700), (5, 18623), (2, 465551), (16, 144278)])
+def test_dct1_f32_bluestein(K, nrow, n):
+    """Lengths whose 2(n-1) has a prime factor above 11 (37, 37, 233, 9311,
+    9311, 72139): Bluestein's algorithm on the four-step passes, against the
+    FP64 oracle; the last two are c2 TOD lengths."""
+    x = np.random.default_rng(n).standard_normal((nrow, n))
+    d = K.DCT1(nrow, n, torch.float32)
+    assert d.engine == 2
+    y = d(dev(x, torch.float32)).cpu().numpy()
+    ref = oracle.dct1(x)
+    assert rel(y, ref) < 1e-5
+    assert np.linalg.norm(y - ref) < 4e-6 * np.linalg.norm(ref)
+
+
 def test_dct1_engines_agree_and_fall_back(K):
     x = np.random.default_rng(9).standard_normal((6, 2311))
     own = K.DCT1(6, 2311, torch.float32)(dev(x, torch.float32)).cpu().numpy()
+    x2 = np.random.default_rng(10).standard_normal((3, 1000))
     try:
         K.set_dct_engine(1)
         assert K.dct_engine() == 1
         d = K.DCT1(6, 2311, torch.float32)
         assert d.engine == 1
         ref = d(dev(x, torch.float32)).cpu().numpy()
+        # engine 2: the four-step FFT for smooth lengths only, cuFFT for the rest
+        K.set_dct_engine(2)
+        assert K.DCT1(6, 2311, torch.float32).engine == 0
+        d2 = K.DCT1(3, 1000, torch.float32)
+        assert d2.engine == 1
+        assert rel(d2(dev(x2, torch.float32)).cpu().numpy(), oracle.dct1(x2)) < 3e-6
     finally:
         K.set_dct_engine(0)
     assert rel(own, ref) < 3e-6
-    # 2(n-1) = 2 * 27 * 37 has a factor above 11: cuFFT
-    x = np.random.default_rng(10).standard_normal((3, 1000))
-    d = K.DCT1(3, 1000, torch.float32)
-    assert d.engine == 1
-    assert rel(d(dev(x, torch.float32)).cpu().numpy(), oracle.dct1(x)) < 3e-6
     with pytest.raises(Exception):
-        K.set_dct_engine(2)
+        K.set_dct_engine(3)
 
 
 @pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
@@ -235,7 +251,7 @@ def test_noise_plans_sharing_one_workspace(K, dtype):
     builds them), used alternately: each gives what it gives on a workspace
     of its own.  Plan state (transform tables, status word) must not live in
     the shared workspace."""
-    shapes = [(16, 3529), (16, 4236), (32, 4097)]
+    shapes = [(16, 3529), (16, 4236), (32, 4097), (16, 1000)]  # the last through Bluestein in FP32
     ws_bytes = max(K.noise_workspace_bytes(nd, n, dtype) for nd, n in shapes)
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
     rng = np.random.default_rng(11)
