@@ -4,13 +4,14 @@ the choice in a JSON file keyed on (GPU, dtype, detector counts, samples,
 map size, hit density).
 
 Cache file: $MINKASI_GB300_AUTOTUNE, else ~/.cache/minkasi_gb300/autotune.json.
-Set MINKASI_GB300_TOD2MAP=atomic|staged|fixed|sorted (or ..._ROT=1|2|3) to force a choice.
+Set MINKASI_GB300_TOD2MAP=atomic|staged|fixed|sorted (or ..._ROT=1|2|3, or
+..._DCT=0|1|2, the kernels.set_dct_engine values) to force a choice.
 """
 from __future__ import annotations
 
 import json
 import os
-from typing import Dict, Iterable, Optional
+from typing import Dict, Iterable, Optional, Sequence, Tuple
 
 import numpy as np
 import torch
@@ -134,3 +135,59 @@ def choose_rot_mode(op) -> int:
     best = min(times, key=times.get)
     _store(key, best)
     return best
+
+
+def with_dct_engine(engine: int, fn):
+    """fn() with kernels.set_dct_engine(engine) in force (plans created in fn
+    keep it), then the previous engine restored."""
+    prev = K.dct_engine()
+    K.set_dct_engine(engine)
+    try:
+        return fn()
+    finally:
+        K.set_dct_engine(prev)
+
+
+def choose_dct_engines(op, shapes: Sequence[Tuple[int, int]]) -> Dict[Tuple[int, int], int]:
+    """Per TOD shape of an FP32 operator, the faster noise filter of the
+    four-step FFT (engine 0, Bluestein included) and cuFFT (engine 1), timed
+    on the shape's first TOD with the rotation the shape will use; FP64
+    operators keep the current engine (their plans use cuFFT)."""
+    cur = K.dct_engine()
+    if op.dtype != torch.float32:
+        return {s: cur for s in shapes}
+    forced = os.environ.get("MINKASI_GB300_DCT")
+    if forced:
+        return {s: int(forced) for s in shapes}
+    gpu = torch.cuda.get_device_name(op.device)
+    out, todo = {}, []
+    for s in shapes:
+        hit = _lookup(f"dct|{gpu}|{s[0]}x{s[1]}")
+        if hit in (0, 1):
+            out[s] = int(hit)
+        else:
+            todo.append(s)
+    if not todo:
+        return out
+    need = max(with_dct_engine(e, lambda s=s: K.noise_workspace_bytes(s[0], s[1], op.dtype))
+               for s in todo for e in (0, 1))
+    ws = torch.empty(need, dtype=torch.uint8, device=op.device)
+    for s in todo:
+        nd, n = s
+        v, vT, w = op.ops[op.dims.index(s)]
+        x = torch.randn((nd, n), dtype=op.dtype, device=op.device)
+        y = torch.empty_like(x)
+        mode = 2 if nd in (32, 64, 128, 256) else 1
+        times = {}
+        for e in (0, 1):
+            plan = with_dct_engine(e, lambda: K.NoisePlan(nd, n, op.dtype, op.device, workspace=ws))
+            if e == 0 and plan.engine == 1:
+                break  # no four-step transform for this length
+            times[e] = time_ms(lambda: plan.apply(v, vT, w, x, out=y, rot_mode=mode))
+            del plan
+        best = min(times, key=times.get) if times else 1
+        out[s] = best
+        _store(f"dct|{gpu}|{nd}x{n}", best)
+        del x, y
+    del ws
+    return out

@@ -82,14 +82,21 @@ class MapmakingOperator:
             return
         self.ops = [t.noise.operands(self.dtype) for t in self.tods]
         shapes = sorted(set(self.dims))
-        ws_bytes = max(K.noise_workspace_bytes(nd, n, self.dtype) for nd, n in shapes)
+        from .autotune import choose_dct_engines, with_dct_engine
+        # the DCT-I transform per shape (FP32: four-step FFT or cuFFT,
+        # whichever runs this shape's filter faster)
+        engines = choose_dct_engines(self, shapes)
+        ws_bytes = max(with_dct_engine(engines[s], lambda s=s: K.noise_workspace_bytes(s[0], s[1], self.dtype))
+                       for s in shapes)
         self.ws = torch.empty(ws_bytes, dtype=torch.uint8, device=self.device)
         # cuFFT allocates its plan tables with cudaMalloc, outside torch's
         # caching allocator: hand back cached blocks first so a near-full
         # device can still build one plan per distinct TOD shape.
         torch.cuda.empty_cache()
-        self.plans = {s: K.NoisePlan(s[0], s[1], self.dtype, self.device, workspace=self.ws)
+        self.plans = {s: with_dct_engine(engines[s], lambda s=s: K.NoisePlan(s[0], s[1], self.dtype, self.device,
+                                                                             workspace=self.ws))
                       for s in shapes}
+        self.dct_engines = {s: p.engine for s, p in self.plans.items()}
         if self.rot_mode == 0:
             from .autotune import choose_rot_mode
             self.rot_mode = choose_rot_mode(self)

@@ -163,6 +163,24 @@ def test_jacobi_and_mixed_reach_1e6_checked_by_oracle(mk):
     assert np.linalg.norm(a - c) / np.linalg.norm(a) < 1e-3
 
 
+def test_fp32_operator_per_shape_dct_engine(mk, monkeypatch):
+    """The FP32 operator picks a DCT transform per TOD shape (four-step FFT,
+    Bluestein on it, or cuFFT); whatever it picks, A x agrees with the same
+    operator on cuFFT alone."""
+    from minkasi_gb300 import synth
+    from minkasi_gb300.engine import MapmakingOperator
+    tv, m = synth.make_todvec(synth.CONFIGS["tiny"])
+    op = tv.engine(m, torch.float32)
+    assert set(op.dct_engines.values()) <= {0, 1, 2}
+    x = torch.randn(m.npix, dtype=torch.float32, device="cuda")
+    a = op.apply(x, torch.empty_like(x)).clone()
+    monkeypatch.setenv("MINKASI_GB300_DCT", "1")
+    ref_op = MapmakingOperator(tv, m, torch.float32, tod2map=op.method, rot_mode=op.rot_mode)
+    assert set(ref_op.dct_engines.values()) == {1}
+    b = ref_op.apply(x, torch.empty_like(x))
+    assert float((a - b).abs().max() / b.abs().max()) < 1e-4
+
+
 def test_mixed_replacement_policies_converge(mk):
     """Every residual-replacement interval, including replacing only when the
     recursive residual claims convergence, reaches the FP64 tolerance; a
