@@ -285,10 +285,10 @@ int mk_tod2map_fixed_noalloc(void *map, const void *dat, const int32_t *ipix, in
  * X_k = x_0 + (-1)^k x_{n-1} + 2 sum_{j=1}^{n-2} x_j cos(pi j k/(n-1)).
  * The DCT-I is the real part of bins 0..n-1 of the DFT of the even
  * extension (length 2(n-1)).  FP64 plans use a batched cuFFT real-to-complex
- * transform of the extension.  FP32 plans whose 2(n-1) factors into 2, 3,
- * 5, 7, 11 (every length minkasi's truncate_tod keeps) use this library's
- * four-step shared-memory FFT: two kernels per DCT, two rows per complex
- * transform, the extension formed while loading; other FP32 plans use cuFFT.
+ * transform of the extension.  FP32 plans use this library's four-step
+ * shared-memory FFT (two rows per complex transform, the extension formed
+ * while loading): two kernels per DCT when 2(n-1) factors into 2, 3, 5, 7,
+ * 11, four (Bluestein's algorithm) otherwise, cuFFT beyond its length limit.
  * `in` and `out` are (nrow, n) dtype-typed and may alias.  The plan uses a
  * workspace of mk_dct1_workspace_bytes() bytes that the CALLER provides
  * (device pointer, 256-byte aligned) and keeps alive while the plan is used.
@@ -307,9 +307,10 @@ int mk_dct1_exec(mk_dct_plan *plan, const void *in, void *out, void *stream);
 int mk_dct1_plan_destroy(mk_dct_plan *plan);
 
 /* Transform for DCT / noise plans created after the call: engine 0
- * (default) as described above, 1 = cuFFT for every plan (for comparisons).
- * mk_dct1_engine / mk_noise_engine report what a plan uses (0 = four-step
- * FFT, 1 = cuFFT). */
+ * (default) as described above, 1 = cuFFT for every plan, 2 = the four-step
+ * FFT only where 2(n-1) factors into 2, 3, 5, 7, 11.  mk_dct1_engine /
+ * mk_noise_engine report what a plan uses (0 = four-step FFT, 2 = four-step
+ * FFT through Bluestein, 1 = cuFFT). */
 int mk_set_dct_engine(int engine);
 int mk_get_dct_engine(void);
 int mk_dct1_engine(const mk_dct_plan *plan);
