@@ -314,6 +314,11 @@ int mk_dct1_plan_destroy(mk_dct_plan *plan);
 int mk_set_dct_engine(int engine);
 int mk_get_dct_engine(void);
 int mk_dct1_engine(const mk_dct_plan *plan);
+/* What an FP32 plan for rows of length n would use under the current
+ * engine, without creating it (host only, no GPU needed): *engine as
+ * mk_dct1_engine, *L the transform length (2(n-1), or Bluestein's M), and
+ * its four-step split *L1 x *L2 (0 x 0 for cuFFT). */
+int mk_dct1_describe(int64_t n, int *engine, int64_t *L, int *L1, int *L2);
 
 /* NoiseSmoothedSVD.apply_noise, minkasi/mapmaking/noise.py:680-714:
  *   out = halve_ends( vT . DCT1( mywt[:, :ndata] * DCT1( v . dat ) ) )

@@ -86,6 +86,8 @@ SIGNATURES = {
     "mk_set_dct_engine": (_i32, [_i32]),
     "mk_get_dct_engine": (_i32, []),
     "mk_dct1_engine": (_i32, [_vp]),
+    "mk_dct1_describe": (_i32, [_i64, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int64),
+                                ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "mk_noise_engine": (_i32, [_vp]),
     "mk_learned_precon_work_bytes": (_sz, [_i32, _i32, _i32, _vp]),
     "mk_learned_precon_apply": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp, _sz, _i32, _vp]),

@@ -544,3 +544,21 @@ static int engine_of(const DctCore &c) { return !c.own ? 1 : c.f4.d.blue ? 2 : 0
 extern "C" int mk_dct1_engine(const mk_dct_plan *plan) { return plan ? engine_of(plan->core) : 1; }
 
 extern "C" int mk_noise_engine(const mk_noise_plan *plan) { return plan ? engine_of(plan->core) : 1; }
+
+extern "C" int mk_dct1_describe(int64_t n, int *engine, int64_t *L, int *L1, int *L2) {
+  MK_CHECK_ARG(engine && L && L1 && L2, "mk_dct1_describe: null output");
+  MK_CHECK_ARG(n >= 2, "mk_dct1_describe: n must be >= 2 (got %lld)", (long long)n);
+  const int e = g_engine.load();
+  mk::Fft4Dev d;
+  if (e != 1 && mk::fft4_shape(n, &d, e == 0)) {
+    *engine = d.blue ? 2 : 0;
+    *L = d.L;
+    *L1 = d.L1;
+    *L2 = d.L2;
+  } else {
+    *engine = 1;
+    *L = 2 * (n - 1);
+    *L1 = *L2 = 0;
+  }
+  return MK_OK;
+}

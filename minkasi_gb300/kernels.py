@@ -393,6 +393,16 @@ def dct_engine() -> int:
     return int(lib().mk_get_dct_engine())
 
 
+def dct_describe(n: int) -> dict:
+    """The transform an FP32 DCT / noise plan for rows of length n would use
+    under the current engine: {"engine", "L", "L1", "L2"} (host only)."""
+    e, L1, L2 = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    L = ctypes.c_int64()
+    check(lib().mk_dct1_describe(int(n), ctypes.byref(e), ctypes.byref(L), ctypes.byref(L1), ctypes.byref(L2)),
+          "dct_describe")
+    return {"engine": e.value, "L": L.value, "L1": L1.value, "L2": L2.value}
+
+
 class DCT1:
     """Batched unnormalised DCT-I (REDFT00) of (nrow, n) arrays."""
 

@@ -39,6 +39,38 @@ def test_argument_errors_need_no_gpu():
     assert h.mk_tod2map_fixed(None, None, None, 1, 1, 1, 0, 0, None, None) == _lib.MK_ERR_ARG
 
 
+def _smooth(x):
+    for p in (2, 3, 5, 7, 11):
+        while x % p == 0:
+            x //= p
+    return x == 1
+
+
+def test_dct_plan_selection_needs_no_gpu():
+    """Which transform an FP32 DCT plan uses, decided on the host: the
+    four-step split of 2(n-1) when it factors into 2..11, Bluestein's
+    smooth M >= 4(n-1) - 1 otherwise, cuFFT beyond 1536 x 1536 or when
+    selected."""
+    from minkasi_gb300 import kernels as K
+    assert K.dct_engine() == 0
+    d = K.dct_describe(130978)                 # 2 * 3^5 * 7^2 * 11
+    assert d == {"engine": 0, "L": 261954, "L1": d["L1"], "L2": d["L2"]}
+    assert d["L1"] * d["L2"] == 261954 and max(d["L1"], d["L2"]) <= 1536 and d["L1"] > 1
+    assert K.dct_describe(2) == {"engine": 0, "L": 2, "L1": 2, "L2": 1}
+    for n in (38, 1000, 465551, 144278):         # 2(n-1) has 37, 37, 9311, 72139
+        d = K.dct_describe(n)
+        assert d["engine"] == 2 and _smooth(d["L"]) and d["L"] >= 4 * (n - 1) - 1
+        assert d["L1"] * d["L2"] == d["L"] and max(d["L1"], d["L2"]) <= 1536
+    assert K.dct_describe(10 ** 7)["engine"] == 1
+    try:
+        K.set_dct_engine(2)
+        assert K.dct_describe(465551)["engine"] == 1 and K.dct_describe(130978)["engine"] == 0
+        K.set_dct_engine(1)
+        assert K.dct_describe(130978) == {"engine": 1, "L": 261954, "L1": 0, "L2": 0}
+    finally:
+        K.set_dct_engine(0)
+
+
 def test_truncation_matches_reference(gold):
     from minkasi_gb300 import truncate
     g = gold("lens.npz")
