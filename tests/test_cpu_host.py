@@ -71,6 +71,29 @@ def test_dct_plan_selection_needs_no_gpu():
         K.set_dct_engine(0)
 
 
+def test_dct_engine_choice_host_logic(monkeypatch):
+    """The per-shape transform choice without a GPU: FP64 operators keep the
+    current engine, MINKASI_GB300_DCT forces one, and with_dct_engine
+    restores the engine even when its body raises."""
+    import torch
+    from types import SimpleNamespace
+    from minkasi_gb300 import kernels as K
+    from minkasi_gb300.autotune import choose_dct_engines, with_dct_engine
+    shapes = [(16, 3529), (32, 4097)]
+    assert choose_dct_engines(SimpleNamespace(dtype=torch.float64), shapes) == {s: 0 for s in shapes}
+    monkeypatch.setenv("MINKASI_GB300_DCT", "1")
+    assert choose_dct_engines(SimpleNamespace(dtype=torch.float32), shapes) == {s: 1 for s in shapes}
+    assert with_dct_engine(2, lambda: K.dct_describe(465551)["engine"]) == 1
+    assert K.dct_engine() == 0
+
+    def boom():
+        assert K.dct_engine() == 1
+        raise RuntimeError("inside")
+    with pytest.raises(RuntimeError):
+        with_dct_engine(1, boom)
+    assert K.dct_engine() == 0
+
+
 def test_truncation_matches_reference(gold):
     from minkasi_gb300 import truncate
     g = gold("lens.npz")
