@@ -44,8 +44,9 @@ sys.path.insert(0, REPO)
 WORKLOAD = "c2: 32 TODs x 256 det x U[2^17,2^19] samples (truncated), 1024x1024 map at 1in, FP64"
 METRIC = "tod2map GB/s"
 BYTES_PER_SAMPLE = 12  # int32 pixel index + float64 sample
-# measured DRAM bytes per sample (read + write) of each FP64 tod2map kernel
-# on the 256 x 130978 small case (profiles/tod2map_fp64_c2.md)
+# measured DRAM bytes per sample (read + write) of each FP64 tod2map kernel:
+# one ncu capture each (dram__bytes_read.sum + dram__bytes_write.sum) of a
+# launch over the first c2 TOD shape, 256 x 130978 = 33,530,368 samples
 NCU_DRAM_BYTES_PER_SAMPLE = {"atomic": (404.32e6 + 3.30e6) / 33530368,
                              "staged": (404.30e6 + 2.87e6) / 33530368}
 
@@ -416,8 +417,8 @@ def run_ours(args):
         return
     clocks = clk.summary()
     # DRAM bytes per sample of the scatter kernel from one ncu capture of the
-    # small case (dram__bytes_read.sum + dram__bytes_write.sum, scaled to a
-    # full launch by the sample count); see profiles/tod2map_fp64_c2.md
+    # small case (dram__bytes_read.sum + dram__bytes_write.sum), scaled to a
+    # full launch by the sample count
     per_sample = NCU_DRAM_BYTES_PER_SAMPLE.get(op.method)
     traffic = None if per_sample is None else per_sample * S
     line = {
