@@ -1,6 +1,8 @@
-"""Benchmark: tod2map GB/s on the 32-TOD FP64 workload (plus the PCG iteration).
+"""Benchmark: tod2map GB/s on the 32-TOD FP64 workload, plus the solver's
+time to a 1e-6 FP64 residual (learned vs Jacobi PCG).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--no-pcg] [--no-solver] [--no-c4]
 
 Workload (the reference's "plain method at GPU scale" configuration): 32
 synthetic TODs, 256 detectors each, nsamp ~ U[2^17, 2^19] truncated to
@@ -9,6 +11,9 @@ FP64.  One step = one tod2map pass of every TOD's timestream into the map
 (the projection of TodVec.make_rhs / TodVec.dot), inputs resident in HBM.
 value = algorithmic bytes (4 B ipix + 8 B dat per sample) / step time.
 The inputs (32 GB) exceed the 129 MB L2, so no flush is needed between steps.
+With N ranks the TODs are split between them (largest first onto the least
+loaded rank, minkasi's TOD sharding) and the map is summed over ranks every
+step: the total work is fixed, so scaling is strong.
 
 e2e: the same step through the public API (SkyMap.tod2map per TOD) with the
 timestream in pinned host memory, copied to the device inside the timed
@@ -18,8 +23,18 @@ caches them (tod.info[tag]).
 
 Extra keys: map2tod GB/s on the same samples; per-iteration timings of the
 full hot path (FP64 Jacobi PCG iteration = batched A-apply + update, and the
-FP32 inner iteration of the mixed-precision solver) on the same TODs, and
-the reference's CPU operator per iteration (a bounded sample, scaled).
+FP32 inner iteration of the mixed-precision solver) on the same TODs; and,
+under "solver", the other half of the benchmark metric: wall time from x0 = 0
+to an FP64 true residual ||b - A x||/||b|| <= 1e-6 for FP64 Jacobi PCG (the
+plain method), the mixed-precision PCG with Jacobi, and the mixed-precision
+PCG with the learned preconditioner (weights made by learned.train_recipe),
+on the 1-TOD configuration (all three run to the end) and on the 200-TOD
+configuration (the FP64 Jacobi solve, about two hours there, is its measured
+iteration time times the mixed solve's iteration count, labelled projected).
+
+CPU baselines run in a separate process with no GPU library loaded (this
+script with --impl reference): the reference's tod2map, and its operator per
+PCG iteration, on all host threads over a bounded sample of the workload.
 
 --impl reference times the reference's CPU tod2map (its own C compiled from
 source when available in oracle/_ref, else the C restatement in oracle/)
@@ -59,8 +74,46 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default="c2")
     ap.add_argument("--no-pcg", action="store_true", help="skip the PCG-iteration extras")
+    ap.add_argument("--no-solver", action="store_true", help="skip the time-to-residual solves")
+    ap.add_argument("--no-c4", action="store_true", help="skip the 200-TOD solves")
+    ap.add_argument("--cpu-pcg", action="store_true",
+                    help="(reference arm) also time the reference CPU operator per PCG iteration")
     ap.add_argument("--method", default=None, help="force the tod2map kernel (atomic|staged|fixed|sorted)")
     return ap.parse_args()
+
+
+def load_synth():
+    """minkasi_gb300/synth.py and the truncate module it imports, loaded by
+    file path under a stand-in package name, so that the CPU arm builds the
+    same pointing without running the package __init__ (which loads the GPU
+    library)."""
+    import importlib.util
+    import types
+
+    name = "_mk_synth_only"
+    if name + ".synth" in sys.modules:
+        return sys.modules[name + ".synth"]
+    pkg = types.ModuleType(name)
+    pkg.__path__ = [os.path.join(REPO, "minkasi_gb300")]
+    sys.modules[name] = pkg
+    for mod in ("truncate", "synth"):
+        spec = importlib.util.spec_from_file_location(f"{name}.{mod}",
+                                                      os.path.join(REPO, "minkasi_gb300", f"{mod}.py"))
+        m = importlib.util.module_from_spec(spec)
+        sys.modules[spec.name] = m
+        spec.loader.exec_module(m)
+    return sys.modules[name + ".synth"]
+
+
+def shard(shapes, rank, world):
+    """The TOD indices this rank owns (greedy largest-first on the transform
+    cost, the same rule as minkasi_gb300.parallel.partition)."""
+    import math
+    costs = [float(nd) * n * math.log2(max(n, 2)) for nd, n in shapes]
+    if world == 1:
+        return list(range(len(shapes)))
+    from minkasi_gb300 import parallel
+    return parallel.partition(costs, world)[rank]
 
 
 def dist_env():
@@ -146,7 +199,7 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------- workload
-def build_workload(cfg_name, device, with_noise):
+def build_workload(cfg_name, device, with_noise, rank=0, world=1):
     import torch
     from minkasi_gb300 import synth
     from minkasi_gb300.maps import SkyMap
@@ -156,7 +209,11 @@ def build_workload(cfg_name, device, with_noise):
     tv = TodVec()
     gen = torch.Generator(device=device)
     gen.manual_seed(1)
-    for k, (ndet, n) in enumerate(synth.tod_shapes(cfg)):
+    shapes = synth.tod_shapes(cfg)
+    mine = set(shard(shapes, rank, world))
+    for k, (ndet, n) in enumerate(shapes):
+        if k not in mine:
+            continue
         if with_noise:
             info = synth.make_tod_info(cfg, k, ndet, n, device)
             tod = Tod(info)
@@ -167,7 +224,8 @@ def build_workload(cfg_name, device, with_noise):
             tod = Tod(info)
         tv.add_tod(tod)
     m = SkyMap(nx=cfg.nx, ny=cfg.ny, device=device)
-    return cfg, tv, m
+    total = sum(nd * n for nd, n in shapes)
+    return cfg, tv, m, total
 
 
 def time_steps(fn, steps, warmup, stream, clk=None):
@@ -218,49 +276,73 @@ def cpu_tod2map_sample(tods_host, npix, seconds=12.0, prefer_ref=True):
     return nbytes / t_used / 1e9, desc, kind, cores
 
 
-def cpu_pcg_iter_sample(tv, npix, seconds=20.0):
+def cpu_pcg_iter_sample(sample, npix, total_samples, seconds=20.0):
     """Seconds per PCG iteration of the reference's CPU operator (map2tod +
     NoiseSmoothedSVD.apply_noise with scipy's DCT-I, the shipped transform,
-    on all host threads + tod2map), measured on the first TOD(s) of the
-    workload and scaled to all of its samples."""
+    on all host threads + tod2map), measured on the sample TODs and scaled
+    to all of the workload's samples.  The noise operands are random arrays
+    of the TODs' shapes: the time of these dense operations does not depend
+    on their values."""
     sys.path.insert(0, os.path.join(REPO, "oracle"))
     import oracle
 
     cores = os.cpu_count() or 1
-    x = np.random.default_rng(0).standard_normal(npix)
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal(npix)
     out = np.zeros(npix)
     used, samp, ntod = 0.0, 0, 0
-    for t in tv.tods:
-        nz = t.noise
-        ip = np.ascontiguousarray(t.info["ipix"].cpu().numpy())
-        v, vT, w = (a.detach().cpu().numpy() for a in (nz.v, nz.vT, nz.mywt))
-        nv = None if nz.noisevec is None else nz.noisevec.detach().cpu().numpy()
+    for ip, _ in sample:
+        nd, n = ip.shape
+        v = rng.standard_normal((nd, nd))
+        vT = np.ascontiguousarray(v.T)
+        w = rng.random((nd, n))
         d = np.zeros(ip.shape)
         t0 = time.perf_counter()
         oracle.map2tod(d, x, ip, False)
-        d = oracle.apply_noise(v, vT, w, d, nv, workers=cores)
-        oracle.tod2map(out, d, ip, nthread=cores)
+        d = oracle.apply_noise(v, vT, w, d, None, workers=cores)
+        oracle.tod2map(out, np.ascontiguousarray(d), ip, nthread=cores)
         used += time.perf_counter() - t0
         samp += ip.size
         ntod += 1
         if used >= seconds:
             break
-    total = tv.get_nsamp()
-    return {"s_per_iter": used / samp * total, "unit": "s", "cores": cores, "kind": "port",
-            "sample": f"{ntod} of the workload's TODs ({samp} samples), scaled to {total} samples; "
+    return {"s_per_iter": used / samp * total_samples, "unit": "s", "cores": cores, "kind": "port",
+            "sample": f"{ntod} of the workload's TODs ({samp} samples), scaled to {total_samples} samples; "
                       f"oracle C projections + numpy/scipy DCT-I apply_noise, {cores} threads"}
 
 
-def host_sample(tv, max_samples=3.5e8):
-    out, tot = [], 0
-    for t in tv.tods:
+def cpu_sample(cfg_name, max_samples=3.5e8):
+    """Host copies of the workload's first TODs: the same pointing as the GPU
+    arm (synth on the CPU) and Gaussian timestreams."""
+    import torch
+    synth = load_synth()
+    cfg = synth.CONFIGS[cfg_name]
+    shapes = synth.tod_shapes(cfg)
+    sample, tot = [], 0
+    for k, (ndet, n) in enumerate(shapes):
         if tot >= max_samples:
             break
-        ip = t.info["ipix"].cpu().numpy()
-        d = t.info["dat_calib"].cpu().numpy()
-        out.append((np.ascontiguousarray(ip), np.ascontiguousarray(d)))
+        info = synth.make_tod_info(cfg, k, ndet, n, torch.device("cpu"), with_data=False, with_radec=False)
+        d = np.random.default_rng(k).standard_normal((ndet, n))
+        sample.append((np.ascontiguousarray(info["ipix"].numpy()), d))
         tot += d.size
-    return out
+    return cfg, shapes, sample
+
+
+def cpu_baseline_subprocess(args):
+    """Run this script's reference arm in a fresh process (no torch CUDA
+    context, no GPU library): the cpu_baseline and the CPU operator time."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--steps", "3", "--warmup", "1",
+           "--config", args.config, "--cpu-pcg"]
+    env = dict(os.environ)
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
+        env.pop(k, None)
+    try:
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, env=env)
+        lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+        return json.loads(lines[-1]) if lines else {"error": r.stderr[-400:]}
+    except (subprocess.TimeoutExpired, ValueError) as e:
+        return {"error": str(e)}
 
 
 # ---------------------------------------------------------------- arms
@@ -268,31 +350,15 @@ def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
         return
-    import torch
-    from minkasi_gb300 import synth
-
-    cfg = synth.CONFIGS[args.config]
-    shapes = synth.tod_shapes(cfg)
+    cfg, shapes, sample = cpu_sample(args.config)
     npix = cfg.nx * cfg.ny
-    # the same pointing and the same kind of data as our arm, generated on
-    # the CPU for a bounded sample of TODs
-    dev = torch.device("cpu")
-    sample = []
-    tot = 0
-    for k, (ndet, n) in enumerate(shapes):
-        if tot >= 2.0e8:
-            break
-        info = synth.make_tod_info(cfg, k, ndet, n, dev, with_data=False)
-        d = np.random.default_rng(k).standard_normal((ndet, n))
-        sample.append((info["ipix"].numpy(), d))
-        tot += d.size
     vals = []
     desc = kind = None
     cores = os.cpu_count()
     for _ in range(args.warmup):
         cpu_tod2map_sample(sample, npix, seconds=0.5)
     for _ in range(args.steps):
-        v, desc, kind, cores = cpu_tod2map_sample(sample, npix, seconds=2.0)
+        v, desc, kind, cores = cpu_tod2map_sample(sample, npix, seconds=4.0)
         vals.append(v)
     value = statistics.median(vals)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": 0,
@@ -304,6 +370,8 @@ def run_reference(args):
             "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "vs_baseline": None}
+    if args.cpu_pcg:
+        line["pcg_iter_cpu_reference"] = cpu_pcg_iter_sample(sample, npix, sum(nd * n for nd, n in shapes))
     print(json.dumps(line))
 
 
@@ -320,9 +388,7 @@ def run_ours(args):
     from minkasi_gb300 import parallel
 
     with_noise = not args.no_pcg
-    cfg, tv, m = build_workload(args.config, dev, with_noise)
-    # weak scaling: every rank runs the full workload on its own GPU and
-    # the map is summed over ranks once per step (the reference's reduction)
+    cfg, tv, m, S_total = build_workload(args.config, dev, with_noise, rank, world)
     if args.method:
         tv.tod2map_method = args.method
     op = tv.engine(m)
@@ -336,18 +402,22 @@ def run_ours(args):
         op.project_out(out)
         parallel.allreduce_(out)
 
+    def max_over_ranks(x):
+        t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+        if world > 1:
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
     # dominant-kernel timing: the scatter kernel alone, on the launching stream
     parallel.barrier()
     with ClockSampler(local) as clk:
         total_ms, per, wall = time_steps(step, args.steps, args.warmup, stream, clk)
     parallel.barrier()
-    tmax = torch.tensor([total_ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
-    total_ms = float(tmax.item())
-    ms_step = total_ms / args.steps
-    gbs = world * S * BYTES_PER_SAMPLE / (ms_step * 1e-3) / 1e9
+    rank_ms_step = total_ms / args.steps
+    ms_step = max_over_ranks(total_ms) / args.steps
+    gbs = S_total * BYTES_PER_SAMPLE / (ms_step * 1e-3) / 1e9
     launches_per_step = {"atomic": 1, "staged": 1, "fixed": 4, "sorted": len(tv.tods)}[op.method]
+    method, ntod_rank = op.method, len(tv.tods)
 
     # e2e through the public API with host buffers
     host = [t.info["dat_calib"].cpu().pin_memory() for t in tv.tods]
@@ -361,6 +431,7 @@ def run_ours(args):
         m.clear()
         for t, h in zip(tv.tods, host):
             m.tod2map(t, h)
+        m.mpi_reduce()
         return m.map.cpu()
 
     def e2e_copy():
@@ -369,22 +440,25 @@ def run_ours(args):
         for t, h, d in zip(tv.tods, host, devbuf):
             d.copy_(h, non_blocking=True)
             m.tod2map(t, d)
+        m.mpi_reduce()
         return m.map.cpu()
 
     def seconds_per_step(fn):
         for _ in range(args.warmup):
             fn()
         torch.cuda.synchronize()
+        parallel.barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
             fn()
         torch.cuda.synchronize()
-        return (time.perf_counter() - t0) / args.steps
+        return max_over_ranks((time.perf_counter() - t0) / args.steps)
 
     e2e_s = seconds_per_step(e2e_api)
     e2e_copy_s = seconds_per_step(e2e_copy)
-    e2e_gbs = world * S * BYTES_PER_SAMPLE / e2e_s / 1e9
-    e2e_copy_gbs = world * S * BYTES_PER_SAMPLE / e2e_copy_s / 1e9
+    e2e_gbs = S_total * BYTES_PER_SAMPLE / e2e_s / 1e9
+    e2e_copy_gbs = S_total * BYTES_PER_SAMPLE / e2e_copy_s / 1e9
+    h2d_total = int(max_over_ranks(h2d)) * world if world > 1 else h2d
     del devbuf, host
 
     # extras: the other projection on the same samples (map2tod, FP64, set
@@ -395,8 +469,9 @@ def run_ours(args):
     m2t_ms, _, _ = time_steps(lambda: K.map2tod(op.tmp, src, op.ipix, False), args.steps, args.warmup, stream)
     m2t_gbs = S * BYTES_PER_SAMPLE / (m2t_ms / args.steps * 1e-3) / 1e9
     extras["map2tod"] = {"value": m2t_gbs, "unit": "GB/s", "ms_per_step": m2t_ms / args.steps,
-                         "frac_of_hbm": None, "bytes_per_sample": BYTES_PER_SAMPLE}
-    if with_noise and rank == 0:
+                         "frac_of_hbm": None, "bytes_per_sample": BYTES_PER_SAMPLE,
+                         "kernel": "k_map2tod_vec"}
+    if with_noise and world == 1:
         extras.update(pcg_extras(tv, m, dev))
 
     peaks = {}
@@ -407,41 +482,67 @@ def run_ours(args):
     peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     extras["map2tod"]["frac_of_hbm"] = extras["map2tod"]["value"] / peak
-    cpu = None
-    if rank == 0 and world == 1:
-        v, desc, kind, cores = cpu_tod2map_sample(host_sample(tv), op.npix, seconds=12.0)
-        cpu = {"value": v, "unit": "GB/s", "cores": cores, "kind": kind, "sample": desc}
-        if with_noise:
-            extras["pcg_iter_cpu_reference"] = cpu_pcg_iter_sample(tv, op.npix)
-    if rank != 0:
-        return
-    clocks = clk.summary()
+    clocks = clk.summary() if rank == 0 else None
     # DRAM bytes per sample of the scatter kernel from one ncu capture of the
     # small case (dram__bytes_read.sum + dram__bytes_write.sum), scaled to a
     # full launch by the sample count
     per_sample = NCU_DRAM_BYTES_PER_SAMPLE.get(op.method)
     traffic = None if per_sample is None else per_sample * S
+    achieved = S * BYTES_PER_SAMPLE / (rank_ms_step * 1e-3) / 1e9
+    nlaunch = launches_per_step * args.steps
+
+    solver = None
+    if world == 1 and not args.no_solver:
+        # free the c2 workload before the solver configurations
+        del op, out, src
+        tv._engines.clear()
+        tv._shared.clear()
+        del tv, m
+        import gc
+        from minkasi_gb300.noise import clear_plan_cache
+        clear_plan_cache()
+        gc.collect()
+        torch.cuda.empty_cache()
+        solver = solver_extras(dev, skip_c4=args.no_c4)
+
+    cpu = None
+    if rank == 0 and world == 1:
+        ref = cpu_baseline_subprocess(args)
+        if "value" in ref:
+            cpu = dict(ref["cpu_baseline"])
+            if with_noise and "pcg_iter_cpu_reference" in ref:
+                extras["pcg_iter_cpu_reference"] = ref["pcg_iter_cpu_reference"]
+        else:
+            cpu = {"value": None, "unit": "GB/s", "error": ref.get("error")}
+    if rank != 0:
+        return
     line = {
         "metric": METRIC, "value": gbs, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "samples": S, "ntod": len(tv.tods), "npix": op.npix,
-                   "tod2map_kernel": op.method, "l2": "inputs (12 B x samples) larger than L2; no flush",
-                   "parallelism": f"replicas x{world}, map all-reduce per step"},
-        "roofline": {"bound": "hbm", "achieved": gbs / world, "peak": peak, "unit": "GB/s",
-                     "frac": gbs / world / peak, "traffic": traffic,
+        "scaling": "strong" if world > 1 else "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "samples": S_total, "samples_rank0": S, "ntod_rank0": ntod_rank,
+                   "npix": int(cfg.nx * cfg.ny), "tod2map_kernel": method,
+                   "l2": "inputs (12 B x samples) larger than L2; no flush",
+                   "parallelism": (f"TODs sharded over {world} ranks, map all-reduce per step" if world > 1
+                                   else "1 GPU")},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": {"atomic": "k_tod2map_atomic8", "staged": "k_tod2map_staged",
+                                "fixed": "k_scatter_fixed8", "sorted": "k_tod2map_sorted"}[method],
                      "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"},
-        "e2e": {"value": e2e_gbs, "unit": "GB/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": op.npix * 8,
+        "e2e": {"value": e2e_gbs, "unit": "GB/s", "h2d_bytes_per_step": h2d_total,
+                "d2h_bytes_per_step": int(cfg.nx * cfg.ny) * 8,
                 "mode": "SkyMap.tod2map per TOD on pinned host timestreams (chunked copies overlapped "
                         "with the scatter), map read back every step",
                 "serial_copy_then_scatter": e2e_copy_gbs},
-        "gpu_launches": launches_per_step * args.steps,
+        "gpu_launches": nlaunch,
         "clocks": clocks,
         "cpu_baseline": cpu,
         "wall_s_timed": wall,
     }
     line.update(extras)
+    if solver is not None:
+        line["solver"] = solver
     print(json.dumps(line))
 
 
@@ -478,6 +579,180 @@ def pcg_extras(tv, m, dev):
         res[name] = {"ms": ms, "Msamp_per_s": S / (ms * 1e-3) / 1e6, "tod2map_kernel": op.method,
                      "rot_mode": op.rot_mode}
         del st
+    return res
+
+
+# ---------------------------------------------------------------- solver
+def _timed(fn, reps=1):
+    """(result, wall seconds of the last of ``reps`` calls, of the first)."""
+    import torch
+    first = None
+    out = None
+    for _ in range(reps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        out = fn()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        first = dt if first is None else first
+    return out, dt, first
+
+
+def _true_rel(op64, b, x):
+    """||b - A x|| / ||b|| with the FP64 operator (sum over ranks)."""
+    import torch
+    from minkasi_gb300.pcg import _true_residual, global_op
+    return _true_residual(global_op(op64), b.reshape(-1), x.reshape(-1))
+
+
+def solve_c1(dev, tol=1e-6):
+    """The 1-TOD configuration (64 x 65,341 samples, 256^2 map): FP64 Jacobi
+    PCG, mixed Jacobi and mixed learned to the FP64 tolerance.  Each wall time
+    is the second of two identical solves (the first adds graph captures)."""
+    import torch
+    import minkasi_gb300 as mk
+    from minkasi_gb300 import learned as L
+    from minkasi_gb300 import synth
+
+    t0 = time.perf_counter()
+    cfg = synth.CONFIGS["c1"]
+    tv, m = synth.make_todvec(cfg, dev)
+    mapset = mk.Mapset()
+    mapset.add_map(m)
+    rhs = mapset.copy()
+    tv.make_rhs(rhs)
+    hits = mk.make_hits(tv, m)
+    pre = mk.jacobi_precon(hits)
+    x0 = rhs.copy()
+    x0.clear()
+    net = L.load(L.weights_path("c1"), dev)
+    ml = L.LearnedPrecon(hits.map, net, (m.nx, m.ny))
+    op64 = tv.engine(m, torch.float64)
+    tv.engine(m, torch.float32)
+    out = {"workload": "c1: 1 TOD x 64 det x 65,341 samples, 256x256 map at 2in", "tol": tol,
+           "samples": tv.get_nsamp(), "setup_s": time.perf_counter() - t0,
+           "learned_weights": os.path.relpath(L.weights_path("c1"), REPO)}
+    runs = {
+        "jacobi_f64": lambda: mk.run_pcg(rhs, x0, tv, pre, maxiter=5000, tol=tol, verbose=False),
+        "mixed_jacobi": lambda: mk.run_pcg_mixed(rhs, x0, tv, pre, tol=tol),
+        "mixed_learned": lambda: mk.run_pcg_mixed(rhs, x0, tv, pre, tol=tol, inner_precon=ml),
+    }
+    for name, fn in runs.items():
+        x, wall, cold = _timed(fn, reps=2)
+        rec = {"wall_s": wall, "cold_wall_s": cold, "iters": int(x.niter),
+               "true_rel_residual": _true_rel(op64, rhs.maps[0].map, x.maps[0].map)}
+        if hasattr(x, "outer"):
+            rec["fp64_residuals"] = int(x.outer)
+        out[name] = rec
+    jf = out["jacobi_f64"]["wall_s"]
+    out["speedup_mixed_jacobi_vs_jacobi_f64"] = jf / out["mixed_jacobi"]["wall_s"]
+    out["speedup_mixed_learned_vs_jacobi_f64"] = jf / out["mixed_learned"]["wall_s"]
+    out["speedup_learned_vs_jacobi_mixed"] = out["mixed_jacobi"]["wall_s"] / out["mixed_learned"]["wall_s"]
+    return out
+
+
+def solve_c4(dev, tol=1e-6, wall_limit_s=420.0):
+    """The 200-TOD configuration (8.8e9 samples, 2048^2 map): setup, the FP32
+    projections' GB/s, the FP64 Jacobi iteration time, and the mixed solves
+    (Jacobi, learned) to the FP64 tolerance, each bounded in wall time."""
+    import torch
+    from minkasi_gb300 import kernels as K
+    from minkasi_gb300 import learned as L
+    from minkasi_gb300 import synth
+    from minkasi_gb300.maps import Mapset
+    from minkasi_gb300.pcg import DevicePCG, MixedOp, run_pcg_mixed
+    from minkasi_gb300.projections import make_hits
+
+    cfg = synth.CONFIGS["c4"]
+    t0 = time.perf_counter()
+    tv, m, rhs = L.build_large(cfg, dev, log=None)
+    hits = make_hits(tv, m).map.reshape(-1)
+    pre = torch.where(hits > 0, 1.0 / hits.clamp(min=1), torch.zeros_like(hits))
+    op64 = tv.engine(m, torch.float64)
+    op32 = tv.engine(m, torch.float32)
+    torch.cuda.synchronize()
+    S = tv.get_nsamp()
+    out = {"workload": "c4: 200 TODs, ndet in {32,64,128,256}, nsamp U[5e4,6e5] (truncated), 2048x2048 map "
+                       "at 0.5in", "tol": tol, "samples": S, "ntod": tv.ntod,
+           "setup_s": time.perf_counter() - t0,
+           "tod2map_kernel_f32": op32.method, "rot_mode_f32": op32.rot_mode,
+           "dct_engines_f32": sorted(set(int(v) for v in op32.dct_engines.values())),
+           "gpu_mem_GB_peak": torch.cuda.max_memory_allocated() / 1e9,
+           "learned_weights": os.path.relpath(L.weights_path("c4"), REPO)}
+    stream = torch.cuda.current_stream()
+    # FP32 projections at this scale (8 B per sample: 4 B index + 4 B sample)
+    src = torch.randn(m.npix, dtype=torch.float32, device=dev)
+    acc = torch.zeros(m.npix, dtype=torch.float32, device=dev)
+    ms, _, _ = time_steps(lambda: K.map2tod(op32.tmp, src, op32.ipix, False), 5, 3, stream)
+    out["map2tod_f32_GBps"] = S * 8 / (ms / 5 * 1e-3) / 1e9
+    ms, _, _ = time_steps(lambda: op32.project_out(acc), 5, 3, stream)
+    out["tod2map_f32_GBps"] = S * 8 / (ms / 5 * 1e-3) / 1e9
+    del src, acc
+    # one FP64 Jacobi PCG iteration (operator + fused update), eager
+    st = DevicePCG(op64, rhs, torch.zeros_like(rhs), pre, graph=False)
+    st.start(Ax=torch.zeros_like(rhs))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    st.step()
+    e1.record()
+    e1.synchronize()
+    ms64 = e0.elapsed_time(e1)
+    out["jacobi_f64_iter_ms"] = ms64
+    del st
+    mp = m.copy()
+    mp.map.copy_(rhs.view(m.nx, m.ny))
+    b = Mapset()
+    b.add_map(mp)
+    x0 = b.copy()
+    x0.clear()
+    pre_ms = b.copy()
+    pre_ms.maps[0].map.copy_(pre.view(m.nx, m.ny))
+    ml = L.LearnedPrecon(hits, L.load(L.weights_path("c4"), dev), (m.nx, m.ny))
+    budget = None
+    for name, kw in (("mixed_jacobi", {}), ("mixed_learned", {"inner_precon": ml})):
+        hist = []
+        if budget is None:
+            # iterations that fit the wall limit at the measured inner iteration
+            stt = DevicePCG(MixedOp(op32, m.npix, dev), rhs, torch.zeros_like(rhs), pre, graph=True)
+            stt.start()
+            stt.step()
+            stt.step()
+            torch.cuda.synchronize()
+            e0.record()
+            for _ in range(3):
+                stt.step()
+            e1.record()
+            e1.synchronize()
+            inner_ms = e0.elapsed_time(e1) / 3
+            out["mixed_inner_iter_ms"] = inner_ms
+            del stt
+            budget = max(100, int((wall_limit_s - 4 * ms64 / 1e3) * 1e3 / (inner_ms * 1.15)))
+        x, wall, _ = _timed(lambda: run_pcg_mixed(b, x0, tv, pre_ms, tol=tol, max_iter=budget, history=hist, **kw))
+        out[name] = {"wall_s": wall, "iters": int(x.niter), "fp64_residuals": int(x.outer),
+                     "restarts": int(x.restarts), "true_rel_residual": float(x.rel_residual),
+                     "reached_tol": bool(x.rel_residual <= tol), "iteration_budget": budget}
+        del x
+    it = out["mixed_jacobi"]["iters"]
+    out["jacobi_f64_projected_s"] = it * ms64 / 1e3
+    out["jacobi_f64_projected_note"] = ("measured FP64 Jacobi iteration x the mixed Jacobi solve's iteration "
+                                        "count (the two counts agree on the 1-TOD configuration, where both run)")
+    out["speedup_mixed_jacobi_vs_jacobi_f64_projected"] = out["jacobi_f64_projected_s"] / out["mixed_jacobi"]["wall_s"]
+    out["speedup_mixed_learned_vs_jacobi_f64_projected"] = (out["jacobi_f64_projected_s"] /
+                                                            out["mixed_learned"]["wall_s"])
+    return out
+
+
+def solver_extras(dev, skip_c4=False):
+    import gc
+    import torch
+    from minkasi_gb300.noise import clear_plan_cache
+
+    res = {"c1": solve_c1(dev)}
+    if not skip_c4:
+        clear_plan_cache()
+        gc.collect()
+        torch.cuda.empty_cache()
+        res["c4"] = solve_c4(dev)
     return res
 
 

@@ -251,7 +251,11 @@ int mk_pixplan_destroy(mk_pixplan *plan);
  * `hmax`, an upper bound on the number of samples hitting any one pixel
  * (fixed by the pointing; e.g. the max of the hit map), so no accumulator
  * can overflow.  Rounding: |error| <= hits * max|dat| * 2^-(62-hbits) per
- * pixel, below FP64 summation error for hmax <= 2^24.
+ * pixel, below FP64 summation error for hmax <= 2^24.  s comes from the
+ * finite samples only; a NaN or +-inf sample is added straight into its own
+ * pixel (a floating-point atomic), so as in the reference's serial sum a
+ * pixel ends up NaN or +-inf exactly when its samples make it so, and the
+ * other pixels are unaffected.
  * `scratch`: device, 256-byte aligned, mk_tod2map_fixed_scratch_bytes(npix)
  * bytes, zeroed once before first use; every call leaves it zeroed again.
  * Calls that share a scratch must be ordered on one stream. */
@@ -268,9 +272,12 @@ int mk_tod2map_fixed(void *map, const void *dat, const int32_t *ipix, int64_t nd
  * built into the library (a 256-byte header plus 8 bytes per pixel for up to
  * MK_NOALLOC_MAX_NPIX pixels, 32 MiB), which every GPU that loads the
  * library holds until the process exits.  npix above the limit is rejected
- * with MK_ERR_ARG.  The first call on a device looks up that array's device
- * address (cudaGetSymbolAddress, with that device current); make this first
- * call before any stream capture.  All calls share the one array, which
+ * with MK_ERR_ARG, and so is a negative npix.  The first call on a device
+ * looks up that array's device address (cudaGetSymbolAddress, with that
+ * device current) and caches it for the life of the process; make this first
+ * call before any stream capture.  A cudaDeviceReset unloads the module and
+ * leaves the cached address stale: do not call this entry point on a device
+ * after resetting it.  All calls share the one array, which
  * every complete call leaves zeroed: calls that overlap on the GPU (on
  * different streams, or from different host threads without ordering) race
  * and give wrong maps.  Inputs, outputs and results are as mk_tod2map_fixed. */
@@ -435,6 +442,20 @@ size_t mk_learned_precon_work_bytes(int H, int W, int nlayer, const int *channel
 int mk_learned_precon_apply(void *z, const void *r, const void *dsq, int H, int W, int nlayer,
                             const int *channels, const float *const *weights, float *work,
                             size_t work_bytes, int dtype, void *stream);
+
+/* The same preconditioner as one stencil: the layers are linear and
+ * shift-invariant, so K^T K is a single-channel convolution with a
+ * (2 half + 1)^2 kernel C, its impulse response (half = 2n for n layers;
+ * 17 x 17 for 4).  This call computes
+ *   u = dsq * r,  z = dsq * (u + C * u),  (C * u)[y][x] = sum C[dy][dx] u[y+dy-half][x+dx-half]
+ * with u = 0 outside the map, in one launch, FP32 stencil sums.  `kern` is
+ * the device array C, (2 half + 1)^2 float32, half <= 8; a symmetric C gives
+ * a symmetric M.  Wherever u vanishes within `half` pixels of the map edge
+ * this equals mk_learned_precon_apply; nearer the edge it zero-pads once
+ * instead of after every layer (still SPD for C = the impulse response of
+ * K^T K).  z, r, dsq are dtype-typed maps; z must not alias r. */
+int mk_learned_precon_stencil(void *z, const void *r, const void *dsq, int H, int W, int half,
+                              const float *kern, int dtype, void *stream);
 
 #ifdef __cplusplus
 }

@@ -91,6 +91,7 @@ SIGNATURES = {
     "mk_noise_engine": (_i32, [_vp]),
     "mk_learned_precon_work_bytes": (_sz, [_i32, _i32, _i32, _vp]),
     "mk_learned_precon_apply": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp, _sz, _i32, _vp]),
+    "mk_learned_precon_stencil": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _i32, _vp]),
 }
 
 _lib: Optional[ctypes.CDLL] = None

@@ -315,7 +315,105 @@ int precon_apply(TT *z, const TT *r, const TT *dsq, int H, int W, int nl, const 
   return rc;
 }
 
+// ---- the preconditioner as one stencil -----------------------------------
+// The layers are linear and shift-invariant, so K^T K is one single-channel
+// convolution whose kernel C is its impulse response, of half-width 2n for n
+// 3x3 layers (17 x 17 for 4 layers).  One kernel then applies
+//   z = dsq * (u + C * u),  u = dsq * r
+// reading each r and dsq once.  A CTA owns a 32 x 32 output tile: u for the
+// tile plus a HALF-pixel halo is staged in shared memory (zero outside the
+// map) at an odd-by-one pitch, so the 4 rows a warp touches fall on distinct
+// banks; each thread accumulates a 1 x 4 strip, with the KS + 3 input values
+// of a stencil row in registers and C read as warp-wide broadcasts.
+constexpr int ST_TX = 32, ST_TY = 32, ST_THREADS = 256, ST_MAXHALF = 8;
+
+template <int HALF, typename TT>
+__global__ void __launch_bounds__(ST_THREADS)
+    k_precon_stencil(const TT *__restrict__ r, const TT *__restrict__ dsq, const float *__restrict__ kern,
+                     TT *__restrict__ z, int H, int W) {
+  constexpr int KS = 2 * HALF + 1, SW = ST_TX + 2 * HALF, SH = ST_TY + 2 * HALF, P = SW | 1;
+  constexpr int PITCH = (P % 4 == 1) ? P : P + 2;  // == 1 (mod 4): the 4 rows of a warp hit distinct banks
+  __shared__ float su[SH * PITCH];
+  __shared__ float sk[KS * KS];
+  const int x0 = blockIdx.x * ST_TX, y0 = blockIdx.y * ST_TY, tid = threadIdx.x;
+  for (int i = tid; i < KS * KS; i += ST_THREADS) sk[i] = kern[i];
+  for (int i = tid; i < SH * SW; i += ST_THREADS) {
+    const int sy = i / SW, sx = i - sy * SW, yy = y0 + sy - HALF, xx = x0 + sx - HALF;
+    float v = 0.f;
+    if (yy >= 0 && yy < H && xx >= 0 && xx < W) {
+      const int64_t g = (int64_t)yy * W + xx;
+      v = (float)mul_rn(dsq[g], r[g]);
+    }
+    su[sy * PITCH + sx] = v;
+  }
+  __syncthreads();
+  const int ty = tid >> 3, tx = (tid & 7) * 4;
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 1
+  for (int dy = 0; dy < KS; dy++) {
+    float row[KS + 3];
+    const float *src = su + (ty + dy) * PITCH + tx;
+#pragma unroll
+    for (int j = 0; j < KS + 3; j++) row[j] = src[j];
+    const float *kr = sk + dy * KS;
+#pragma unroll
+    for (int dx = 0; dx < KS; dx++) {
+      const float k = kr[dx];
+#pragma unroll
+      for (int o = 0; o < 4; o++) acc[o] = fmaf(k, row[o + dx], acc[o]);
+    }
+  }
+  const int yy = y0 + ty;
+  if (yy >= H) return;
+#pragma unroll
+  for (int o = 0; o < 4; o++) {
+    const int xx = x0 + tx + o;
+    if (xx < W) {
+      const int64_t g = (int64_t)yy * W + xx;
+      const TT u = mul_rn(dsq[g], r[g]);
+      z[g] = mul_rn(dsq[g], add_rn(u, (TT)acc[o]));
+    }
+  }
+}
+
+template <int HALF, typename TT>
+int stencil_launch(TT *z, const TT *r, const TT *dsq, const float *kern, int H, int W, cudaStream_t st) {
+  const dim3 grid((W + ST_TX - 1) / ST_TX, (H + ST_TY - 1) / ST_TY);
+  k_precon_stencil<HALF, TT><<<grid, ST_THREADS, 0, st>>>(r, dsq, kern, z, H, W);
+  return mk::launch_status("mk_learned_precon_stencil");
+}
+
+template <typename TT>
+int stencil_dispatch(TT *z, const TT *r, const TT *dsq, const float *kern, int H, int W, int half,
+                     cudaStream_t st) {
+  switch (half) {
+    case 0: return stencil_launch<0, TT>(z, r, dsq, kern, H, W, st);
+    case 1: return stencil_launch<1, TT>(z, r, dsq, kern, H, W, st);
+    case 2: return stencil_launch<2, TT>(z, r, dsq, kern, H, W, st);
+    case 3: return stencil_launch<3, TT>(z, r, dsq, kern, H, W, st);
+    case 4: return stencil_launch<4, TT>(z, r, dsq, kern, H, W, st);
+    case 5: return stencil_launch<5, TT>(z, r, dsq, kern, H, W, st);
+    case 6: return stencil_launch<6, TT>(z, r, dsq, kern, H, W, st);
+    case 7: return stencil_launch<7, TT>(z, r, dsq, kern, H, W, st);
+    default: return stencil_launch<8, TT>(z, r, dsq, kern, H, W, st);
+  }
+}
+
 }  // namespace
+
+extern "C" int mk_learned_precon_stencil(void *z, const void *r, const void *dsq, int H, int W, int half,
+                                         const float *kern, int dtype, void *stream) {
+  MK_CHECK_ARG(MK_DTYPE_OK(dtype), "mk_learned_precon_stencil: bad dtype %d", dtype);
+  MK_CHECK_ARG(H > 0 && W > 0, "mk_learned_precon_stencil: bad map shape %d x %d", H, W);
+  MK_CHECK_ARG(half >= 0 && half <= ST_MAXHALF, "mk_learned_precon_stencil: half-width %d outside 0..%d", half,
+               ST_MAXHALF);
+  MK_CHECK_ARG(z && r && dsq && kern, "mk_learned_precon_stencil: null pointer");
+  MK_CHECK_ARG(z != r, "mk_learned_precon_stencil: z must not alias r (the halo reads neighbours of r)");
+  cudaStream_t st = mk::as_stream(stream);
+  if (dtype == MK_F64)
+    return stencil_dispatch<double>((double *)z, (const double *)r, (const double *)dsq, kern, H, W, half, st);
+  return stencil_dispatch<float>((float *)z, (const float *)r, (const float *)dsq, kern, H, W, half, st);
+}
 
 extern "C" int mk_conv3x3_fwd(const float *x, const float *w, float *y, int B, int Cin, int Cout, int H,
                               int W, void *stream) {

@@ -185,9 +185,14 @@ __global__ void __launch_bounds__(256) k_tod2map_sorted(T *__restrict__ map, con
 // and every pixel hit at most hmax <= 2^hbits times, each term
 // llrint(dat * 2^s) is below 2^(e+1+s) and a pixel's sum below
 // 2^(e+1+s+hbits) = 2^62 for s = 61 - e - hbits.
-// Header words of the scratch: [0] max|dat| as the bits of a non-negative
-// double (atomicMax on the bit pattern orders like the value; NaN sorts
-// above +inf), [1] the shift s chosen by the scatter pass.
+// Header words of the scratch: [0] max|dat| over the finite samples, as the
+// bits of a non-negative double (atomicMax on the bit pattern orders like the
+// value), [1] the shift s chosen by the scatter pass.
+// Non-finite samples (NaN, +-inf) bypass the integers: each is added straight
+// into its own pixel of the map with a floating-point atomic, so a pixel ends
+// up NaN / +-inf exactly when the reference's serial sum would (the IEEE sum
+// of the special values a pixel receives does not depend on their order),
+// and every other pixel is untouched by them.
 struct FixHdr {
   unsigned long long dmax_bits;
   long long shift;
@@ -203,6 +208,9 @@ __device__ __forceinline__ unsigned long long abs_bits(double x) {
   return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
 }
 __device__ __forceinline__ unsigned int abs_bits(float x) { return __float_as_uint(x) & 0x7FFFFFFFu; }
+// |x| bit patterns at or above these are +inf or NaN
+__device__ __forceinline__ bool nonfinite_bits(unsigned long long a) { return a >= 0x7FF0000000000000ull; }
+__device__ __forceinline__ bool nonfinite_bits(unsigned int a) { return a >= 0x7F800000u; }
 
 __device__ __forceinline__ long long shift_round(unsigned long long m, int sh, bool neg) {
   unsigned long long r;
@@ -270,11 +278,22 @@ __device__ __forceinline__ void flush_i64(unsigned long long *__restrict__ acc, 
   if (v != 0 && (uint32_t)key < (uint64_t)npix) atomicAdd(acc + key, (unsigned long long)v);
 }
 
-// shift s from the header, or INT_MIN if there is nothing (or nothing finite) to add
+// shift s from the header; any s when every finite sample is zero
 __device__ __forceinline__ int fixed_shift(const FixHdr *h, int hbits) {
   const double dmax = __longlong_as_double((long long)h->dmax_bits);
-  if (!(dmax > 0.0) || !isfinite(dmax)) return INT_MIN;
+  if (!(dmax > 0.0)) return 0;
   return 61 - ilogb(dmax) - hbits;
+}
+
+// The fixed-point term of one sample; a non-finite sample is added to its
+// pixel of the map directly and contributes nothing to the accumulator.
+template <typename T>
+__device__ __forceinline__ long long fixed_term(T *__restrict__ map, int32_t key, T x, int s, int64_t npix) {
+  if (nonfinite_bits(abs_bits(x))) {
+    if ((uint32_t)key < (uint64_t)npix) atomicAdd(map + key, x);
+    return 0;
+  }
+  return to_fixed(x, s);
 }
 
 
@@ -285,7 +304,7 @@ __global__ void __launch_bounds__(256) k_absmax(const T *__restrict__ dat, int64
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     U a = abs_bits(__ldcs(dat + i));
-    m = a > m ? a : m;
+    m = (a > m && !nonfinite_bits(a)) ? a : m;
   }
   absmax_finish<T>(m, h);
 }
@@ -307,11 +326,11 @@ __device__ __forceinline__ void warp_run_add_i64(unsigned long long *__restrict_
 }
 
 template <typename T, int U>
-__global__ void __launch_bounds__(256) k_scatter_fixed(unsigned long long *__restrict__ acc, const T *__restrict__ dat,
+__global__ void __launch_bounds__(256) k_scatter_fixed(unsigned long long *__restrict__ acc, T *__restrict__ map,
+                                                       const T *__restrict__ dat,
                                                        const int32_t *__restrict__ ipix, int64_t n,
                                                        int64_t npix, int hbits, FixHdr *h) {
   const int s = fixed_shift(h, hbits);
-  if (s == INT_MIN) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) h->shift = s;
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -324,7 +343,7 @@ __global__ void __launch_bounds__(256) k_scatter_fixed(unsigned long long *__res
       int64_t i = base + u * 32 + lane;
       if (i < n) {
         p[u] = __ldcs(ipix + i);
-        v[u] = to_fixed(__ldcs(dat + i), s);
+        v[u] = fixed_term(map, p[u], __ldcs(dat + i), s, npix);
       } else {
         p[u] = -1;
         v[u] = 0;
@@ -384,23 +403,22 @@ __global__ void __launch_bounds__(256, 8) k_absmax8(const T *__restrict__ dat, i
 #pragma unroll
     for (int k = 0; k < 8; k++) {
       U a = abs_bits(v[k]);
-      m = a > m ? a : m;  // NaN patterns sort above +inf
+      m = (a > m && !nonfinite_bits(a)) ? a : m;
     }
   }
   if (blockIdx.x == 0 && threadIdx.x < (n & 7)) {
     U a = abs_bits(dat[(n8 << 3) + threadIdx.x]);
-    m = a > m ? a : m;
+    m = (a > m && !nonfinite_bits(a)) ? a : m;
   }
   absmax_finish<T>(m, h);
 }
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_scatter_fixed8(unsigned long long *__restrict__ acc,
-                                                        const T *__restrict__ dat,
+                                                        T *__restrict__ map, const T *__restrict__ dat,
                                                         const int32_t *__restrict__ ipix, int64_t n,
                                                         int64_t npix, int hbits, FixHdr *h) {
   const int s = fixed_shift(h, hbits);
-  if (s == INT_MIN) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) h->shift = s;
   const int64_t n8 = n >> 3;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -410,10 +428,10 @@ __global__ void __launch_bounds__(256) k_scatter_fixed8(unsigned long long *__re
     load8i(ipix + 8 * g, p);
     load8(dat + 8 * g, v);
     int32_t key = p[0];
-    long long cur = to_fixed(v[0], s);
+    long long cur = fixed_term(map, p[0], v[0], s, npix);
 #pragma unroll
     for (int k = 1; k < 8; k++) {
-      long long t = to_fixed(v[k], s);
+      long long t = fixed_term(map, p[k], v[k], s, npix);
       if (p[k] == key) {
         cur += t;
       } else {
@@ -426,16 +444,15 @@ __global__ void __launch_bounds__(256) k_scatter_fixed8(unsigned long long *__re
   }
   if (blockIdx.x == 0 && threadIdx.x < (n & 7)) {
     int64_t i = (n8 << 3) + threadIdx.x;
-    flush_i64(acc, ipix[i], to_fixed(dat[i], s), npix);
+    flush_i64(acc, ipix[i], fixed_term(map, ipix[i], dat[i], s, npix), npix);
   }
 }
 
-// map += acc * 2^-s, acc cleared; non-finite data poisons the touched map with NaN.
+// map += acc * 2^-s, acc cleared (a pixel already made NaN / inf by a
+// non-finite sample stays so)
 template <typename T>
 __global__ void k_fixed_finalize(T *__restrict__ map, unsigned long long *__restrict__ acc, int64_t npix,
                                  FixHdr *h, int64_t nsamp) {
-  const double dmax = __longlong_as_double((long long)h->dmax_bits);
-  const bool bad = !isfinite(dmax);
   const double inv = ldexp(1.0, -(int)h->shift);
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < npix; p += stride) {
@@ -444,7 +461,6 @@ __global__ void k_fixed_finalize(T *__restrict__ map, unsigned long long *__rest
       map[p] = (T)((double)map[p] + (double)a * inv);
       acc[p] = 0ull;
     }
-    if (bad && p == 0) map[0] = (T)NAN;
   }
 }
 
@@ -796,13 +812,13 @@ int tod2map_fixed_t(void *map, const void *dat, const int32_t *ipix, int64_t n, 
   const bool vec = ((uintptr_t)dat % 16 == 0) && ((uintptr_t)ipix % 16 == 0);
   if (vec) {
     k_absmax8<T><<<mk_grid_fit(k_absmax8<T>, (n + 7) / 8, 256), 256, 0, st>>>((const T *)dat, n, h);
-    k_scatter_fixed8<T><<<mk_grid_fit(k_scatter_fixed8<T>, (n + 7) / 8, 256), 256, 0, st>>>(acc, (const T *)dat, ipix, n, npix,
-                                                                      hbits, h);
+    k_scatter_fixed8<T><<<mk_grid_fit(k_scatter_fixed8<T>, (n + 7) / 8, 256), 256, 0, st>>>(
+        acc, (T *)map, (const T *)dat, ipix, n, npix, hbits, h);
   } else {
     k_absmax<T><<<mk_grid_fit(k_absmax<T>, n, 256), 256, 0, st>>>((const T *)dat, n, h);
     constexpr int U = 4;
-    k_scatter_fixed<T, U><<<mk_grid_fit(k_scatter_fixed<T, U>, (n + U - 1) / U, 256), 256, 0, st>>>(acc, (const T *)dat, ipix, n,
-                                                                            npix, hbits, h);
+    k_scatter_fixed<T, U><<<mk_grid_fit(k_scatter_fixed<T, U>, (n + U - 1) / U, 256), 256, 0, st>>>(
+        acc, (T *)map, (const T *)dat, ipix, n, npix, hbits, h);
   }
   k_fixed_finalize<T><<<mk_grid_fit(k_fixed_finalize<T>, npix, 256), 256, 0, st>>>((T *)map, acc, npix, h, n);
   k_fixed_reset<T><<<1, 1, 0, st>>>(h);
@@ -1061,7 +1077,8 @@ int noalloc_scratch(void **out) {
 extern "C" int mk_tod2map_fixed_noalloc(void *map, const void *dat, const int32_t *ipix,
                                         int64_t ndet, int64_t ndata, int64_t npix, int64_t hmax,
                                         int dtype, void *stream) {
-  MK_CHECK_ARG(npix >= 0 && npix <= NOALLOC_MAX_NPIX,
+  MK_CHECK_ARG(npix >= 0, "mk_tod2map_fixed_noalloc: negative npix=%lld", (long long)npix);
+  MK_CHECK_ARG(npix <= NOALLOC_MAX_NPIX,
                "mk_tod2map_fixed_noalloc: npix=%lld exceeds the built-in scratch limit of %lld pixels "
                "(use mk_tod2map_fixed with caller scratch for larger maps)",
                (long long)npix, (long long)NOALLOC_MAX_NPIX);

@@ -139,10 +139,33 @@ class ConvNet:
 
 
 # ---------------------------------------------------------------- the preconditioner
-class LearnedPrecon:
-    """z = M r with M = D^-1/2 (I + K^T K) D^-1/2 on an (nx, ny) map."""
+def impulse_response(net: "ConvNet") -> torch.Tensor:
+    """The kernel C of K^T K as one convolution: K^T K applied (by the
+    layered convolution kernels) to a unit impulse at the centre of a
+    (4n + 1)^2 canvas, n = the number of layers.  Each layer spreads the
+    impulse by one pixel, so nothing reaches past the canvas and the response
+    is exact; it is then symmetrised (K^T K is symmetric, so this only
+    removes FP32 rounding) so that the stencil apply is symmetric."""
+    half = 2 * len(net.weights)
+    side = 2 * half + 1
+    dev = net.weights[0].device
+    canvas = torch.zeros((1, 1, side, side), dtype=torch.float32, device=dev)
+    canvas[0, 0, half, half] = 1.0
+    c = net.ktk(canvas)[0, 0]
+    return (0.5 * (c + torch.flip(c, dims=(0, 1)))).contiguous()
 
-    def __init__(self, hits: torch.Tensor, net: ConvNet, shape: Tuple[int, int]):
+
+class LearnedPrecon:
+    """z = M r with M = D^-1/2 (I + K^T K) D^-1/2 on an (nx, ny) map.
+
+    By default K^T K is applied as one stencil, its impulse response C
+    (mk_learned_precon_stencil: one launch, 2(2n+1)^2 flops per pixel);
+    ``stencil=False`` runs the 2n layered convolutions instead
+    (mk_learned_precon_apply).  The two agree wherever the residual vanishes
+    within 2n pixels of the map edge (the scan footprints of the benchmark
+    maps stay well inside), and both are symmetric positive definite."""
+
+    def __init__(self, hits: torch.Tensor, net: ConvNet, shape: Tuple[int, int], stencil: bool = True):
         h = hits.reshape(-1).double()
         dsq = torch.where(h > 0, 1.0 / torch.sqrt(torch.clamp(h, min=1e-300)), torch.zeros_like(h))
         self.dsq64 = dsq.contiguous()
@@ -150,16 +173,27 @@ class LearnedPrecon:
         self.net = net
         self.shape = tuple(shape)
         ws = net.weights
+        self.half = 2 * len(ws)
+        self.stencil = bool(stencil) and self.half <= 8
+        self.kern = impulse_response(net) if self.stencil else None
         self._ch = (ctypes.c_int * (len(ws) + 1))(int(ws[0].shape[1]), *[int(w.shape[0]) for w in ws])
-        nb = int(lib().mk_learned_precon_work_bytes(self.shape[0], self.shape[1], len(ws), self._ch))
-        self._work = torch.empty((nb + 3) // 4, dtype=torch.float32, device=hits.device)
+        nb = 0 if self.stencil else int(lib().mk_learned_precon_work_bytes(self.shape[0], self.shape[1],
+                                                                           len(ws), self._ch))
+        self._work = torch.empty(max((nb + 3) // 4, 1), dtype=torch.float32, device=hits.device)
 
     def apply(self, r: torch.Tensor, z: torch.Tensor) -> torch.Tensor:
         """z = M r for flat maps (float32 or float64): one library call
-        (mk_learned_precon_apply, 2n convolution launches)."""
+        (the stencil, or the 2n layered convolution launches)."""
         dsq = self.dsq64 if r.dtype == torch.float64 else self.dsq32
         if z.dtype != r.dtype or r.numel() != dsq.numel() or z.numel() != dsq.numel():
             raise ValueError("LearnedPrecon.apply: r and z must be maps of one dtype and the map's size")
+        if self.stencil:
+            if z.data_ptr() == r.data_ptr():
+                raise ValueError("LearnedPrecon.apply: z must not alias r")
+            check(lib().mk_learned_precon_stencil(_p(z), _p(r), _p(dsq), self.shape[0], self.shape[1],
+                                                  self.half, _p(self.kern), K.dtype_code(z), _stream()),
+                  "learned_precon_stencil")
+            return z
         ws = self.net.weights
         wp = (ctypes.c_void_p * len(ws))(*[w.data_ptr() for w in ws])
         check(lib().mk_learned_precon_apply(_p(z), _p(r), _p(dsq), self.shape[0], self.shape[1], len(ws),
@@ -397,3 +431,112 @@ def save(net: ConvNet, path: str) -> None:
 
 def load(path: str, device=None) -> ConvNet:
     return ConvNet.from_state(dict(np.load(path)), device)
+
+
+# ---------------------------------------------------------------- the seeded recipe
+WEIGHTS_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights")
+
+
+def weights_path(config: str) -> str:
+    """The committed weights for a benchmark configuration (made by train_recipe)."""
+    return os.path.join(WEIGHTS_DIR, f"learned_{config}.npz")
+
+
+def train_recipe(config: str, out: Optional[str] = None, device=None, log=print) -> dict:
+    """Train the preconditioner for a benchmark configuration from seed 0, on
+    the GPU with this module's kernels, and save the weights.
+
+    c1 (1 TOD, 256^2 map): 2500 pairs (r_k, x* - x_k) from FP64 Jacobi solves
+    to 1e-10 on seeded skies (seeds 1000, 1001, ...), 2500 white pairs, Adam
+    for 30 epochs, batch 64.
+    c4 (200 TODs, 2048^2 map): each pair costs an FP32 operator application
+    of 8.8e9 samples, so 2 known-solution skies (seeds 1000, 1001; every 3rd
+    of 240 PCG iterates) and 64 white pairs, 12 epochs, batch 4.
+    Returns a record of the run (pair counts, times, losses)."""
+    import time
+    from .pcg import MixedOp
+    from .projections import make_hits
+    from .synth import CONFIGS, make_todvec
+
+    dev = device or torch.device("cuda", torch.cuda.current_device())
+    cfg = CONFIGS[config]
+    out = out or weights_path(config)
+    t0 = time.perf_counter()
+    if config == "c4":
+        tv, m, _ = build_large(cfg, dev, log=log)
+    else:
+        tv, m = make_todvec(cfg, dev)
+    hits = make_hits(tv, m).map.reshape(-1)
+    op64 = tv.engine(m, torch.float64)
+    op32 = tv.engine(m, torch.float32)
+    t1 = time.perf_counter()
+    if config == "c4":
+        R, E = known_solution_pairs(MixedOp(op32, m.npix, dev), m, hits, [1000, 1001], cfg.pixsize_arcsec,
+                                    n_iter=240, every=3)
+        rw, ew = white_pairs(op32, hits, 64)
+        epochs, batch = 12, 4
+    else:
+        R, E, seed = [], [], 1000
+        while sum(r.shape[0] for r in R) < 2500:
+            r, e, _ = solve_pairs(op64, m, hits, [seed], cfg.pixsize_arcsec)
+            R.append(r)
+            E.append(e)
+            seed += 1
+        R, E = torch.cat(R)[:2500], torch.cat(E)[:2500]
+        rw, ew = white_pairs(op32, hits, 2500)
+        epochs, batch = 30, 64
+    R, E = torch.cat([R, rw]), torch.cat([E, ew])
+    del rw, ew
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    net = ConvNet.init(seed=0, device=dev)
+    hist = train(net, hits, (m.nx, m.ny), R, E, epochs=epochs, batch=batch)
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    save(net, out)
+    rec = {"config": config, "pairs": int(R.shape[0]), "epochs": epochs, "batch": batch,
+           "setup_s": t1 - t0, "pair_gen_s": t2 - t1, "train_s": t3 - t2,
+           "loss_first": hist[0], "loss_last": hist[-1], "out": out}
+    log(rec)
+    return rec
+
+
+def build_large(cfg, dev, log=print):
+    """The TODs of a large configuration generated one at a time on the GPU:
+    each TOD's noise model is built from its data, its contribution to the
+    right-hand side b = sum P^T N d is accumulated, and its timestream is
+    dropped.  Returns (TodVec, SkyMap, b)."""
+    from . import kernels as Kn
+    from .maps import SkyMap
+    from .noise import NoiseSmoothedSVD, clear_plan_cache
+    from .synth import make_tod_info, tod_shapes
+    from .tods import Tod, TodVec
+
+    m = SkyMap(nx=cfg.nx, ny=cfg.ny, device=dev)
+    rhs = torch.zeros(m.npix, dtype=torch.float64, device=dev)
+    tv = TodVec()
+    for k, (ndet, n) in enumerate(tod_shapes(cfg)):
+        info = make_tod_info(cfg, k, ndet, n, dev, with_radec=False)
+        tod = Tod(info)
+        tod.set_noise(NoiseSmoothedSVD)
+        dd = tod.noise.apply_noise(info["dat_calib"])
+        Kn.tod2map(rhs, dd, info["ipix"])
+        del dd
+        tod.info["dat_calib"] = torch.empty((ndet, n), dtype=torch.float64, device="meta")
+        tv.add_tod(tod)
+        del tod, info
+        if log and (k + 1) % 50 == 0:
+            log(f"  {k + 1}/{cfg.ntod} TODs, {torch.cuda.memory_allocated() / 1e9:.1f} GB allocated")
+    clear_plan_cache()
+    torch.cuda.empty_cache()
+    return tv, m, rhs
+
+
+if __name__ == "__main__":
+    import argparse
+    ap = argparse.ArgumentParser(description="train the learned preconditioner of a benchmark configuration")
+    ap.add_argument("--config", default="c1", choices=["c1", "c4"])
+    ap.add_argument("--out", default=None)
+    a = ap.parse_args()
+    train_recipe(a.config, a.out)

@@ -11,6 +11,14 @@ graph -- no host round trip per iteration.
 ``run_pcg_mixed`` is the mixed-precision solver: FP64 vectors, dot products
 and scalars around FP32 operator applications, refined by FP64 true
 residuals (residual replacement) until ||b - A x|| / ||b|| reaches ``tol``.
+
+With more than one rank (torch.distributed), each rank holds its own TODs
+and every operator application inside these solvers is followed by a sum of
+the map over ranks (``RankSumOp``), as the reference's TodVec.dot does
+(minkasi/tods/core.py:1021-1022).  The maps, and so every PCG scalar, are
+then identical on all ranks.  Iterations are not captured as CUDA graphs
+in that case: the exchange runs on the host (gloo) or as a separate NCCL
+call between the captured halves.
 """
 from __future__ import annotations
 
@@ -23,6 +31,7 @@ import numpy as np
 import torch
 
 from . import kernels as K
+from . import parallel
 from ._lib import MK_S_FLAG, MK_S_ITER, MK_S_RR, MK_S_ZR
 from .maps import Mapset, SkyMap, _reducer
 from .tods import TodVec
@@ -46,6 +55,34 @@ class null_precon:
 
     def __mul__(self, val):
         return val
+
+
+class RankSumOp:
+    """A rank's operator followed by the sum of the map over ranks: the one
+    exchange per operator application of the reference's TodVec.dot
+    (minkasi/tods/core.py:1021-1022 -> minkasi/maps/skymap.py:742-783).
+    ``op`` applies this rank's share, A_r = sum over its TODs of P^T N P."""
+
+    def __init__(self, op):
+        self.op = op
+
+    def __getattr__(self, name):
+        return getattr(self.op, name)
+
+    def apply(self, x: torch.Tensor, out: torch.Tensor, accumulate: bool = False) -> torch.Tensor:
+        if not accumulate:
+            self.op.apply(x, out)
+            parallel.allreduce_(out)
+            return out
+        part = self.op.apply(x, torch.empty_like(out))
+        parallel.allreduce_(part)
+        out.add_(part)
+        return out
+
+
+def global_op(op):
+    """The operator summed over ranks; the local operator itself on one rank."""
+    return RankSumOp(op) if parallel.have_mpi() else op
 
 
 def _is_map_precon(precon) -> bool:
@@ -143,9 +180,10 @@ def run_pcg_wprior(b: Mapset, x0: Mapset, tods: TodVec, prior=None, precon=None,
         return _run_pcg_generic(b, x0, tods, prior, precon, mask, maxiter, outroot, save_iters,
                                 save_ind, save_tail, verbose, history)
     t0 = time.time()
-    op = tods.engine(b.maps[0])
+    op = global_op(tods.engine(b.maps[0]))
     x = x0.copy()
-    st = DevicePCG(op, b.maps[0].map, x.maps[0].map, _precon_arg(precon), graph=graph)
+    st = DevicePCG(op, b.maps[0].map, x.maps[0].map, _precon_arg(precon),
+                   graph=graph and not parallel.have_mpi())
     st.start()
     bnorm = math.sqrt(b.dot(b)) if tol is not None else None
     nsamp = tods.get_nsamp()
@@ -278,8 +316,9 @@ def run_pcg_mixed(b: Mapset, x0: Mapset, tods: TodVec, precon=None, tol: float =
         return _run_refine(b, x0, tods, precon, tol, inner_iters, max_outer, graph, verbose,
                            history, inner_precon, on_outer)
     m64 = b.maps[0]
-    op64 = tods.engine(m64, torch.float64)
-    op32 = tods.engine(m64, torch.float32)
+    op64 = global_op(tods.engine(m64, torch.float64))
+    op32 = global_op(tods.engine(m64, torch.float32))
+    graph = graph and not parallel.have_mpi()
     x = x0.copy()
     xf = x.maps[0].map.reshape(-1)
     bf = m64.map.reshape(-1)
@@ -347,8 +386,9 @@ def run_pcg_mixed(b: Mapset, x0: Mapset, tods: TodVec, precon=None, tol: float =
 def _run_refine(b, x0, tods, precon, tol, inner_iters, max_outer, graph, verbose, history,
                 inner_precon, on_outer) -> Mapset:
     m64 = b.maps[0]
-    op64 = tods.engine(m64, torch.float64)
-    op32 = tods.engine(m64, torch.float32)
+    op64 = global_op(tods.engine(m64, torch.float64))
+    op32 = global_op(tods.engine(m64, torch.float32))
+    graph = graph and not parallel.have_mpi()
     x = x0.copy()
     xf = x.maps[0].map.reshape(-1)
     bf = m64.map.reshape(-1)

@@ -147,6 +147,46 @@ def test_tod2map_ragged_sizes_and_bad_pixels(K, n, kern):
     assert K.tod2map_status() == 0
 
 
+@pytest.mark.parametrize("kern", ["atomic", "staged", "fixed", "sorted"])
+def test_tod2map_nonfinite_samples_touch_only_their_pixels(K, kern):
+    """NaN and +-inf samples: as in the reference's serial sum, a pixel is
+    NaN when one of its samples is NaN or it gets both +inf and -inf, +-inf
+    when it gets one sign of inf, and every other pixel is the finite sum."""
+    rng = np.random.default_rng(7)
+    ndet, ndata, npix = 4, 20_000, 500
+    walk = np.cumsum(rng.integers(-1, 2, size=(ndet, ndata)), axis=1) // 3
+    ipix = np.mod(walk + rng.integers(0, npix, size=(ndet, 1)), npix).astype(np.int32)
+    dat = rng.standard_normal((ndet, ndata))
+    dat[0, 100] = np.nan
+    dat[1, 5000] = np.inf
+    dat[3, 9000] = -np.inf
+    p = ipix[2, 7000]
+    j = np.flatnonzero((ipix.ravel() == p))
+    j = j[j != 2 * ndata + 7000][0]
+    dat[2, 7000] = np.inf
+    dat.ravel()[j] = -np.inf
+    ref = np.zeros(npix)
+    oracle.tod2map_serial(ref, dat, ipix)
+    assert np.isnan(ref).sum() >= 2 and np.isinf(ref).sum() >= 1
+    m = torch.zeros(npix, dtype=torch.float64, device=cuda)
+    gd, gi = dev(dat), dev(ipix)
+    if kern == "atomic":
+        K.tod2map(m, gd, gi)
+    elif kern == "staged":
+        K.tod2map_staged(m, gd, gi)
+    elif kern == "fixed":
+        hmax = int(np.bincount(ipix.ravel(), minlength=npix).max())
+        K.tod2map_fixed(m, gd, gi, hmax, K.FixedScratch(npix, cuda))
+    else:
+        K.PixPlan(gi, npix).tod2map(m, gd)
+    got = m.cpu().numpy()
+    assert np.array_equal(np.isnan(got), np.isnan(ref))
+    assert np.array_equal(np.isposinf(got), np.isposinf(ref))
+    assert np.array_equal(np.isneginf(got), np.isneginf(ref))
+    fin = np.isfinite(ref)
+    assert rel(got[fin], ref[fin]) < 1e-12
+
+
 def test_tod2map_staged_rejects_host_and_misaligned(K, gold):
     g = gold("proj.npz")
     host = torch.from_numpy(np.ascontiguousarray(g["dat"])).pin_memory()

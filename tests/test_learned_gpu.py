@@ -94,7 +94,7 @@ def test_fused_precon_apply(L, shape, dtype):
     hits_np = rng.integers(0, 5, size=n).astype(np.float64)
     hits = torch.from_numpy(hits_np).to(cuda)
     net = L.ConvNet.init(seed=2, scale=0.3, device=cuda)
-    M = L.LearnedPrecon(hits, net, shape)
+    M = L.LearnedPrecon(hits, net, shape, stencil=False)
     r = torch.from_numpy(rng.standard_normal(n)).to(cuda, dtype)
     z = torch.empty_like(r)
     M.apply(r, z)
@@ -122,3 +122,45 @@ def test_fused_precon_apply(L, shape, dtype):
     r2 = r.clone()
     M.apply(r2, r2)
     assert torch.equal(r2, z)
+
+
+@pytest.mark.parametrize("shape", [(40, 36), (300, 517)])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_stencil_apply_equals_layered_inside_the_edge(L, shape, dtype):
+    """K^T K as one 17 x 17 stencil (its impulse response) against the 8
+    layered convolutions and the float64 oracle, with the hit pixels (and so
+    u) at least 8 pixels from the map edge, where the two forms are the same
+    operator; and the stencil form is symmetric positive definite."""
+    rng = np.random.default_rng(shape[1])
+    n = shape[0] * shape[1]
+    hits_np = rng.integers(0, 5, size=shape).astype(np.float64)
+    hits_np[:8], hits_np[-8:], hits_np[:, :8], hits_np[:, -8:] = 0, 0, 0, 0
+    hits = torch.from_numpy(hits_np.ravel()).to(cuda)
+    net = L.ConvNet.init(seed=4, scale=0.4, device=cuda)
+    S = L.LearnedPrecon(hits, net, shape)
+    assert S.stencil and tuple(S.kern.shape) == (17, 17)
+    Lay = L.LearnedPrecon(hits, net, shape, stencil=False)
+    r = torch.from_numpy(rng.standard_normal(n)).to(cuda, dtype)
+    zs, zl = torch.empty_like(r), torch.empty_like(r)
+    S.apply(r, zs)
+    Lay.apply(r, zl)
+    assert rel(zs.double().cpu().numpy(), zl.double().cpu().numpy()) < 1e-5
+    d = S.dsq64.cpu().numpy()
+    u64 = d * r.double().cpu().numpy()
+    a = u64.reshape(1, 1, *shape)
+    ws = [w.double().cpu().numpy() for w in net.weights]
+    for w in ws:
+        a = lo.conv_fwd(a, w)
+    for w in reversed(ws):
+        a = lo.conv_adj(a, w)
+    ref = d * (u64 + a.reshape(-1))
+    assert rel(zs.double().cpu().numpy(), ref) < 1e-5
+    b = torch.from_numpy(rng.standard_normal(n)).to(cuda, torch.float64)
+    a64 = r.double()
+    Ma, Mb = torch.empty_like(a64), torch.empty_like(b)
+    S.apply(a64, Ma)
+    S.apply(b, Mb)
+    assert abs(float(b @ Ma) - float(a64 @ Mb)) < 1e-5 * float((a64.abs() * b.abs()).sum())
+    assert float(a64 @ Ma) > 0
+    with pytest.raises(ValueError):
+        S.apply(a64, a64)

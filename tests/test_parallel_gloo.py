@@ -69,6 +69,68 @@ def _hb_worker(rank, world, port, q, fail_rank):
     time.sleep(1.0)
 
 
+class _DenseShare:
+    """A rank's share of an operator, mocked on the CPU: A_r = B_r^T B_r over
+    the rows of B this rank owns (the TODs of a rank, in miniature)."""
+
+    def __init__(self, B):
+        self.B = B
+
+    def apply(self, x, out, accumulate=False):
+        y = self.B.T @ (self.B @ x)
+        if accumulate:
+            out += y
+        else:
+            out.copy_(y)
+        return out
+
+
+def _ranksum_worker(rank, world, port, q, fail_rank):
+    import datetime
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    torch.distributed.init_process_group("gloo", rank=rank, world_size=world,
+                                         timeout=datetime.timedelta(seconds=20))
+    from minkasi_gb300 import parallel
+    from minkasi_gb300.pcg import RankSumOp, global_op
+    try:
+        g = torch.Generator().manual_seed(0)
+        B = torch.randn(40, 12, generator=g, dtype=torch.float64)
+        costs = [float(1 + (i % 7)) for i in range(B.shape[0])]
+        mine = parallel.partition(costs, world)[rank]
+        op = global_op(_DenseShare(B[mine]))
+        assert isinstance(op, RankSumOp)
+        x = torch.randn(12, generator=g, dtype=torch.float64)
+        full = B.T @ (B @ x)
+        y = op.apply(x, torch.empty(12, dtype=torch.float64))
+        acc = torch.ones(12, dtype=torch.float64)
+        op.apply(x, acc, accumulate=True)
+        # a few CG steps on the summed operator: every rank must hold the
+        # same iterates, equal to the one-rank solve
+        A = B.T @ B + torch.eye(12, dtype=torch.float64)
+        class Shifted:
+            def apply(self_, v, out, accumulate=False):
+                op.apply(v, out)
+                out += v  # the identity, added after the sum (same on every rank)
+                return out
+        b = torch.randn(12, generator=g, dtype=torch.float64)
+        xs, r = torch.zeros(12, dtype=torch.float64), b.clone()
+        p, Ap = r.clone(), torch.empty(12, dtype=torch.float64)
+        rr = float(r @ r)
+        for _ in range(12):
+            Shifted().apply(p, Ap)
+            a = rr / float(p @ Ap)
+            xs += a * p
+            r -= a * Ap
+            rr_new = float(r @ r)
+            p = r + (rr_new / rr) * p
+            rr = rr_new
+        q.put((rank, float((y - full).abs().max() / full.abs().max()),
+               float((acc - 1 - full).abs().max() / full.abs().max()),
+               float((A @ xs - b).norm() / b.norm()), sorted(mine), xs.tolist()))
+    finally:
+        torch.distributed.destroy_process_group()
+
+
 def _run(world, fail_rank=-1, target=None):
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
@@ -100,3 +162,16 @@ def test_failed_rank_is_detected_by_heartbeat():
     assert out[0][1] == "peer-failure" and out[0][2] == [0]
     ok = _run(2, target=_hb_worker)
     assert all(o[1] == "ok" and o[2] == [0, 1, 2] for o in ok)
+
+
+def test_rank_sum_operator_sums_the_shares():
+    """Each rank applies the operator of the items it owns (a greedy
+    partition), and RankSumOp sums the map over ranks after every
+    application: both ranks see the full operator, and a CG run on it gives
+    the same iterates on every rank, converged on the full system."""
+    out = _run(2, target=_ranksum_worker)
+    (_, e0, a0, res0, own0, x0), (_, e1, a1, res1, own1, x1) = out
+    assert max(e0, e1, a0, a1) < 1e-13
+    assert sorted(own0 + own1) == list(range(40)) and not set(own0) & set(own1)
+    assert x0 == x1
+    assert res0 < 1e-8
