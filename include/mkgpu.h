@@ -326,6 +326,14 @@ int mk_dct1_engine(const mk_dct_plan *plan);
  * mk_dct1_engine, *L the transform length (2(n-1), or Bluestein's M), and
  * its four-step split *L1 x *L2 (0 x 0 for cuFFT). */
 int mk_dct1_describe(int64_t n, int *engine, int64_t *L, int *L1, int *L2);
+/* The four-step split (the tile shape of the two passes) that FP32 plans
+ * created after the call take: rank 0 (default) = the divisor pair L1 x L2
+ * of the transform length closest to sqrt(L), rank r = the r-th next
+ * closest (the last one when there are fewer).  The autotuner times a few
+ * ranks per TOD shape.  mk_noise_split reports a noise plan's L1 x L2
+ * (0 x 0 for cuFFT).  No reference counterpart (FFTW plans its own). */
+int mk_set_fft4_split(int rank);
+int mk_get_fft4_split(void);
 
 /* NoiseSmoothedSVD.apply_noise, minkasi/mapmaking/noise.py:680-714:
  *   out = halve_ends( vT . DCT1( mywt[:, :ndata] * DCT1( v . dat ) ) )
@@ -347,6 +355,7 @@ int mk_apply_noise(mk_noise_plan *plan, const void *v, const void *vT, const voi
                    int64_t mywt_ld, const void *dat, void *out, int rot_mode, void *stream);
 int mk_noise_plan_destroy(mk_noise_plan *plan);
 int mk_noise_engine(const mk_noise_plan *plan);
+int mk_noise_split(const mk_noise_plan *plan, int *L1, int *L2);
 
 /* The detector rotation alone, R = A . X, for the plan's (ndet, ndata):
  * A (ndet, ndet), X and R (ndet, ndata), dtype-typed, R must not alias X.

@@ -89,6 +89,9 @@ SIGNATURES = {
     "mk_dct1_describe": (_i32, [_i64, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int64),
                                 ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "mk_noise_engine": (_i32, [_vp]),
+    "mk_noise_split": (_i32, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    "mk_set_fft4_split": (_i32, [_i32]),
+    "mk_get_fft4_split": (_i32, []),
     "mk_learned_precon_work_bytes": (_sz, [_i32, _i32, _i32, _vp]),
     "mk_learned_precon_apply": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp, _sz, _i32, _vp]),
     "mk_learned_precon_stencil": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _i32, _vp]),

@@ -4,6 +4,8 @@ the choice in a JSON file keyed on (GPU, dtype, detector counts, samples,
 map size, hit density).
 
 Cache file: $MINKASI_GB300_AUTOTUNE, else ~/.cache/minkasi_gb300/autotune.json.
+It also picks, per TOD shape, the DCT-I transform and the four-step split
+L1 x L2 (the tile shape of the FFT passes).
 Set MINKASI_GB300_TOD2MAP=atomic|staged|fixed|sorted (or ..._ROT=1|2|3, or
 ..._DCT=0|1|2, the kernels.set_dct_engine values) to force a choice.
 """
@@ -137,34 +139,44 @@ def choose_rot_mode(op) -> int:
     return best
 
 
-def with_dct_engine(engine: int, fn):
-    """fn() with kernels.set_dct_engine(engine) in force (plans created in fn
-    keep it), then the previous engine restored."""
-    prev = K.dct_engine()
-    K.set_dct_engine(engine)
+def with_dct_engine(engine, fn):
+    """fn() with kernels.set_dct_engine in force (plans created in fn keep
+    it), then the previous setting restored.  ``engine`` is an engine number
+    or an (engine, split rank) pair: the rank also selects the four-step
+    split L1 x L2 (kernels.set_fft4_split)."""
+    e, rank = (engine, 0) if isinstance(engine, int) else (int(engine[0]), int(engine[1]))
+    prev, prev_rank = K.dct_engine(), K.fft4_split()
+    K.set_dct_engine(e)
+    K.set_fft4_split(rank)
     try:
         return fn()
     finally:
         K.set_dct_engine(prev)
+        K.set_fft4_split(prev_rank)
 
 
-def choose_dct_engines(op, shapes: Sequence[Tuple[int, int]]) -> Dict[Tuple[int, int], int]:
-    """Per TOD shape of an FP32 operator, the faster noise filter of the
-    four-step FFT (engine 0, Bluestein included) and cuFFT (engine 1), timed
-    on the shape's first TOD with the rotation the shape will use; FP64
+SPLIT_RANKS = 3  # four-step splits tried per TOD shape (closest to sqrt(L) first)
+
+
+def choose_dct_engines(op, shapes: Sequence[Tuple[int, int]]) -> Dict[Tuple[int, int], Tuple[int, int]]:
+    """Per TOD shape of an FP32 operator, the fastest noise filter among the
+    four-step FFT (engine 0, Bluestein included) with each of its
+    SPLIT_RANKS closest L1 x L2 splits (the tile shapes of its two passes)
+    and cuFFT (engine 1), timed on the shape's first TOD with the rotation
+    the shape will use.  Returns {shape: (engine, split rank)}; FP64
     operators keep the current engine (their plans use cuFFT)."""
     cur = K.dct_engine()
     if op.dtype != torch.float32:
-        return {s: cur for s in shapes}
+        return {s: (cur, 0) for s in shapes}
     forced = os.environ.get("MINKASI_GB300_DCT")
     if forced:
-        return {s: int(forced) for s in shapes}
+        return {s: (int(forced), 0) for s in shapes}
     gpu = torch.cuda.get_device_name(op.device)
     out, todo = {}, []
     for s in shapes:
-        hit = _lookup(f"dct|{gpu}|{s[0]}x{s[1]}")
-        if hit in (0, 1):
-            out[s] = int(hit)
+        hit = _lookup(f"dct2|{gpu}|{s[0]}x{s[1]}")
+        if isinstance(hit, list) and len(hit) == 2:
+            out[s] = (int(hit[0]), int(hit[1]))
         else:
             todo.append(s)
     if not todo:
@@ -178,16 +190,18 @@ def choose_dct_engines(op, shapes: Sequence[Tuple[int, int]]) -> Dict[Tuple[int,
         x = torch.randn((nd, n), dtype=op.dtype, device=op.device)
         y = torch.empty_like(x)
         mode = 2 if nd in (32, 64, 128, 256) else 1
-        times = {}
-        for e in (0, 1):
-            plan = with_dct_engine(e, lambda: K.NoisePlan(nd, n, op.dtype, op.device, workspace=ws))
-            if e == 0 and plan.engine == 1:
-                break  # no four-step transform for this length
-            times[e] = time_ms(lambda: plan.apply(v, vT, w, x, out=y, rot_mode=mode))
+        times, seen = {}, set()
+        for cand in [(0, r) for r in range(SPLIT_RANKS)] + [(1, 0)]:
+            plan = with_dct_engine(cand, lambda: K.NoisePlan(nd, n, op.dtype, op.device, workspace=ws))
+            if cand[0] == 0 and (plan.engine == 1 or plan.split in seen):
+                del plan
+                continue  # no four-step transform, or the same split again
+            seen.add(plan.split)
+            times[cand] = time_ms(lambda: plan.apply(v, vT, w, x, out=y, rot_mode=mode))
             del plan
-        best = min(times, key=times.get) if times else 1
+        best = min(times, key=times.get)
         out[s] = best
-        _store(f"dct|{gpu}|{nd}x{n}", best)
+        _store(f"dct2|{gpu}|{nd}x{n}", list(best))
         del x, y
     del ws
     return out

@@ -1,7 +1,10 @@
 // FP32 DCT-I by a four-step FFT in shared memory (see mk_fft4.cuh).
 #include <cufft.h>
 
+#include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <utility>
 #include <vector>
 
 #include "mk_async.cuh"
@@ -144,17 +147,20 @@ struct PassA {
   const float2 *U;  // AM_CPLX: this pair's sequence
   const float2 *chirp;
   bool has2;
-  int L1, j1_0, nb, m, Lx;
+  int L1, j1_0, nb, m, Lx, M;
   const int *iperm;
 };
 
+// input at position j: the even extension e_j (AM_DCT, j < 2m); for
+// Bluestein, z_{|i|} c_{|i|} at the position j = i mod M of i in [-m + 1, m]
+// and zero in between; or the sequence U
 template <int AM>
 __device__ __forceinline__ float2 a_input(const PassA &pa, int j) {
   if (AM == AM_CPLX) return pa.U[j];
-  if (AM == AM_BLUE && j >= pa.Lx) return make_float2(0.f, 0.f);
-  const int jj = j <= pa.m ? j : pa.Lx - j;
+  if (AM == AM_BLUE && j > pa.m && j <= pa.M - pa.m) return make_float2(0.f, 0.f);
+  const int jj = j <= pa.m ? j : (AM == AM_BLUE ? pa.M : pa.Lx) - j;
   const float2 z = make_float2(__ldg(pa.x1 + jj), pa.has2 ? __ldg(pa.x2 + jj) : 0.f);
-  return AM == AM_BLUE ? cmul(z, __ldg(pa.chirp + j)) : z;
+  return AM == AM_BLUE ? cmul(z, __ldg(pa.chirp + jj)) : z;
 }
 
 template <int R, bool FIRST, int AM>
@@ -225,6 +231,7 @@ __global__ void __launch_bounds__(NT) k_fft4_a(const float *__restrict__ x, int6
   pa.nb = min(FB, L1 - pa.j1_0);
   pa.m = (int)p.m;
   pa.Lx = (int)p.Lx;
+  pa.M = (int)p.L;
   pa.iperm = p.iperm2;
   const int S = p.nr2;
   if (S == 0) {  // L2 == 1: the column is its own transform
@@ -457,7 +464,7 @@ TableLayout layout(const Fft4Dev &d) {
   t.tblk = o;
   o += al((size_t)d.L1 * d.nb32 * sizeof(float2));
   t.chirp = o;
-  o += d.blue ? al((size_t)d.Lx * sizeof(float2)) : 0;
+  o += d.blue ? al((size_t)(d.m + 1) * sizeof(float2)) : 0;
   t.bhat = o;
   o += d.blue ? al((size_t)d.L * sizeof(float2)) : 0;
   t.total = o;
@@ -499,8 +506,16 @@ bool g_attr[64] = {false};
 
 }  // namespace
 
-// L1 x L2 split of a transform of length L (the divisor pair closest to
-// sqrt(L) with both parts <= LMAX and L1 > 1), radices and stage constants
+// Which L1 x L2 split new plans take: 0 = the divisor pair closest to
+// sqrt(L), r = the r-th next closest (the last one when there are fewer).
+// Set by the autotuner around plan creation; a plan keeps its split.
+static std::atomic<int> g_split_rank{0};
+void fft4_set_split_rank(int r) { g_split_rank.store(r < 0 ? 0 : r); }
+int fft4_split_rank() { return g_split_rank.load(); }
+
+// L1 x L2 split of a transform of length L (by g_split_rank among the
+// divisor pairs with both parts <= LMAX and L1 > 1, ordered by closeness to
+// sqrt(L)), radices and stage constants
 static bool split_len(int64_t L, Fft4Dev *t) {
   if (L < 2 || L > (int64_t)FFT4_LMAX * FFT4_LMAX) return false;
   std::vector<int> f;
@@ -516,18 +531,16 @@ static bool split_len(int64_t L, Fft4Dev *t) {
       if (!seen) ds.push_back(v);
     }
   }
-  int64_t best = -1;
-  double bc = 1e300;
+  std::vector<std::pair<double, int64_t>> cand;
   for (int64_t a : ds) {
     const int64_t b = L / a;
     if (a > FFT4_LMAX || b > FFT4_LMAX || a == 1) continue;  // pass B needs at least one stage
-    const double c = std::fabs(std::log((double)a) - std::log((double)b));
-    if (c < bc) {
-      bc = c;
-      best = a;
-    }
+    cand.push_back({std::fabs(std::log((double)a) - std::log((double)b)), a});
   }
-  if (best < 0) return false;
+  if (cand.empty()) return false;
+  std::sort(cand.begin(), cand.end());
+  const size_t rank = (size_t)g_split_rank.load();
+  const int64_t best = cand[rank < cand.size() ? rank : cand.size() - 1].second;
   t->L = L;
   t->L1 = (int)best;
   t->L2 = (int)(L / best);
@@ -562,7 +575,7 @@ bool fft4_shape(int64_t n, Fft4Dev *d, bool bluestein) {
     return true;
   }
   if (!bluestein) return false;
-  for (int64_t M = 2 * t.Lx - 1; M <= (int64_t)FFT4_LMAX * FFT4_LMAX; M++) {
+  for (int64_t M = 3 * t.m; M <= (int64_t)FFT4_LMAX * FFT4_LMAX; M++) {
     if (split_len(M, &t)) {
       t.blue = true;
       *d = t;
@@ -578,17 +591,18 @@ size_t fft4_t_bytes(const Fft4Dev &d, int64_t nrow) {
   return (d.blue ? 2 : 1) * (size_t)((nrow + 1) / 2) * (size_t)d.L * sizeof(float2);
 }
 
-// B^ = DFT_M(b) / M with b_t = conj(c_t) at t mod M for |t| < Lx, in double
-// precision through a cuFFT Z2Z transform, rounded to float
+// B^ = DFT_M(b) / M with b_t = conj(c_t) at t mod M for t in [-m, 2m - 1]
+// (M >= 3m keeps those positions distinct), in double precision through a
+// cuFFT Z2Z transform, rounded to float
 static int bluestein_bhat(const Fft4Dev &d, float2 *out) {
-  const int64_t M = d.L, Lx = d.Lx;
+  const int64_t M = d.L, Lx = d.Lx, m = d.m;
   std::vector<cufftDoubleComplex> b((size_t)M);
   for (auto &v : b) v.x = v.y = 0.0;
-  for (int64_t t = 0; t < Lx; t++) {
+  for (int64_t t = 0; t < 2 * m; t++) {
     const double a = M_PI * (double)((t * t) % (2 * Lx)) / (double)Lx;  // conj(c_t) = exp(+i a)
     b[(size_t)t].x = std::cos(a);
     b[(size_t)t].y = std::sin(a);
-    if (t > 0) b[(size_t)(M - t)] = b[(size_t)t];
+    if (t > 0 && t <= m) b[(size_t)(M - t)] = b[(size_t)t];
   }
   cufftDoubleComplex *db = nullptr;
   MK_CUDA(cudaMalloc(&db, (size_t)M * sizeof(cufftDoubleComplex)));
@@ -638,7 +652,7 @@ int fft4_init(Fft4Plan *p, int64_t n, void *dev_tables, bool bluestein) {
   }
   if (d.blue) {
     float2 *chirp = (float2 *)(h.data() + t.chirp);
-    for (int64_t j = 0; j < d.Lx; j++) chirp[j] = unit((double)((j * j) % (2 * d.Lx)), 2.0 * (double)d.Lx);
+    for (int64_t j = 0; j <= d.m; j++) chirp[j] = unit((double)((j * j) % (2 * d.Lx)), 2.0 * (double)d.Lx);
     const int rc = bluestein_bhat(d, (float2 *)(h.data() + t.bhat));
     if (rc) return rc;
   }

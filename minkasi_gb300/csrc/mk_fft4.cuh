@@ -19,13 +19,18 @@
 // double precision on the host.
 //
 // Lengths whose 2m has a prime factor above 11 (minkasi's truncate_tod leaves
-// some) go through Bluestein's algorithm on the same passes: with the chirp
-// c_j = exp(-i pi j^2 / L), DFT(z)_k = c_k (a (*) b)_k, a_j = z_j c_j (zero
-// past L), b_t = conj(c_t) for |t| < L, a circular convolution of a smooth
-// length M >= 2L - 1:  pass A forms a from the rows; pass B multiplies by
-// B^ = DFT_M(b) / M and stores U = conj(DFT(a) B^); pass A and pass B run
-// again on U, and the last stage writes c_k conj(DFT(U)_k) for k <= m with the
-// usual epilogue.
+// some) go through Bluestein's algorithm on the same passes.  With the chirp
+// c_t = exp(-i pi t^2 / 2m) (even in t), W^{jk} = c_j c_k conj(c_{k-j}) for
+// W = exp(-i pi / m), and the extension is periodic in j with period 2m, so
+//   F_k = c_k sum_{j=-m+1}^{m} (e_j c_j) conj(c_{k-j}),   e_{-j} = e_j = z_{|j|}.
+// Only k = 0..m are needed, so the lags k - j cover [-m, 2m - 1]: 3m values.
+// F is then a circular convolution a (*) b of a smooth length M >= 3m, with
+// a at positions j mod M (z_{|j|} c_{|j|}, zero elsewhere) and b_t = conj(c_t)
+// at t mod M for t in [-m, 2m - 1] (one quarter shorter than the M >= 4m - 1
+// of taking j, k over a whole period).  Pass A forms a from the rows; pass B
+// multiplies by B^ = DFT_M(b) / M and stores U = conj(DFT(a) B^); pass A and
+// pass B run again on U, and the last stage writes c_k conj(DFT(U)_k) for
+// k <= m with the usual epilogue.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -51,7 +56,7 @@ struct Fft4Dev {
   const int *iperm1, *iperm2;  // natural index at each digit-reversed (DIT input) position
   // four-step twiddle W_L^{j1 k2} = tblk[j1 nb32 + k2 / 32] * tlane[32 j1 + k2 % 32]
   const float2 *tlane, *tblk;
-  const float2 *chirp;  // Bluestein: c_j, j < Lx
+  const float2 *chirp;  // Bluestein: c_t, t <= m
   const float2 *bhat;   // Bluestein: DFT_M(b) / M
 };
 
@@ -65,9 +70,12 @@ struct Fft4Plan {
 
 // The transform for rows of length n: L = 2(n-1) split into L1 x L2 with
 // radix lists, or, when 2(n-1) has a prime factor above 11 and `bluestein`
-// is set, the smallest splittable M >= 4(n-1) - 1; false when neither fits
+// is set, the smallest splittable M >= 3(n-1); false when neither fits
 // within FFT4_LMAX x FFT4_LMAX.
 bool fft4_shape(int64_t n, Fft4Dev *d, bool bluestein = true);
+// the rank of the L1 x L2 split new plans take (0: closest to sqrt(L))
+void fft4_set_split_rank(int r);
+int fft4_split_rank();
 // bytes of the device tables for that shape
 size_t fft4_table_bytes(const Fft4Dev &d);
 // bytes of the scratch (T, and U for Bluestein) for nrow rows

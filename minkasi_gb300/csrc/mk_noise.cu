@@ -545,6 +545,22 @@ extern "C" int mk_dct1_engine(const mk_dct_plan *plan) { return plan ? engine_of
 
 extern "C" int mk_noise_engine(const mk_noise_plan *plan) { return plan ? engine_of(plan->core) : 1; }
 
+extern "C" int mk_set_fft4_split(int rank) {
+  MK_CHECK_ARG(rank >= 0 && rank < 16, "mk_set_fft4_split: rank must be 0..15 (got %d)", rank);
+  mk::fft4_set_split_rank(rank);
+  return MK_OK;
+}
+
+extern "C" int mk_get_fft4_split(void) { return mk::fft4_split_rank(); }
+
+extern "C" int mk_noise_split(const mk_noise_plan *plan, int *L1, int *L2) {
+  MK_CHECK_ARG(plan && L1 && L2, "mk_noise_split: null argument");
+  const bool four = plan->core.own;
+  *L1 = four ? plan->core.f4.d.L1 : 0;
+  *L2 = four ? plan->core.f4.d.L2 : 0;
+  return MK_OK;
+}
+
 extern "C" int mk_dct1_describe(int64_t n, int *engine, int64_t *L, int *L1, int *L2) {
   MK_CHECK_ARG(engine && L && L1 && L2, "mk_dct1_describe: null output");
   MK_CHECK_ARG(n >= 2, "mk_dct1_describe: n must be >= 2 (got %lld)", (long long)n);

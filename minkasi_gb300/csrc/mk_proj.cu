@@ -25,35 +25,60 @@ __device__ __forceinline__ T gather(const T *__restrict__ map, int32_t p, int64_
 }
 
 // ---- map2tod --------------------------------------------------------------
-// Vector body: each thread moves 4 consecutive samples (one 16-byte ipix
-// load, 16/32-byte dat accesses).  Requires ipix and dat 16-byte aligned;
-// the host peels nothing -- it falls back to the scalar kernel otherwise.
+// Vector body: a warp takes 32 x MU consecutive 16-byte ipix groups (4
+// samples each) and lane l the groups l, l + 32, ... of it, so every load and
+// store instruction of the warp covers a contiguous span.  The MU index loads
+// are all issued before the dependent map gathers: one 16-byte load in flight
+// per thread leaves the stream latency-bound (about 32 KB in flight per SM at
+// full occupancy, below what HBM needs), MU = 4 gives 64 B per thread.
+// Requires ipix and dat 16-byte aligned; the host falls back to the scalar
+// kernel otherwise.
+constexpr int MU = 4;
+
 template <typename T, bool ADD>
 __global__ void __launch_bounds__(256) k_map2tod_vec(T *__restrict__ dat, const T *__restrict__ map,
                                                      const int32_t *__restrict__ ipix, int64_t n,
                                                      int64_t npix) {
   const int64_t n4 = n >> 2;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarp = ((int64_t)gridDim.x * blockDim.x) >> 5;
   const int4 *ip4 = reinterpret_cast<const int4 *>(ipix);
-  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n4; g += stride) {
-    int4 p = __ldcs(ip4 + g);
-    T v0 = gather(map, p.x, npix), v1 = gather(map, p.y, npix);
-    T v2 = gather(map, p.z, npix), v3 = gather(map, p.w, npix);
-    if constexpr (sizeof(T) == 8) {
-      double2 *d2 = reinterpret_cast<double2 *>(dat) + 2 * g;
-      if (ADD) {
-        double2 a = __ldcs(d2), b = __ldcs(d2 + 1);
-        v0 += a.x; v1 += a.y; v2 += b.x; v3 += b.y;
+  for (int64_t base = warp * (32 * MU); base < n4; base += nwarp * (32 * MU)) {
+    int4 p[MU];
+#pragma unroll
+    for (int u = 0; u < MU; u++) {
+      const int64_t g = base + 32 * u + lane;
+      p[u] = g < n4 ? __ldcs(ip4 + g) : make_int4(-1, -1, -1, -1);
+    }
+    T v[MU][4];
+#pragma unroll
+    for (int u = 0; u < MU; u++) {
+      v[u][0] = gather(map, p[u].x, npix);
+      v[u][1] = gather(map, p[u].y, npix);
+      v[u][2] = gather(map, p[u].z, npix);
+      v[u][3] = gather(map, p[u].w, npix);
+    }
+#pragma unroll
+    for (int u = 0; u < MU; u++) {
+      const int64_t g = base + 32 * u + lane;
+      if (g >= n4) continue;
+      if constexpr (sizeof(T) == 8) {
+        double2 *d2 = reinterpret_cast<double2 *>(dat) + 2 * g;
+        if (ADD) {
+          const double2 a = __ldcs(d2), b = __ldcs(d2 + 1);
+          v[u][0] += a.x; v[u][1] += a.y; v[u][2] += b.x; v[u][3] += b.y;
+        }
+        __stcs(d2, make_double2(v[u][0], v[u][1]));
+        __stcs(d2 + 1, make_double2(v[u][2], v[u][3]));
+      } else {
+        float4 *d4 = reinterpret_cast<float4 *>(dat) + g;
+        if (ADD) {
+          const float4 a = __ldcs(d4);
+          v[u][0] += a.x; v[u][1] += a.y; v[u][2] += a.z; v[u][3] += a.w;
+        }
+        __stcs(d4, make_float4(v[u][0], v[u][1], v[u][2], v[u][3]));
       }
-      __stcs(d2, make_double2(v0, v1));
-      __stcs(d2 + 1, make_double2(v2, v3));
-    } else {
-      float4 *d4 = reinterpret_cast<float4 *>(dat) + g;
-      if (ADD) {
-        float4 a = __ldcs(d4);
-        v0 += a.x; v1 += a.y; v2 += a.z; v3 += a.w;
-      }
-      __stcs(d4, make_float4(v0, v1, v2, v3));
     }
   }
   // tail (n % 4 samples), handled by the first threads of block 0
@@ -476,10 +501,10 @@ int map2tod_t(void *dat, const void *map, const int32_t *ipix, int64_t n, int64_
   const int B = 256;
   if (vec) {
     if (do_add)
-      k_map2tod_vec<T, true><<<mk_grid_fit(k_map2tod_vec<T, true>, n >> 2, B), B, 0, st>>>(
+      k_map2tod_vec<T, true><<<mk_grid_fit(k_map2tod_vec<T, true>, ((n >> 2) + MU - 1) / MU, B), B, 0, st>>>(
           (T *)dat, (const T *)map, ipix, n, npix);
     else
-      k_map2tod_vec<T, false><<<mk_grid_fit(k_map2tod_vec<T, false>, n >> 2, B), B, 0, st>>>(
+      k_map2tod_vec<T, false><<<mk_grid_fit(k_map2tod_vec<T, false>, ((n >> 2) + MU - 1) / MU, B), B, 0, st>>>(
           (T *)dat, (const T *)map, ipix, n, npix);
   } else {
     if (do_add)

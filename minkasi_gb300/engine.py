@@ -97,6 +97,7 @@ class MapmakingOperator:
                                                                              workspace=self.ws))
                       for s in shapes}
         self.dct_engines = {s: p.engine for s, p in self.plans.items()}
+        self.dct_splits = {s: p.split for s, p in self.plans.items()}
         if self.rot_mode == 0:
             from .autotune import choose_rot_mode
             self.rot_mode = choose_rot_mode(self)

@@ -8,7 +8,7 @@ error, and so is a missing library.
 from __future__ import annotations
 
 import ctypes
-from typing import Optional
+from typing import Optional, Tuple
 
 import torch
 
@@ -389,6 +389,16 @@ def set_dct_engine(engine: int) -> None:
     check(lib().mk_set_dct_engine(int(engine)), "set_dct_engine")
 
 
+def set_fft4_split(rank: int) -> None:
+    """Four-step split for plans created afterwards: 0 = L1 x L2 closest to
+    sqrt(L), r = the r-th next closest divisor pair (mk_set_fft4_split)."""
+    check(lib().mk_set_fft4_split(int(rank)), "set_fft4_split")
+
+
+def fft4_split() -> int:
+    return int(lib().mk_get_fft4_split())
+
+
 def dct_engine() -> int:
     return int(lib().mk_get_dct_engine())
 
@@ -472,6 +482,13 @@ class NoisePlan:
     def engine(self) -> int:
         """0: four-step FFT, 2: four-step FFT through Bluestein, 1: cuFFT."""
         return int(lib().mk_noise_engine(self._h))
+
+    @property
+    def split(self) -> Tuple[int, int]:
+        """The four-step split L1 x L2 of this plan's transform ((0, 0) for cuFFT)."""
+        a, b = ctypes.c_int(0), ctypes.c_int(0)
+        check(lib().mk_noise_split(self._h, ctypes.byref(a), ctypes.byref(b)), "noise split")
+        return int(a.value), int(b.value)
 
     def rotate(self, A: torch.Tensor, X: torch.Tensor, out: Optional[torch.Tensor] = None,
                rot_mode: int = 0) -> torch.Tensor:

@@ -7,7 +7,12 @@ exercise (projections, NoiseSmoothedSVD, TodVec.dot, make_hits, run_pcg,
 fft_r2r, truncate_tod): the WCS/FITS classes raise if called, and the scipy
 DCT backend of ``minkasi/tools/py_fft.py`` is what the transform resolves to.
 ``libminkasi.so`` is the reference's own C, compiled from its source by
-``make -C oracle ref``.
+``make -C oracle ref REF_ROOT=<the reference checkout>``.
+
+The reference checkout is named by the environment variable
+MINKASI_REF_ROOT (the directory that holds ``minkasi/``); there is no
+default, so running the fixture script states where the reference is:
+``MINKASI_REF_ROOT=<checkout> python tests/golden/make_golden.py``.
 
 This module is only used by ``make_golden.py``; nothing under tests/ that runs
 on a GPU machine imports it.
@@ -17,7 +22,9 @@ import os
 import sys
 import types
 
-REF_ROOT = os.environ.get("MINKASI_REF_ROOT", "/root/reference")
+REF_ROOT = os.environ.get("MINKASI_REF_ROOT")
+if not REF_ROOT:
+    raise RuntimeError("set MINKASI_REF_ROOT to the reference checkout (the directory holding minkasi/)")
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 

@@ -48,9 +48,10 @@ def _smooth(x):
 
 def test_dct_plan_selection_needs_no_gpu():
     """Which transform an FP32 DCT plan uses, decided on the host: the
-    four-step split of 2(n-1) when it factors into 2..11, Bluestein's
-    smooth M >= 4(n-1) - 1 otherwise, cuFFT beyond 1536 x 1536 or when
-    selected."""
+    four-step split of 2(n-1) when it factors into 2..11, otherwise
+    Bluestein's smallest splittable smooth M >= 3(n-1) (only outputs
+    0..n-1 are kept and the even extension is symmetric, so the lags span
+    3(n-1) values), cuFFT beyond 1536 x 1536 or when selected."""
     from minkasi_gb300 import kernels as K
     assert K.dct_engine() == 0
     d = K.dct_describe(130978)                 # 2 * 3^5 * 7^2 * 11
@@ -59,7 +60,10 @@ def test_dct_plan_selection_needs_no_gpu():
     assert K.dct_describe(2) == {"engine": 0, "L": 2, "L1": 2, "L2": 1}
     for n in (38, 1000, 465551, 144278):         # 2(n-1) has 37, 37, 9311, 72139
         d = K.dct_describe(n)
-        assert d["engine"] == 2 and _smooth(d["L"]) and d["L"] >= 4 * (n - 1) - 1
+        assert d["engine"] == 2 and _smooth(d["L"]) and d["L"] >= 3 * (n - 1)
+        # and the smallest such length with a split into two parts <= 1536
+        assert not any(_smooth(M) and any(M % a == 0 and M // a <= 1536 for a in range(2, 1537))
+                       for M in range(3 * (n - 1), d["L"]))
         assert d["L1"] * d["L2"] == d["L"] and max(d["L1"], d["L2"]) <= 1536
     assert K.dct_describe(10 ** 7)["engine"] == 1
     try:
@@ -80,11 +84,17 @@ def test_dct_engine_choice_host_logic(monkeypatch):
     from minkasi_gb300 import kernels as K
     from minkasi_gb300.autotune import choose_dct_engines, with_dct_engine
     shapes = [(16, 3529), (32, 4097)]
-    assert choose_dct_engines(SimpleNamespace(dtype=torch.float64), shapes) == {s: 0 for s in shapes}
+    assert choose_dct_engines(SimpleNamespace(dtype=torch.float64), shapes) == {s: (0, 0) for s in shapes}
     monkeypatch.setenv("MINKASI_GB300_DCT", "1")
-    assert choose_dct_engines(SimpleNamespace(dtype=torch.float32), shapes) == {s: 1 for s in shapes}
+    assert choose_dct_engines(SimpleNamespace(dtype=torch.float32), shapes) == {s: (1, 0) for s in shapes}
     assert with_dct_engine(2, lambda: K.dct_describe(465551)["engine"]) == 1
     assert K.dct_engine() == 0
+    # a split rank selects another L1 x L2 of the same length, and is restored
+    d0 = K.dct_describe(130978)
+    d1 = with_dct_engine((0, 1), lambda: K.dct_describe(130978))
+    assert d0["L"] == d1["L"] and d0["L1"] * d0["L2"] == d1["L1"] * d1["L2"] == d0["L"]
+    assert (d0["L1"], d0["L2"]) != (d1["L1"], d1["L2"])
+    assert K.fft4_split() == 0
 
     def boom():
         assert K.dct_engine() == 1
