@@ -462,9 +462,17 @@ int mk_learned_precon_apply(void *z, const void *r, const void *dsq, int H, int 
  * a symmetric M.  Wherever u vanishes within `half` pixels of the map edge
  * this equals mk_learned_precon_apply; nearer the edge it zero-pads once
  * instead of after every layer (still SPD for C = the impulse response of
- * K^T K).  z, r, dsq are dtype-typed maps; z must not alias r. */
+ * K^T K).  z, r, dsq are dtype-typed maps; z must not alias r.
+ * pool > 1 applies the network on a coarser grid (the multi-scale form):
+ *   z = dsq * (u + P^T C * P u)
+ * with P the pool x pool block mean (pixels outside the map count as 0) and
+ * P^T its transpose; the footprint is then pool (2 half + 1) pixels.  It
+ * needs `work` of mk_learned_precon_stencil_work_bytes(H, W, pool) bytes
+ * (two coarse maps); pool == 1 needs none. */
+size_t mk_learned_precon_stencil_work_bytes(int H, int W, int pool);
 int mk_learned_precon_stencil(void *z, const void *r, const void *dsq, int H, int W, int half,
-                              const float *kern, int dtype, void *stream);
+                              const float *kern, int pool, void *work, size_t work_bytes, int dtype,
+                              void *stream);
 
 #ifdef __cplusplus
 }

@@ -94,7 +94,8 @@ SIGNATURES = {
     "mk_get_fft4_split": (_i32, []),
     "mk_learned_precon_work_bytes": (_sz, [_i32, _i32, _i32, _vp]),
     "mk_learned_precon_apply": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _vp, _vp, _sz, _i32, _vp]),
-    "mk_learned_precon_stencil": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _i32, _vp]),
+    "mk_learned_precon_stencil": (_i32, [_vp, _vp, _vp, _i32, _i32, _i32, _vp, _i32, _vp, _sz, _i32, _vp]),
+    "mk_learned_precon_stencil_work_bytes": (_sz, [_i32, _i32, _i32]),
 }
 
 _lib: Optional[ctypes.CDLL] = None

@@ -327,7 +327,9 @@ int precon_apply(TT *z, const TT *r, const TT *dsq, int H, int W, int nl, const 
 // of a stencil row in registers and C read as warp-wide broadcasts.
 constexpr int ST_TX = 32, ST_TY = 32, ST_THREADS = 256, ST_MAXHALF = 8;
 
-template <int HALF, typename TT>
+// PLAIN: the coarse-grid form of the pooled preconditioner, u = r and
+// z = C * u (no D^-1/2, no identity term); dsq is unused.
+template <int HALF, typename TT, bool PLAIN = false>
 __global__ void __launch_bounds__(ST_THREADS)
     k_precon_stencil(const TT *__restrict__ r, const TT *__restrict__ dsq, const float *__restrict__ kern,
                      TT *__restrict__ z, int H, int W) {
@@ -342,7 +344,7 @@ __global__ void __launch_bounds__(ST_THREADS)
     float v = 0.f;
     if (yy >= 0 && yy < H && xx >= 0 && xx < W) {
       const int64_t g = (int64_t)yy * W + xx;
-      v = (float)mul_rn(dsq[g], r[g]);
+      v = PLAIN ? (float)r[g] : (float)mul_rn(dsq[g], r[g]);
     }
     su[sy * PITCH + sx] = v;
   }
@@ -370,46 +372,124 @@ __global__ void __launch_bounds__(ST_THREADS)
     const int xx = x0 + tx + o;
     if (xx < W) {
       const int64_t g = (int64_t)yy * W + xx;
-      const TT u = mul_rn(dsq[g], r[g]);
-      z[g] = mul_rn(dsq[g], add_rn(u, (TT)acc[o]));
+      if (PLAIN) {
+        z[g] = (TT)acc[o];
+      } else {
+        const TT u = mul_rn(dsq[g], r[g]);
+        z[g] = mul_rn(dsq[g], add_rn(u, (TT)acc[o]));
+      }
     }
   }
 }
 
-template <int HALF, typename TT>
+template <int HALF, typename TT, bool PLAIN = false>
 int stencil_launch(TT *z, const TT *r, const TT *dsq, const float *kern, int H, int W, cudaStream_t st) {
   const dim3 grid((W + ST_TX - 1) / ST_TX, (H + ST_TY - 1) / ST_TY);
-  k_precon_stencil<HALF, TT><<<grid, ST_THREADS, 0, st>>>(r, dsq, kern, z, H, W);
+  k_precon_stencil<HALF, TT, PLAIN><<<grid, ST_THREADS, 0, st>>>(r, dsq, kern, z, H, W);
   return mk::launch_status("mk_learned_precon_stencil");
 }
 
-template <typename TT>
+template <typename TT, bool PLAIN = false>
 int stencil_dispatch(TT *z, const TT *r, const TT *dsq, const float *kern, int H, int W, int half,
                      cudaStream_t st) {
   switch (half) {
-    case 0: return stencil_launch<0, TT>(z, r, dsq, kern, H, W, st);
-    case 1: return stencil_launch<1, TT>(z, r, dsq, kern, H, W, st);
-    case 2: return stencil_launch<2, TT>(z, r, dsq, kern, H, W, st);
-    case 3: return stencil_launch<3, TT>(z, r, dsq, kern, H, W, st);
-    case 4: return stencil_launch<4, TT>(z, r, dsq, kern, H, W, st);
-    case 5: return stencil_launch<5, TT>(z, r, dsq, kern, H, W, st);
-    case 6: return stencil_launch<6, TT>(z, r, dsq, kern, H, W, st);
-    case 7: return stencil_launch<7, TT>(z, r, dsq, kern, H, W, st);
-    default: return stencil_launch<8, TT>(z, r, dsq, kern, H, W, st);
+    case 0: return stencil_launch<0, TT, PLAIN>(z, r, dsq, kern, H, W, st);
+    case 1: return stencil_launch<1, TT, PLAIN>(z, r, dsq, kern, H, W, st);
+    case 2: return stencil_launch<2, TT, PLAIN>(z, r, dsq, kern, H, W, st);
+    case 3: return stencil_launch<3, TT, PLAIN>(z, r, dsq, kern, H, W, st);
+    case 4: return stencil_launch<4, TT, PLAIN>(z, r, dsq, kern, H, W, st);
+    case 5: return stencil_launch<5, TT, PLAIN>(z, r, dsq, kern, H, W, st);
+    case 6: return stencil_launch<6, TT, PLAIN>(z, r, dsq, kern, H, W, st);
+    case 7: return stencil_launch<7, TT, PLAIN>(z, r, dsq, kern, H, W, st);
+    default: return stencil_launch<8, TT, PLAIN>(z, r, dsq, kern, H, W, st);
   }
+}
+
+// ---- the pooled (multi-scale) form ------------------------------------------
+//   M r = dsq * (u + P^T C * P u),  u = dsq * r,
+// P the b x b block mean onto an Hc x Wc grid (Hc = ceil(H / b); pixels
+// outside the map count as 0) and P^T its transpose (each fine pixel gets its
+// block's value / b^2).  The network then acts at b times the pixel scale,
+// so its footprint is b (4n + 1) fine pixels; M stays symmetric positive
+// definite.  Three launches: pool, the plain stencil on the coarse grid,
+// and the unpool with the identity term and both D^-1/2 scalings.
+template <typename TT>
+__global__ void __launch_bounds__(256) k_pool(const TT *__restrict__ r, const TT *__restrict__ dsq,
+                                              float *__restrict__ uc, int H, int W, int b, int Hc, int Wc) {
+  const int64_t n = (int64_t)Hc * Wc;
+  const float inv = 1.0f / (float)(b * b);
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+    const int I = (int)(c / Wc), J = (int)(c - (int64_t)I * Wc);
+    float acc = 0.f;
+    for (int di = 0; di < b; di++) {
+      const int i = I * b + di;
+      if (i >= H) break;
+      for (int dj = 0; dj < b; dj++) {
+        const int j = J * b + dj;
+        if (j >= W) break;
+        const int64_t g = (int64_t)i * W + j;
+        acc += (float)mul_rn(dsq[g], r[g]);
+      }
+    }
+    uc[c] = acc * inv;
+  }
+}
+
+template <typename TT>
+__global__ void __launch_bounds__(256) k_unpool(const TT *__restrict__ r, const TT *__restrict__ dsq,
+                                                const float *__restrict__ wc, TT *__restrict__ z, int H, int W,
+                                                int b, int Wc) {
+  const int64_t n = (int64_t)H * W;
+  const float inv = 1.0f / (float)(b * b);
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(g / W), j = (int)(g - (int64_t)i * W);
+    const TT u = mul_rn(dsq[g], r[g]);
+    const TT w = (TT)(wc[(int64_t)(i / b) * Wc + j / b] * inv);
+    z[g] = mul_rn(dsq[g], add_rn(u, w));
+  }
+}
+
+template <typename TT>
+int pooled_apply(TT *z, const TT *r, const TT *dsq, const float *kern, int H, int W, int half, int b,
+                 float *work, cudaStream_t st) {
+  const int Hc = (H + b - 1) / b, Wc = (W + b - 1) / b;
+  float *uc = work, *wc = work + (size_t)Hc * Wc;
+  k_pool<TT><<<mk_grid((int64_t)Hc * Wc, 256, 8), 256, 0, st>>>(r, dsq, uc, H, W, b, Hc, Wc);
+  int rc = mk::launch_status("mk_learned_precon_stencil/pool");
+  if (!rc) rc = stencil_dispatch<float, true>(wc, uc, nullptr, kern, Hc, Wc, half, st);
+  if (rc) return rc;
+  k_unpool<TT><<<mk_grid((int64_t)H * W, 256, 8), 256, 0, st>>>(r, dsq, wc, z, H, W, b, Wc);
+  return mk::launch_status("mk_learned_precon_stencil/unpool");
 }
 
 }  // namespace
 
+extern "C" size_t mk_learned_precon_stencil_work_bytes(int H, int W, int pool) {
+  if (H <= 0 || W <= 0 || pool <= 1) return 0;
+  const size_t hc = (size_t)(H + pool - 1) / pool, wc = (size_t)(W + pool - 1) / pool;
+  return 2 * hc * wc * sizeof(float);
+}
+
 extern "C" int mk_learned_precon_stencil(void *z, const void *r, const void *dsq, int H, int W, int half,
-                                         const float *kern, int dtype, void *stream) {
+                                         const float *kern, int pool, void *work, size_t work_bytes, int dtype,
+                                         void *stream) {
   MK_CHECK_ARG(MK_DTYPE_OK(dtype), "mk_learned_precon_stencil: bad dtype %d", dtype);
   MK_CHECK_ARG(H > 0 && W > 0, "mk_learned_precon_stencil: bad map shape %d x %d", H, W);
   MK_CHECK_ARG(half >= 0 && half <= ST_MAXHALF, "mk_learned_precon_stencil: half-width %d outside 0..%d", half,
                ST_MAXHALF);
+  MK_CHECK_ARG(pool >= 1 && pool <= 64, "mk_learned_precon_stencil: pool factor %d outside 1..64", pool);
   MK_CHECK_ARG(z && r && dsq && kern, "mk_learned_precon_stencil: null pointer");
   MK_CHECK_ARG(z != r, "mk_learned_precon_stencil: z must not alias r (the halo reads neighbours of r)");
+  MK_CHECK_ARG(pool == 1 || (work && work_bytes >= mk_learned_precon_stencil_work_bytes(H, W, pool)),
+               "mk_learned_precon_stencil: work too small for pool %d (%zu bytes)", pool, work_bytes);
   cudaStream_t st = mk::as_stream(stream);
+  if (pool > 1) {
+    if (dtype == MK_F64)
+      return pooled_apply<double>((double *)z, (const double *)r, (const double *)dsq, kern, H, W, half, pool,
+                                  (float *)work, st);
+    return pooled_apply<float>((float *)z, (const float *)r, (const float *)dsq, kern, H, W, half, pool,
+                               (float *)work, st);
+  }
   if (dtype == MK_F64)
     return stencil_dispatch<double>((double *)z, (const double *)r, (const double *)dsq, kern, H, W, half, st);
   return stencil_dispatch<float>((float *)z, (const float *)r, (const float *)dsq, kern, H, W, half, st);

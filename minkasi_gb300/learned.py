@@ -77,19 +77,22 @@ def conv_wgrad(x: torch.Tensor, h: torch.Tensor) -> torch.Tensor:
 
 # ---------------------------------------------------------------- the network
 class ConvNet:
-    """K = L_n ... L_1 with 3x3 kernels; weights[l] has shape (Cout, Cin, 3, 3)."""
+    """K = L_n ... L_1 with 3x3 kernels; weights[l] has shape (Cout, Cin, 3, 3).
+    ``pool`` = b > 1 applies K on the b x b block mean of the map (the
+    multi-scale form, P^T K^T K P), which widens its footprint b times."""
 
-    def __init__(self, weights: Sequence[torch.Tensor]):
+    def __init__(self, weights: Sequence[torch.Tensor], pool: int = 1):
         self.weights = [w.contiguous().float() for w in weights]
+        self.pool = int(pool)
 
     @classmethod
-    def init(cls, channels=CHANNELS, scale: float = 0.05, seed: int = 0, device=None):
+    def init(cls, channels=CHANNELS, scale: float = 0.05, seed: int = 0, device=None, pool: int = 1):
         g = torch.Generator().manual_seed(seed)
         ws = []
         for cin, cout in zip(channels[:-1], channels[1:]):
             w = torch.randn((cout, cin, 3, 3), generator=g) * (scale / math.sqrt(cin * 9))
             ws.append(w.to(device or torch.device("cuda", torch.cuda.current_device())))
-        return cls(ws)
+        return cls(ws, pool)
 
     def forward(self, u: torch.Tensor) -> List[torch.Tensor]:
         acts = [u]
@@ -129,13 +132,35 @@ class ConvNet:
         return grads
 
     def state(self) -> dict:
-        return {f"w{i}": w.detach().cpu().numpy() for i, w in enumerate(self.weights)}
+        st = {f"w{i}": w.detach().cpu().numpy() for i, w in enumerate(self.weights)}
+        st["pool"] = np.int64(self.pool)
+        return st
 
     @classmethod
     def from_state(cls, st: dict, device=None):
         ws = [torch.from_numpy(np.asarray(st[f"w{i}"], np.float32)).to(device or "cuda")
               for i in range(len([k for k in st if k.startswith("w")]))]
-        return cls(ws)
+        return cls(ws, int(st["pool"]) if "pool" in st else 1)
+
+
+def pool_maps(x: torch.Tensor, b: int) -> torch.Tensor:
+    """P: the b x b block mean of [B, C, H, W] maps, pixels outside the map
+    counting as 0 (the same P as the CUDA apply)."""
+    if b == 1:
+        return x
+    B, C, H, W = x.shape
+    Hc, Wc = -(-H // b), -(-W // b)
+    xp = torch.nn.functional.pad(x, (0, Wc * b - W, 0, Hc * b - H))
+    return xp.view(B, C, Hc, b, Wc, b).sum(dim=(3, 5)) / float(b * b)
+
+
+def unpool_maps(y: torch.Tensor, b: int, H: int, W: int) -> torch.Tensor:
+    """P^T: each fine pixel gets its block's coarse value / b^2."""
+    if b == 1:
+        return y
+    B, C, Hc, Wc = y.shape
+    up = (y / float(b * b))[:, :, :, None, :, None].expand(B, C, Hc, b, Wc, b).reshape(B, C, Hc * b, Wc * b)
+    return up[:, :, :H, :W].contiguous()
 
 
 # ---------------------------------------------------------------- the preconditioner
@@ -172,13 +197,18 @@ class LearnedPrecon:
         self.dsq32 = dsq.float().contiguous()
         self.net = net
         self.shape = tuple(shape)
+        self.pool = net.pool
         ws = net.weights
         self.half = 2 * len(ws)
         self.stencil = bool(stencil) and self.half <= 8
+        if self.pool > 1 and not self.stencil:
+            raise ValueError("a pooled network is applied as a stencil (at most 4 layers)")
         self.kern = impulse_response(net) if self.stencil else None
         self._ch = (ctypes.c_int * (len(ws) + 1))(int(ws[0].shape[1]), *[int(w.shape[0]) for w in ws])
-        nb = 0 if self.stencil else int(lib().mk_learned_precon_work_bytes(self.shape[0], self.shape[1],
-                                                                           len(ws), self._ch))
+        if self.stencil:
+            nb = int(lib().mk_learned_precon_stencil_work_bytes(self.shape[0], self.shape[1], self.pool))
+        else:
+            nb = int(lib().mk_learned_precon_work_bytes(self.shape[0], self.shape[1], len(ws), self._ch))
         self._work = torch.empty(max((nb + 3) // 4, 1), dtype=torch.float32, device=hits.device)
 
     def apply(self, r: torch.Tensor, z: torch.Tensor) -> torch.Tensor:
@@ -191,7 +221,8 @@ class LearnedPrecon:
             if z.data_ptr() == r.data_ptr():
                 raise ValueError("LearnedPrecon.apply: z must not alias r")
             check(lib().mk_learned_precon_stencil(_p(z), _p(r), _p(dsq), self.shape[0], self.shape[1],
-                                                  self.half, _p(self.kern), K.dtype_code(z), _stream()),
+                                                  self.half, _p(self.kern), self.pool, _p(self._work),
+                                                  self._work.numel() * 4, K.dtype_code(z), _stream()),
                   "learned_precon_stencil")
             return z
         ws = self.net.weights
@@ -365,8 +396,10 @@ def loss_and_grad(net: ConvNet, dsq: torch.Tensor, mask: torch.Tensor, R: torch.
     gradient is the partial derivative at that c."""
     B = R.shape[0]
     nhit = float(mask.sum())
+    b = net.pool
     u = (R * dsq[None, :])
-    kk = net.ktk(u.view(B, 1, *shape).contiguous()).reshape(B, -1)
+    uc = pool_maps(u.view(B, 1, *shape), b).contiguous()
+    kk = unpool_maps(net.ktk(uc), b, *shape).reshape(B, -1)
     mr = dsq[None, :] * (u + kk)
     pe = _project(E, mask, nhit)
     a = _project(mr, mask, nhit)
@@ -378,8 +411,9 @@ def loss_and_grad(net: ConvNet, dsq: torch.Tensor, mask: torch.Tensor, R: torch.
         return loss, None
     # dL/d(mr) = 2 c P res / den / B ; mr = dsq*(u + z) -> dL/dz = dsq * dL/dmr
     gmr = 2.0 * c[:, None] * _project(res, mask, nhit) / den[:, None] / B
-    gz = (dsq[None, :] * gmr).view(B, 1, *shape).contiguous()
-    return loss, net.grad(u.view(B, 1, *shape).contiguous(), gz)
+    gz = (dsq[None, :] * gmr).view(B, 1, *shape)
+    # kk = P^T K^T K P u  ->  dL/dw = grad of K^T K at P u against P gz
+    return loss, net.grad(uc, pool_maps(gz, b).contiguous())
 
 
 def train(net: ConvNet, hits: torch.Tensor, shape, R: torch.Tensor, E: torch.Tensor,
@@ -449,9 +483,12 @@ def train_recipe(config: str, out: Optional[str] = None, device=None, log=print)
     c1 (1 TOD, 256^2 map): 2500 pairs (r_k, x* - x_k) from FP64 Jacobi solves
     to 1e-10 on seeded skies (seeds 1000, 1001, ...), 2500 white pairs, Adam
     for 30 epochs, batch 64.
-    c4 (200 TODs, 2048^2 map): each pair costs an FP32 operator application
-    of 8.8e9 samples, so 2 known-solution skies (seeds 1000, 1001; every 3rd
-    of 240 PCG iterates) and 64 white pairs, 12 epochs, batch 4.
+    c4 (200 TODs, 2048^2 map at 0.5"): the network acts on the 8 x 8 block
+    mean of the map (pool 8): the 1/f noise there correlates pixels over
+    ~100 pixels along the scan, far beyond the 17-pixel footprint of K^T K on
+    the fine grid.  Each pair costs an FP32 operator application of 8.8e9
+    samples, so 3 known-solution skies (seeds 1000-1002; every 3rd of 300
+    PCG iterates) and 96 white pairs, 20 epochs, batch 8.
     Returns a record of the run (pair counts, times, losses)."""
     import time
     from .pcg import MixedOp
@@ -470,11 +507,12 @@ def train_recipe(config: str, out: Optional[str] = None, device=None, log=print)
     op64 = tv.engine(m, torch.float64)
     op32 = tv.engine(m, torch.float32)
     t1 = time.perf_counter()
+    pool = 1
     if config == "c4":
-        R, E = known_solution_pairs(MixedOp(op32, m.npix, dev), m, hits, [1000, 1001], cfg.pixsize_arcsec,
-                                    n_iter=240, every=3)
-        rw, ew = white_pairs(op32, hits, 64)
-        epochs, batch = 12, 4
+        R, E = known_solution_pairs(MixedOp(op32, m.npix, dev), m, hits, [1000, 1001, 1002],
+                                    cfg.pixsize_arcsec, n_iter=300, every=3)
+        rw, ew = white_pairs(op32, hits, 96)
+        epochs, batch, pool = 20, 8, 8
     else:
         R, E, seed = [], [], 1000
         while sum(r.shape[0] for r in R) < 2500:
@@ -489,13 +527,13 @@ def train_recipe(config: str, out: Optional[str] = None, device=None, log=print)
     del rw, ew
     torch.cuda.synchronize()
     t2 = time.perf_counter()
-    net = ConvNet.init(seed=0, device=dev)
+    net = ConvNet.init(seed=0, device=dev, pool=pool)
     hist = train(net, hits, (m.nx, m.ny), R, E, epochs=epochs, batch=batch)
     torch.cuda.synchronize()
     t3 = time.perf_counter()
     os.makedirs(os.path.dirname(out), exist_ok=True)
     save(net, out)
-    rec = {"config": config, "pairs": int(R.shape[0]), "epochs": epochs, "batch": batch,
+    rec = {"config": config, "pool": pool, "pairs": int(R.shape[0]), "epochs": epochs, "batch": batch,
            "setup_s": t1 - t0, "pair_gen_s": t2 - t1, "train_s": t3 - t2,
            "loss_first": hist[0], "loss_last": hist[-1], "out": out}
     log(rec)

@@ -164,3 +164,66 @@ def test_stencil_apply_equals_layered_inside_the_edge(L, shape, dtype):
     assert float(a64 @ Ma) > 0
     with pytest.raises(ValueError):
         S.apply(a64, a64)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_pooled_stencil_apply(L, dtype):
+    """The multi-scale form z = D^-1/2 (u + P^T C * P u) with P the 8 x 8
+    block mean: against the same operator built from pool_maps, the layered
+    K^T K on the coarse grid and unpool_maps (hit pixels 64 fine pixels from
+    the edge, so 8 coarse pixels: the layered and stencil forms agree), and
+    symmetric positive definite."""
+    rng = np.random.default_rng(11)
+    shape, b = (256, 200), 8
+    n = shape[0] * shape[1]
+    hits_np = rng.integers(0, 5, size=shape).astype(np.float64)
+    hits_np[:64], hits_np[-64:], hits_np[:, :64], hits_np[:, -64:] = 0, 0, 0, 0
+    hits = torch.from_numpy(hits_np.ravel()).to(cuda)
+    net = L.ConvNet.init(seed=5, scale=0.4, device=cuda, pool=b)
+    S = L.LearnedPrecon(hits, net, shape)
+    r = torch.from_numpy(rng.standard_normal(n)).to(cuda, dtype)
+    z = torch.empty_like(r)
+    S.apply(r, z)
+    dsq = S.dsq64 if dtype == torch.float64 else S.dsq32
+    u = dsq * r
+    uc = L.pool_maps(u.float().view(1, 1, *shape), b).contiguous()
+    want = dsq * (u + L.unpool_maps(net.ktk(uc), b, *shape).reshape(-1).to(dtype))
+    assert rel(z.double().cpu().numpy(), want.double().cpu().numpy()) < 1e-5
+    a64, b64 = r.double(), torch.from_numpy(rng.standard_normal(n)).to(cuda)
+    Ma, Mb = torch.empty_like(a64), torch.empty_like(b64)
+    S.apply(a64, Ma)
+    S.apply(b64, Mb)
+    assert abs(float(b64 @ Ma) - float(a64 @ Mb)) < 1e-5 * float((a64.abs() * b64.abs()).sum())
+    assert float(a64 @ Ma) > 0
+    with pytest.raises(ValueError):
+        L.LearnedPrecon(hits, net, shape, stencil=False)
+
+
+def test_pooled_training_gradient_directional(L):
+    """The pooled loss gradient (P applied to the incoming gradient, then the
+    network's own backward kernels) against a central finite difference of
+    the loss along a random direction of the weights."""
+    rng = np.random.default_rng(12)
+    shape, b, B = (48, 40), 4, 3
+    n = shape[0] * shape[1]
+    hits = torch.from_numpy(rng.integers(0, 6, size=n).astype(np.float32)).to(cuda)
+    mask = (hits > 0).float()
+    dsq = torch.where(hits > 0, 1 / torch.sqrt(hits.clamp(min=1)), torch.zeros_like(hits))
+    R = torch.from_numpy(rng.standard_normal((B, n)).astype(np.float32)).to(cuda)
+    E = torch.from_numpy(rng.standard_normal((B, n)).astype(np.float32)).to(cuda)
+    net = L.ConvNet.init(seed=6, scale=0.6, device=cuda, pool=b)
+    loss, grads = L.loss_and_grad(net, dsq, mask, R, E, shape)
+    dirs = [torch.from_numpy(rng.standard_normal(tuple(w.shape)).astype(np.float32)).to(cuda)
+            for w in net.weights]
+    ana = float(sum((g * d).sum() for g, d in zip(grads, dirs)))
+    h = 1e-3
+    base = [w.clone() for w in net.weights]
+    vals = []
+    for sgn in (1, -1):
+        for w, w0, d in zip(net.weights, base, dirs):
+            w.copy_(w0 + sgn * h * d)
+        vals.append(L.loss_and_grad(net, dsq, mask, R, E, shape, need_grad=False)[0])
+    for w, w0 in zip(net.weights, base):
+        w.copy_(w0)
+    num = (vals[0] - vals[1]) / (2 * h)
+    assert abs(num - ana) < 2e-2 * max(abs(ana), 1e-6), (num, ana)
