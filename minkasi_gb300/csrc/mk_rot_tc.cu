@@ -24,6 +24,8 @@
 // copies.  Every mbarrier wait is bounded: on timeout the CTA records an
 // error code, waits (bounded) for its outstanding MMAs, frees its tensor
 // memory and returns.
+#include <cstdlib>
+
 #include "mk_async.cuh"
 #include "mk_common.cuh"
 #include "mk_rot.cuh"
@@ -290,6 +292,198 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
 }
 
+// ---- warp-specialised version ---------------------------------------------
+// The same tiles, products and operand images, with the roles split so that
+// no CTA-wide barrier sits in the main loop:
+//   warps 0-3 (split): thread t owns sample row t of every tile; it splits its
+//     32 values of a K-chunk into hi / lo and writes them into the chunk's
+//     A stage, then arrives on full_a[stage];
+//   warp 4, lane 0 (MMA): bulk-copies the chunk's B image into the stage
+//     (full_b[stage]), waits for both halves, issues the 12 MMAs and commits
+//     them to mma_done[stage] (which frees the stage for chunk g + 2); after
+//     a tile's last chunk it commits to acc_full[buffer];
+//   warps 5-8 (epilogue): tensor memory holds two accumulators (2 x ndet
+//     columns), so while the MMAs of tile i + 1 run, these warps read tile i
+//     (warp w reads TMEM lanes 32 (w % 4) ..) and store it, then arrive on
+//     acc_empty[buffer].
+// Every wait is bounded and also polls the CTA's abort flag, so a timeout in
+// one role ends all of them; the MMA thread then drains its outstanding
+// MMAs (bounded) before the tensor memory is freed.
+constexpr int WS_SPLIT = 4, WS_EPI = 4;
+constexpr int WS_THREADS = (WS_SPLIT + 1 + WS_EPI) * 32;
+
+__device__ __forceinline__ bool ws_wait(uint64_t *bar, uint32_t parity, volatile int *abort_flag) {
+  for (uint32_t i = 0; i < mk::SPIN_LIMIT; i++) {
+    if (mk::mbar_try_wait(bar, parity)) return true;
+    if ((i & 31u) == 31u && *abort_flag) return false;
+  }
+  *abort_flag = 1;
+  return false;
+}
+
+__global__ void __launch_bounds__(WS_THREADS, 1)
+    k_rot_tc_ws(const float *__restrict__ X, int64_t ldx, float *__restrict__ R, int64_t ldr, int ndet,
+                int64_t ncol, const char *__restrict__ bimg, int *__restrict__ err, int64_t mirror_n,
+                int64_t xs, int halve_ends) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const uint32_t a_bytes = TILE_M * 128;
+  const uint32_t b_bytes = (uint32_t)ndet * 128;
+  const uint32_t stage_bytes = 2 * a_bytes + 2 * b_bytes;
+  float *raw = (float *)(smem + NSTAGE * stage_bytes);
+  __shared__ uint64_t full_a[NSTAGE], full_b[NSTAGE], mma_done[NSTAGE], acc_full[2], acc_empty[2];
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ int abort_sh;
+  volatile int *abort_flag = &abort_sh;
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nchunk = ndet / KC;
+  const uint32_t ncols = 2u * (ndet < 32 ? 32u : (uint32_t)ndet);  // two accumulators, a power of two
+  const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(ndet >> 3) << 17) |
+                         ((uint32_t)(TILE_M >> 4) << 24);
+  if (tid == 0) {
+    for (int s = 0; s < NSTAGE; s++) {
+      mbar_init(&full_a[s], WS_SPLIT * 32);
+      mbar_init(&full_b[s], 1);
+      mbar_init(&mma_done[s], 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      mbar_init(&acc_full[b], 1);
+      mbar_init(&acc_empty[b], WS_EPI * 32);
+    }
+    abort_sh = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base_sh)),
+                 "r"(ncols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = tmem_base_sh;
+  const int64_t ntile = (ncol + TILE_M - 1) / TILE_M;
+  uint32_t g_issued = 0;  // MMA thread: chunks whose MMAs were committed
+
+  if (warp < WS_SPLIT) {
+    // ---- split role ----
+    for (uint32_t q = 0; q < (uint32_t)RSTAGE; q++) prefetch_chunk(X, ldx, xs, ncol, nchunk, ntile, q, raw, tid);
+    uint32_t g = 0;
+    for (int64_t tile = blockIdx.x; tile < ntile && !*abort_flag; tile += gridDim.x) {
+      const int64_t my = tile * TILE_M + tid;
+      const float hscale = (halve_ends && (my == 0 || my == ncol - 1)) ? 0.5f : 1.0f;
+      for (int c = 0; c < nchunk; c++, g++) {
+        const uint32_t s = g % NSTAGE, use = g / NSTAGE;
+        float h[KC], l[KC];
+        cp_async_wait<RSTAGE - 1>();
+        const float *rw = raw + (size_t)(g % RSTAGE) * KC * TILE_M + tid;
+#pragma unroll
+        for (int kk = 0; kk < KC; kk++) {
+          const float x = rw[kk * TILE_M] * hscale;
+          h[kk] = tf32_round(x);
+          l[kk] = tf32_round(x - h[kk]);
+        }
+        prefetch_chunk(X, ldx, xs, ncol, nchunk, ntile, g + RSTAGE, raw, tid);
+        if (g >= NSTAGE && !ws_wait(&mma_done[s], (use - 1) & 1, abort_flag)) break;
+        unsigned char *ah = smem + s * stage_bytes, *al = ah + a_bytes;
+#pragma unroll
+        for (int q = 0; q < KC / 4; q++) {
+          const uint32_t off = sw128_off(tid, 4 * q);
+          *(float4 *)(ah + off) = make_float4(h[4 * q], h[4 * q + 1], h[4 * q + 2], h[4 * q + 3]);
+          *(float4 *)(al + off) = make_float4(l[4 * q], l[4 * q + 1], l[4 * q + 2], l[4 * q + 3]);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mk::mbar_arrive(&full_a[s]);
+      }
+    }
+    cp_async_wait<0>();  // no copy into this CTA's shared memory outlives it
+  } else if (warp == WS_SPLIT) {
+    // ---- MMA role (one thread) ----
+    if (lane == 0) {
+      uint32_t g = 0;
+      int64_t it = 0;
+      for (int64_t tile = blockIdx.x; tile < ntile && !*abort_flag; tile += gridDim.x, it++) {
+        const uint32_t ab = (uint32_t)(it & 1), au = (uint32_t)(it >> 1);
+        if (it >= 2 && !ws_wait(&acc_empty[ab], (au - 1) & 1, abort_flag)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        const uint32_t dacc = tmem + ab * (ncols / 2);
+        bool ok = true;
+        for (int c = 0; c < nchunk; c++, g++) {
+          const uint32_t s = g % NSTAGE, use = g / NSTAGE;
+          unsigned char *st = smem + s * stage_bytes;
+          if (g >= NSTAGE && !ws_wait(&mma_done[s], (use - 1) & 1, abort_flag)) {
+            ok = false;
+            break;
+          }
+          mbar_expect_tx(&full_b[s], 2 * b_bytes);
+          bulk_g2s(st + 2 * a_bytes, bimg + (size_t)c * 2 * b_bytes, 2 * b_bytes, &full_b[s]);
+          if (!ws_wait(&full_b[s], use & 1, abort_flag) || !ws_wait(&full_a[s], use & 1, abort_flag)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;");
+          const uint32_t sa_h = smem_u32(st), sa_l = sa_h + a_bytes;
+          const uint32_t sb_h = smem_u32(st + 2 * a_bytes), sb_l = sb_h + b_bytes;
+#pragma unroll
+          for (int k8 = 0; k8 < KC / 8; k8++) {
+            const uint32_t ko = k8 * 32;
+            const uint32_t acc0 = (c == 0 && k8 == 0) ? 0u : 1u;
+            mma_tf32(dacc, sdesc(sa_h + ko), sdesc(sb_h + ko), idesc, acc0);
+            mma_tf32(dacc, sdesc(sa_l + ko), sdesc(sb_h + ko), idesc, 1u);
+            mma_tf32(dacc, sdesc(sa_h + ko), sdesc(sb_l + ko), idesc, 1u);
+          }
+          mma_commit(&mma_done[s]);
+          g_issued = g + 1;
+        }
+        if (!ok) break;
+        mma_commit(&acc_full[ab]);
+      }
+    }
+  } else {
+    // ---- epilogue role ----
+    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    const int row = 32 * q + lane;
+    int64_t it = 0;
+    for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x, it++) {
+      const uint32_t ab = (uint32_t)(it & 1), au = (uint32_t)(it >> 1);
+      // every lane waits; the warp goes on only if all of them saw the
+      // phase complete (tcgen05.ld below needs the whole warp converged)
+      const bool okw = ws_wait(&acc_full[ab], au & 1, abort_flag);
+      if (!__all_sync(0xffffffffu, okw)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      const int64_t my = tile * TILE_M + row;
+      const uint32_t base = tmem + ((uint32_t)(32 * q) << 16) + ab * (ncols / 2);
+      for (int c0 = 0; c0 < ndet; c0 += 32) {
+        float v[32];
+        tmem_ld32(base + (uint32_t)c0, v);
+        if (my < ncol) {
+#pragma unroll
+          for (int j = 0; j < 32; j++) __stcs(R + (int64_t)(c0 + j) * ldr + my, v[j]);
+          if (mirror_n > 0 && my >= 1 && my <= ncol - 2) {
+#pragma unroll
+            for (int j = 0; j < 32; j++) __stcs(R + (int64_t)(c0 + j) * ldr + (mirror_n - my), v[j]);
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      mk::mbar_arrive(&acc_empty[ab]);
+    }
+  }
+  __syncthreads();
+  if (*abort_flag && tid == WS_SPLIT * 32) {
+    atomicExch(err, 1);
+    // bounded drain of the MMAs this thread issued before freeing tensor memory
+    for (uint32_t g = (g_issued > NSTAGE ? g_issued - NSTAGE : 0); g < g_issued; g++)
+      (void)mbar_wait(&mma_done[g % NSTAGE], (g / NSTAGE) & 1);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+}
+
 }  // namespace
 
 namespace mk {
@@ -321,10 +515,29 @@ int rot_tc_f32(const float *A, const float *X, int64_t ldx, float *R, int64_t ld
     MK_CUDA(cudaFuncSetAttribute(k_rot_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr_set[dev] = (int)smem;
   }
+  int64_t ntile = (ncol + TILE_M - 1) / TILE_M;
+  // the warp-specialised kernel by default; MINKASI_GB300_ROT_TC_V1=1 keeps
+  // the single-role kernel (for comparisons)
+  static const bool v1 = [] {
+    const char *e = getenv("MINKASI_GB300_ROT_TC_V1");
+    return e && e[0] == '1';
+  }();
+  if (!v1) {
+    static int attr_ws[64] = {0};
+    if (dev >= 0 && dev < 64 && attr_ws[dev] < (int)smem) {
+      MK_CUDA(cudaFuncSetAttribute(k_rot_tc_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      attr_ws[dev] = (int)smem;
+    }
+    // one CTA per SM: its two accumulators take up to all 512 TMEM columns
+    int64_t grid = (int64_t)sm_count();
+    if (grid > ntile) grid = ntile;
+    k_rot_tc_ws<<<(unsigned)grid, WS_THREADS, smem, st>>>(X, ldx, R, ldr, nd, ncol, (const char *)bimg, err,
+                                                          mirror_n, x_stride, halve_ends);
+    return launch_status("rot_tc_f32");
+  }
   int per_sm = (int)(220 * 1024 / smem);
   if (per_sm < 1) per_sm = 1;
   if (per_sm > 2) per_sm = 2;  // tensor memory: <= 2 x 256 columns per SM
-  int64_t ntile = (ncol + TILE_M - 1) / TILE_M;
   int64_t grid = (int64_t)sm_count() * per_sm;
   if (grid > ntile) grid = ntile;
   k_rot_tc<<<(unsigned)grid, NTHREADS, smem, st>>>(X, ldx, R, ldr, nd, ncol, (const char *)bimg, err,

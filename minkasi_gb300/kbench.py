@@ -1,10 +1,12 @@
 """Kernel micro-benchmarks on one synthetic TOD shape (CUDA events, best of N).
 
     python -m minkasi_gb300.kbench [--config c2s] [--only tod2map,map2tod,rot,noise,dct,conv,point,pol]
+                                   [--shape NDET,NDATA]
 
 Uses the first TOD shape and daisy pointing of a synthetic configuration
-(default c2s: 256 detectors x 130978 samples onto a 1024x1024 map) with
-random data, and reports per kernel the time and, for the projections, the
+(default c2s: 256 detectors x 130978 samples onto a 1024x1024 map; --shape
+overrides the TOD shape, e.g. 256,144278 for a length whose transform runs
+Bluestein's algorithm) with random data, and reports per kernel the time and, for the projections, the
 algorithmic GB/s (4 B pixel index + one sample per sample; the map is
 L2-resident).  Rotations report their relative error against cuBLAS on the
 FP64 / FP32 units and their TF/s counted as 2 ndet^2 ndata flops
@@ -38,10 +40,10 @@ def best_ms(fn, reps: int = 5, warm: int = 2) -> float:
     return best
 
 
-def run(config: str = "c2s", only=None) -> dict:
+def run(config: str = "c2s", only=None, shape=None) -> dict:
     dev = torch.device("cuda", torch.cuda.current_device())
     cfg = CONFIGS[config]
-    ndet, n = tod_shapes(cfg)[0]
+    ndet, n = shape if shape else tod_shapes(cfg)[0]
     info = make_tod_info(cfg, 0, ndet, n, dev, with_data=False)
     ipix = info["ipix"]
     npix = cfg.nx * cfg.ny
@@ -205,5 +207,7 @@ if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--config", default="c2s")
     ap.add_argument("--only", default="")
+    ap.add_argument("--shape", default="", help="NDET,NDATA instead of the configuration's first TOD")
     a = ap.parse_args()
-    print(json.dumps(run(a.config, [s for s in a.only.split(",") if s] or None)))
+    shape = tuple(int(v) for v in a.shape.split(",")) if a.shape else None
+    print(json.dumps(run(a.config, [s for s in a.only.split(",") if s] or None, shape)))

@@ -3,7 +3,8 @@
 The reference has no scan simulator; its configurations are described by
 their shapes and physics, which this module turns into data:
 
-* pointing: a daisy scan r = R sin(w1 t), theta = w2 t around a scan centre,
+* pointing: a daisy scan r = R sin(w1 t), theta = w2 t around a scan centre
+  (or, for the sparse variant, raster sweeps along a few fixed rows),
   detectors on a square grid at ``det_pitch`` arcsec, flat-sky CAR pixels
   (ipix = x * ny + y, int32, the reference's layout);
 * signal: a beta-model cluster amp (1 + r^2/theta_c^2)^(0.5 - 1.5 beta) at
@@ -55,6 +56,11 @@ class SynthConfig:
     gain_scatter: float = 0.02
     truncate: bool = True
     seed: int = 0
+    # "daisy", or "raster": constant-declination sweeps x = L sin(w1 t) along
+    # one of `tracks` fixed rows spread over +-centre_spread (every TOD
+    # retraces one of them), so the hit pixels are a few narrow bands
+    scan: str = "daisy"
+    tracks: int = 0
 
 
 CONFIGS = {
@@ -69,6 +75,12 @@ CONFIGS = {
     "c4": SynthConfig(name="c4", ntod=200, ndet_choices=(32, 64, 128, 256),
                       nsamp_range=(50000, 600000), nx=2048, ny=2048, pixsize_arcsec=0.5,
                       scan_radius_arcmin=1.5, centre_spread_arcmin=4.5),
+    # c4 with sparse hits: raster sweeps that retrace 3 narrow tracks, so
+    # about 5% of the pixels inside the scan footprint are hit
+    "c4sparse": SynthConfig(name="c4sparse", ntod=200, ndet_choices=(32, 64, 128, 256),
+                            nsamp_range=(50000, 600000), nx=2048, ny=2048, pixsize_arcsec=0.5,
+                            scan_radius_arcmin=6.0, centre_spread_arcmin=6.0, det_pitch_arcsec=5.0,
+                            scan="raster", tracks=3),
     # a small case of c2 for profiler captures: 4 TODs x 256 x 2^17 (1.6 GB of inputs)
     "c2s": SynthConfig(name="c2s", ntod=4, ndet_choices=(256,), nsamp_range=(1 << 17, 1 << 17),
                        nx=1024, ny=1024, pixsize_arcsec=1.0),
@@ -123,17 +135,25 @@ def make_tod_info(cfg: SynthConfig, k: int, ndet: int, ndata: int, device,
     w1 = 2 * math.pi / cfg.petal_period_s
     w2 = w1 / 1.6180339887
     ph1, ph2 = rng.uniform(0, 2 * math.pi, size=2)
-    r = R * torch.sin(w1 * t + ph1)
-    th = w2 * t + ph2
-    if cfg.centre_spread_arcmin > 0:
-        rr = cfg.centre_spread_arcmin * 60.0 * math.sqrt(rng.uniform())
-        aa = rng.uniform(0, 2 * math.pi)
-        cx, cy = rr * math.cos(aa), rr * math.sin(aa)
-    else:
-        cx = cy = 0.0
     off = torch.from_numpy(det_offsets(ndet, cfg.det_pitch_arcsec)).to(device)
-    x = (cx + r * torch.cos(th))[None, :] + off[:, :1]      # arcsec from map centre
-    y = (cy + r * torch.sin(th))[None, :] + off[:, 1:]
+    if cfg.scan == "raster":
+        # sweep along x over +-R; the row is one of `tracks` fixed rows
+        track = int(rng.integers(0, max(cfg.tracks, 1)))
+        spread = cfg.centre_spread_arcmin * 60.0
+        cy = -spread + 2 * spread * (track + 0.5) / max(cfg.tracks, 1)
+        x = (R * torch.sin(w1 * t + ph1))[None, :] + off[:, :1]
+        y = torch.full_like(t, cy)[None, :] + off[:, 1:]
+    else:
+        r = R * torch.sin(w1 * t + ph1)
+        th = w2 * t + ph2
+        if cfg.centre_spread_arcmin > 0:
+            rr = cfg.centre_spread_arcmin * 60.0 * math.sqrt(rng.uniform())
+            aa = rng.uniform(0, 2 * math.pi)
+            cx, cy = rr * math.cos(aa), rr * math.sin(aa)
+        else:
+            cx = cy = 0.0
+        x = (cx + r * torch.cos(th))[None, :] + off[:, :1]      # arcsec from map centre
+        y = (cy + r * torch.sin(th))[None, :] + off[:, 1:]
     px = torch.round(x / cfg.pixsize_arcsec + cfg.nx / 2).clamp(0, cfg.nx - 1)
     py = torch.round(y / cfg.pixsize_arcsec + cfg.ny / 2).clamp(0, cfg.ny - 1)
     ipix = (px * cfg.ny + py).to(torch.int32).contiguous()
