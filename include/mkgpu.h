@@ -370,6 +370,28 @@ int mk_rotate(mk_noise_plan *plan, const void *A, const void *X, void *R, int ro
  * and clears the word; synchronises `stream`. */
 int mk_noise_status(mk_noise_plan *plan, int *code, void *stream);
 
+/* NoiseSmoothedSVD.apply_noise of many TODs in one call, in place on each
+ * TOD's (ndet, ndata) float32 timestream data[t] (the batched operator's
+ * pooled buffer): the v and vT detector rotations of all TODs with the same
+ * detector count run as one tensor-core launch each (3xTF32, as rot_mode 2),
+ * and each TOD's two DCT-I run on its plan (plans[t]: FP32, four-step FFT,
+ * ndet in {32, 64, 128, 256}).  Same arithmetic as mk_apply_noise with
+ * rot_mode 2 on each TOD, bit for bit.  The group keeps the rotation
+ * operand images of v and vT (built at creation: 8 ndet^2 bytes each) and
+ * the device job tables; the data pointers, v, vT and mywt must stay valid
+ * and unchanged while it is used.  Plans that share a workspace must have
+ * their calls ordered on one stream.  mk_noise_group_status reports (and
+ * clears) a timed-out wait inside the rotation kernel.  Replaces the
+ * per-TOD loop of minkasi/tods/core.py:517-580 (Tod.apply_noise) inside
+ * TodVec.dot (core.py:967-1026). */
+typedef struct mk_noise_group mk_noise_group;
+int mk_noise_group_create(mk_noise_group **group, int ntod, mk_noise_plan *const *plans,
+                          const float *const *v, const float *const *vT, const float *const *mywt,
+                          const int64_t *ldw, float *const *data, void *stream);
+int mk_noise_group_exec(mk_noise_group *group, void *stream);
+int mk_noise_group_status(mk_noise_group *group, int *code, void *stream);
+int mk_noise_group_destroy(mk_noise_group *group);
+
 /* ---- map-space vector algebra and the PCG recurrence ------------------- */
 
 /* *result (DEVICE double) = sum_i a[i]*b[i], accumulated in FP64 with a

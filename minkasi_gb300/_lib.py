@@ -89,6 +89,10 @@ SIGNATURES = {
     "mk_dct1_describe": (_i32, [_i64, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int64),
                                 ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "mk_noise_engine": (_i32, [_vp]),
+    "mk_noise_group_create": (_i32, [_vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "mk_noise_group_exec": (_i32, [_vp, _vp]),
+    "mk_noise_group_status": (_i32, [_vp, ctypes.POINTER(ctypes.c_int), _vp]),
+    "mk_noise_group_destroy": (_i32, [_vp]),
     "mk_noise_split": (_i32, [_vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "mk_set_fft4_split": (_i32, [_i32]),
     "mk_get_fft4_split": (_i32, []),

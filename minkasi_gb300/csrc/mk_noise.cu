@@ -36,6 +36,7 @@
 #include <atomic>
 #include <mutex>
 #include <new>
+#include <vector>
 
 #include "mk_common.cuh"
 #include "mk_fft4.cuh"
@@ -527,6 +528,149 @@ extern "C" int mk_noise_status(mk_noise_plan *plan, int *code, void *stream) {
   cudaStream_t st = mk::as_stream(stream);
   MK_CUDA(cudaMemcpyAsync(code, plan->core.tc_err, sizeof(int), cudaMemcpyDeviceToHost, st));
   MK_CUDA(cudaMemsetAsync(plan->core.tc_err, 0, sizeof(int), st));
+  MK_CUDA(cudaStreamSynchronize(st));
+  return MK_OK;
+}
+
+// ---- many TODs, one filter call ---------------------------------------------
+// apply_noise in place on every TOD of a group: the v and vT rotations of all
+// TODs with the same detector count run as one tensor-core launch each (the
+// rotation works in place: a tile's inputs are all read before its outputs
+// are written), and each TOD's two DCT-I passes run on its own plan.  The
+// rotation operand images are built once, when the group is created.
+struct mk_noise_group {
+  struct Tod {
+    DctCore *core;
+    const float *w;
+    int64_t ldw;
+    float *data;
+  };
+  struct Class {  // the TODs with one detector count
+    int64_t ndet = 0, ntile = 0;
+    int njobs = 0;
+    mk::RotJob *jobs_v = nullptr, *jobs_vT = nullptr;  // device tables
+  };
+  std::vector<Tod> tods;
+  std::vector<Class> classes;
+  void *mem = nullptr;  // operand images, job tables, status word
+  int *err = nullptr;
+};
+
+extern "C" int mk_noise_group_destroy(mk_noise_group *g) {
+  if (!g) return MK_OK;
+  cudaFree(g->mem);
+  delete g;
+  return MK_OK;
+}
+
+extern "C" int mk_noise_group_create(mk_noise_group **group, int ntod, mk_noise_plan *const *plans,
+                                     const float *const *v, const float *const *vT, const float *const *mywt,
+                                     const int64_t *ldw, float *const *data, void *stream) {
+  MK_CHECK_ARG(group, "mk_noise_group_create: null group pointer");
+  *group = nullptr;
+  MK_CHECK_ARG(ntod >= 1 && plans && v && vT && mywt && ldw && data, "mk_noise_group_create: bad arguments");
+  for (int t = 0; t < ntod; t++) {
+    MK_CHECK_ARG(plans[t] && v[t] && vT[t] && mywt[t] && data[t], "mk_noise_group_create: TOD %d: null pointer",
+                 t);
+    const DctCore &c = plans[t]->core;
+    MK_CHECK_ARG(c.own && c.dtype == MK_F32 && mk::rot_tc_supported(c.nrow),
+                 "mk_noise_group_create: TOD %d: needs an FP32 four-step plan with ndet in {32,64,128,256}", t);
+    MK_CHECK_ARG(ldw[t] >= c.n, "mk_noise_group_create: TOD %d: ldw below ndata", t);
+  }
+  mk_noise_group *g = new (std::nothrow) mk_noise_group;
+  MK_CHECK_ARG(g, "mk_noise_group_create: out of host memory");
+  std::vector<int64_t> nds;
+  for (int t = 0; t < ntod; t++) {
+    const int64_t nd = plans[t]->core.nrow;
+    bool seen = false;
+    for (int64_t x : nds) seen |= (x == nd);
+    if (!seen) nds.push_back(nd);
+  }
+  // one allocation: per TOD two operand images, per class two job tables, the status word
+  size_t bytes = 256, img_total = 0;
+  for (int t = 0; t < ntod; t++) img_total += 2 * align_up(mk::rot_tc_bimg_bytes(plans[t]->core.nrow));
+  bytes += img_total + 2 * nds.size() * align_up((size_t)ntod * sizeof(mk::RotJob));
+  if (cudaMalloc(&g->mem, bytes) != cudaSuccess) {
+    delete g;
+    mk::set_error("mk_noise_group_create: cudaMalloc of %zu bytes failed", bytes);
+    return MK_ERR_CUDA;
+  }
+  cudaStream_t st = mk::as_stream(stream);
+  char *p = (char *)g->mem;
+  g->err = (int *)p;
+  int rc = cudaMemsetAsync(g->err, 0, sizeof(int), st) == cudaSuccess ? MK_OK : MK_ERR_CUDA;
+  p += 256;
+  std::vector<const char *> img_v(ntod), img_vT(ntod);
+  for (int t = 0; t < ntod && !rc; t++) {
+    const DctCore &c = plans[t]->core;
+    const size_t ib = align_up(mk::rot_tc_bimg_bytes(c.nrow));
+    img_v[t] = p;
+    rc = mk::rot_tc_bprep(v[t], c.nrow, p, st);
+    p += ib;
+    img_vT[t] = p;
+    if (!rc) rc = mk::rot_tc_bprep(vT[t], c.nrow, p, st);
+    p += ib;
+    g->tods.push_back({&plans[t]->core, mywt[t], ldw[t], data[t]});
+  }
+  for (size_t k = 0; k < nds.size() && !rc; k++) {
+    mk_noise_group::Class cl;
+    cl.ndet = nds[k];
+    std::vector<mk::RotJob> jv, jvT;
+    for (int t = 0; t < ntod; t++) {
+      const DctCore &c = plans[t]->core;
+      if (c.nrow != cl.ndet) continue;
+      const int64_t tiles = (c.n + 127) / 128;
+      jv.push_back({data[t], data[t], img_v[t], c.n, c.n, c.n, cl.ntile});
+      jvT.push_back({data[t], data[t], img_vT[t], c.n, c.n, c.n, cl.ntile});
+      cl.ntile += tiles;
+    }
+    cl.njobs = (int)jv.size();
+    const size_t tb = align_up((size_t)ntod * sizeof(mk::RotJob));
+    cl.jobs_v = (mk::RotJob *)p;
+    p += tb;
+    cl.jobs_vT = (mk::RotJob *)p;
+    p += tb;
+    if (cudaMemcpyAsync(cl.jobs_v, jv.data(), jv.size() * sizeof(mk::RotJob), cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(cl.jobs_vT, jvT.data(), jvT.size() * sizeof(mk::RotJob), cudaMemcpyHostToDevice, st) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+      mk::set_error("mk_noise_group_create: uploading the job tables failed");
+      rc = MK_ERR_CUDA;
+    }
+    g->classes.push_back(cl);
+  }
+  if (rc) {
+    mk_noise_group_destroy(g);
+    return rc;
+  }
+  *group = g;
+  return MK_OK;
+}
+
+extern "C" int mk_noise_group_exec(mk_noise_group *g, void *stream) {
+  MK_CHECK_ARG(g, "mk_noise_group_exec: null group");
+  cudaStream_t st = mk::as_stream(stream);
+  int rc;
+  for (const auto &cl : g->classes)
+    if ((rc = mk::rot_tc_group(cl.jobs_v, cl.njobs, cl.ntile, cl.ndet, g->err, st))) return rc;
+  for (const auto &t : g->tods) {
+    DctCore *c = t.core;
+    if ((rc = mk::fft4_dct(c->f4, t.data, c->n, c->nrow, c->T, t.data, c->n, mk::FFT4_FILTER, t.w, t.ldw, st)))
+      return rc;
+    if ((rc = mk::fft4_dct(c->f4, t.data, c->n, c->nrow, c->T, t.data, c->n, mk::FFT4_HALVE, nullptr, 0, st)))
+      return rc;
+  }
+  for (const auto &cl : g->classes)
+    if ((rc = mk::rot_tc_group(cl.jobs_vT, cl.njobs, cl.ntile, cl.ndet, g->err, st))) return rc;
+  return MK_OK;
+}
+
+extern "C" int mk_noise_group_status(mk_noise_group *g, int *code, void *stream) {
+  MK_CHECK_ARG(g && code, "mk_noise_group_status: null pointer");
+  cudaStream_t st = mk::as_stream(stream);
+  MK_CUDA(cudaMemcpyAsync(code, g->err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  MK_CUDA(cudaMemsetAsync(g->err, 0, sizeof(int), st));
   MK_CUDA(cudaStreamSynchronize(st));
   return MK_OK;
 }

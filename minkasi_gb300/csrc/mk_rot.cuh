@@ -20,4 +20,19 @@ size_t rot_tc_bimg_bytes(int64_t nrow);
 int rot_tc_f32(const float *A, const float *X, int64_t ldx, float *R, int64_t ldr, int64_t nrow,
                int64_t ncol, void *bimg, int *err, cudaStream_t st, int64_t mirror_n = 0,
                int64_t x_stride = 1, int halve_ends = 0);
+
+// One TOD of a grouped rotation: R = A . X with A given by its operand image
+// bimg (rot_tc_bprep); tile0 = the first of its ceil(ncol / 128) tiles in the
+// launch (jobs sorted by tile0, contiguous).  R may equal X (in place): the
+// kernel reads all of a tile's inputs before it writes that tile.
+struct RotJob {
+  const float *X;
+  float *R;
+  const char *bimg;
+  int64_t ldx, ldr, ncol, tile0;
+};
+// the operand image of A (rot_tc_bimg_bytes(nrow) bytes)
+int rot_tc_bprep(const float *A, int64_t nrow, void *bimg, cudaStream_t st);
+// every job of the (device) table in one launch; all jobs have nrow detectors
+int rot_tc_group(const RotJob *jobs_dev, int njobs, int64_t ntile, int64_t nrow, int *err, cudaStream_t st);
 }  // namespace mk

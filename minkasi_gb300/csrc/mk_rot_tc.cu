@@ -321,10 +321,39 @@ __device__ __forceinline__ bool ws_wait(uint64_t *bar, uint32_t parity, volatile
   return false;
 }
 
+// The job (TOD) that owns tile t of the launch; jobs are sorted by tile0 and
+// each role walks its tiles in increasing order, so the cursor only moves on.
+__device__ __forceinline__ int job_at(const mk::RotJob *jobs, int njobs, int64_t t, int cur) {
+  while (cur + 1 < njobs && jobs[cur + 1].tile0 <= t) cur++;
+  return cur;
+}
+
+// queue the copy of chunk q of this CTA (tile blockIdx.x + (q / nchunk) *
+// gridDim.x, K-chunk q % nchunk) into raw slot q % RSTAGE; always commits one
+// group so that group counting stays uniform
+__device__ __forceinline__ void prefetch_job(const mk::RotJob *jobs, int njobs, int &pcur, int64_t xs, int nchunk,
+                                             int64_t ntile, uint32_t q, float *raw, int tid) {
+  const int64_t tile = blockIdx.x + (int64_t)(q / nchunk) * gridDim.x;
+  const int c = (int)(q % nchunk);
+  if (tile < ntile) {
+    pcur = job_at(jobs, njobs, tile, pcur);
+    const mk::RotJob &J = jobs[pcur];
+    const int64_t my = (tile - J.tile0) * TILE_M + tid;
+    const bool ok = my < J.ncol;
+    const float *src = J.X + (int64_t)(c * KC) * J.ldx + (ok ? my : 0) * xs;
+    float *dst = raw + (size_t)(q % RSTAGE) * KC * TILE_M + tid;
+#pragma unroll
+    for (int kk = 0; kk < KC; kk++) cp_async4(dst + kk * TILE_M, src + (int64_t)kk * J.ldx, ok);
+  }
+  cp_async_commit();
+}
+
+// `jobs` (device memory, sorted by tile0) lists the TODs of a grouped launch,
+// all with ndet detectors; for one TOD it is null and `j0` is that TOD.
+// mirror_n, xs and halve_ends apply to single-TOD launches (0, 1, 0 in groups).
 __global__ void __launch_bounds__(WS_THREADS, 1)
-    k_rot_tc_ws(const float *__restrict__ X, int64_t ldx, float *__restrict__ R, int64_t ldr, int ndet,
-                int64_t ncol, const char *__restrict__ bimg, int *__restrict__ err, int64_t mirror_n,
-                int64_t xs, int halve_ends) {
+    k_rot_tc_ws(const mk::RotJob *__restrict__ jobs_in, int njobs, const mk::RotJob j0, int64_t ntile, int ndet,
+                int *__restrict__ err, int64_t mirror_n, int64_t xs, int halve_ends) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *smem = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const uint32_t a_bytes = TILE_M * 128;
@@ -335,6 +364,8 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
   __shared__ uint32_t tmem_base_sh;
   __shared__ int abort_sh;
   volatile int *abort_flag = &abort_sh;
+  const mk::RotJob *jobs = jobs_in ? jobs_in : &j0;
+  if (!jobs_in) njobs = 1;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nchunk = ndet / KC;
@@ -364,15 +395,16 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = tmem_base_sh;
-  const int64_t ntile = (ncol + TILE_M - 1) / TILE_M;
   uint32_t g_issued = 0;  // MMA thread: chunks whose MMAs were committed
 
   if (warp < WS_SPLIT) {
     // ---- split role ----
-    for (uint32_t q = 0; q < (uint32_t)RSTAGE; q++) prefetch_chunk(X, ldx, xs, ncol, nchunk, ntile, q, raw, tid);
+    int pcur = 0, cur = 0;
+    for (uint32_t q = 0; q < (uint32_t)RSTAGE; q++) prefetch_job(jobs, njobs, pcur, xs, nchunk, ntile, q, raw, tid);
     uint32_t g = 0;
     for (int64_t tile = blockIdx.x; tile < ntile && !*abort_flag; tile += gridDim.x) {
-      const int64_t my = tile * TILE_M + tid;
+      cur = job_at(jobs, njobs, tile, cur);
+      const int64_t my = (tile - jobs[cur].tile0) * TILE_M + tid, ncol = jobs[cur].ncol;
       const float hscale = (halve_ends && (my == 0 || my == ncol - 1)) ? 0.5f : 1.0f;
       for (int c = 0; c < nchunk; c++, g++) {
         const uint32_t s = g % NSTAGE, use = g / NSTAGE;
@@ -385,7 +417,7 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
           h[kk] = tf32_round(x);
           l[kk] = tf32_round(x - h[kk]);
         }
-        prefetch_chunk(X, ldx, xs, ncol, nchunk, ntile, g + RSTAGE, raw, tid);
+        prefetch_job(jobs, njobs, pcur, xs, nchunk, ntile, g + RSTAGE, raw, tid);
         if (g >= NSTAGE && !ws_wait(&mma_done[s], (use - 1) & 1, abort_flag)) break;
         unsigned char *ah = smem + s * stage_bytes, *al = ah + a_bytes;
 #pragma unroll
@@ -404,7 +436,10 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
     if (lane == 0) {
       uint32_t g = 0;
       int64_t it = 0;
+      int cur = 0;
       for (int64_t tile = blockIdx.x; tile < ntile && !*abort_flag; tile += gridDim.x, it++) {
+        cur = job_at(jobs, njobs, tile, cur);
+        const char *bimg = jobs[cur].bimg;
         const uint32_t ab = (uint32_t)(it & 1), au = (uint32_t)(it >> 1);
         if (it >= 2 && !ws_wait(&acc_empty[ab], (au - 1) & 1, abort_flag)) break;
         asm volatile("tcgen05.fence::after_thread_sync;");
@@ -446,14 +481,18 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
     const int q = warp & 3;  // TMEM lane quarter this warp may access
     const int row = 32 * q + lane;
     int64_t it = 0;
+    int cur = 0;
     for (int64_t tile = blockIdx.x; tile < ntile; tile += gridDim.x, it++) {
+      cur = job_at(jobs, njobs, tile, cur);
       const uint32_t ab = (uint32_t)(it & 1), au = (uint32_t)(it >> 1);
       // every lane waits; the warp goes on only if all of them saw the
       // phase complete (tcgen05.ld below needs the whole warp converged)
       const bool okw = ws_wait(&acc_full[ab], au & 1, abort_flag);
       if (!__all_sync(0xffffffffu, okw)) break;
       asm volatile("tcgen05.fence::after_thread_sync;");
-      const int64_t my = tile * TILE_M + row;
+      const mk::RotJob &J = jobs[cur];
+      const int64_t my = (tile - J.tile0) * TILE_M + row, ncol = J.ncol, ldr = J.ldr;
+      float *R = J.R;
       const uint32_t base = tmem + ((uint32_t)(32 * q) << 16) + ab * (ncols / 2);
       for (int c0 = 0; c0 < ndet; c0 += 32) {
         float v[32];
@@ -482,6 +521,22 @@ __global__ void __launch_bounds__(WS_THREADS, 1)
   __syncthreads();
   if (warp == 0)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(ncols));
+}
+
+size_t ws_smem_bytes(int nd) {
+  const size_t stage = 2 * (size_t)TILE_M * 128 + 2 * (size_t)nd * 128;
+  return NSTAGE * stage + (size_t)RSTAGE * KC * TILE_M * sizeof(float) + 1024;
+}
+
+int ws_prepare(size_t smem) {
+  static int attr_ws[64] = {0};
+  int dev = 0;
+  MK_CUDA(cudaGetDevice(&dev));
+  if (dev >= 0 && dev < 64 && attr_ws[dev] < (int)smem) {
+    MK_CUDA(cudaFuncSetAttribute(k_rot_tc_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_ws[dev] = (int)smem;
+  }
+  return MK_OK;
 }
 
 }  // namespace
@@ -523,16 +578,15 @@ int rot_tc_f32(const float *A, const float *X, int64_t ldx, float *R, int64_t ld
     return e && e[0] == '1';
   }();
   if (!v1) {
-    static int attr_ws[64] = {0};
-    if (dev >= 0 && dev < 64 && attr_ws[dev] < (int)smem) {
-      MK_CUDA(cudaFuncSetAttribute(k_rot_tc_ws, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      attr_ws[dev] = (int)smem;
-    }
+    const size_t wsmem = ws_smem_bytes(nd);
+    int rc = ws_prepare(wsmem);
+    if (rc) return rc;
+    RotJob j0{X, R, (const char *)bimg, ldx, ldr, ncol, 0};
     // one CTA per SM: its two accumulators take up to all 512 TMEM columns
     int64_t grid = (int64_t)sm_count();
     if (grid > ntile) grid = ntile;
-    k_rot_tc_ws<<<(unsigned)grid, WS_THREADS, smem, st>>>(X, ldx, R, ldr, nd, ncol, (const char *)bimg, err,
-                                                          mirror_n, x_stride, halve_ends);
+    k_rot_tc_ws<<<(unsigned)grid, WS_THREADS, wsmem, st>>>(nullptr, 1, j0, ntile, nd, err, mirror_n, x_stride,
+                                                           halve_ends);
     return launch_status("rot_tc_f32");
   }
   int per_sm = (int)(220 * 1024 / smem);
@@ -543,6 +597,35 @@ int rot_tc_f32(const float *A, const float *X, int64_t ldx, float *R, int64_t ld
   k_rot_tc<<<(unsigned)grid, NTHREADS, smem, st>>>(X, ldx, R, ldr, nd, ncol, (const char *)bimg, err,
                                                    mirror_n, x_stride, halve_ends);
   return launch_status("rot_tc_f32");
+}
+
+}  // namespace mk
+
+namespace mk {
+
+int rot_tc_bprep(const float *A, int64_t nrow, void *bimg, cudaStream_t st) {
+  MK_CHECK_ARG(rot_tc_supported(nrow), "tensor-core rotation supports ndet in {32,64,128,256}, got %lld",
+               (long long)nrow);
+  MK_CHECK_ARG(A && bimg && ((uintptr_t)bimg % 16) == 0, "tensor-core rotation: bad operand image");
+  const int nd = (int)nrow;
+  k_bprep<<<(nd * nd + 255) / 256, 256, 0, st>>>(A, nd, (char *)bimg);
+  return launch_status("rot_tc_bprep");
+}
+
+int rot_tc_group(const RotJob *jobs_dev, int njobs, int64_t ntile, int64_t nrow, int *err, cudaStream_t st) {
+  MK_CHECK_ARG(rot_tc_supported(nrow), "tensor-core rotation supports ndet in {32,64,128,256}, got %lld",
+               (long long)nrow);
+  MK_CHECK_ARG(jobs_dev && njobs >= 1 && err, "tensor-core rotation group: bad arguments");
+  if (ntile <= 0) return MK_OK;
+  const int nd = (int)nrow;
+  const size_t wsmem = ws_smem_bytes(nd);
+  int rc = ws_prepare(wsmem);
+  if (rc) return rc;
+  int64_t grid = (int64_t)sm_count();
+  if (grid > ntile) grid = ntile;
+  RotJob none{};
+  k_rot_tc_ws<<<(unsigned)grid, WS_THREADS, wsmem, st>>>(jobs_dev, njobs, none, ntile, nd, err, 0, 1, 0);
+  return launch_status("rot_tc_group");
 }
 
 }  // namespace mk

@@ -9,13 +9,17 @@ HBM layout (one operator, S = total samples over all TODs, P = pixels):
           per-shape noise plans (they run in stream order)
   map   : dtype[P], L2-resident during the projections
 So map2tod and tod2map are ONE launch each over all S samples, whatever the
-number and shapes of the TODs; only the noise filter runs per TOD.
+number and shapes of the TODs.  The noise filter's detector rotations are
+one launch per detector count over all TODs (kernels.NoiseGroup, in place on
+tmp); its DCT-I passes run per TOD shape plan, because each TOD's FFT needs
+its own length-dependent tables and scratch.
 
 The reference does the same work TOD by TOD with a fresh (ndet, ndata)
 temporary per call (minkasi/tods/core.py:582-620,649-691,967-1026).
 """
 from __future__ import annotations
 
+import os
 from typing import Dict, List, Optional, Tuple
 
 import numpy as np
@@ -68,6 +72,8 @@ class MapmakingOperator:
         self._hmax: Optional[int] = None
         self._fixed: Optional[K.FixedScratch] = None
         self._pixplans: Optional[List[K.PixPlan]] = None
+        self._group = None
+        self._group_key = None
         self.method = tod2map
         if tod2map == "auto":
             from .autotune import choose_tod2map
@@ -137,8 +143,33 @@ class MapmakingOperator:
         else:
             raise ValueError(f"unknown tod2map method {m!r}")
 
+    def _noise_group(self):
+        """The one-call filter over all TODs (kernels.NoiseGroup) when every
+        TOD runs the FP32 four-step FFT with tensor-core rotations, else
+        None (then the filter runs TOD by TOD)."""
+        if self._group is False:
+            return None
+        key = self.tmp.data_ptr()
+        if self._group is not None and self._group_key == key:
+            return self._group
+        ok = (self.dtype == torch.float32 and self.rot_mode == 2 and
+              all(p.engine in (0, 2) for p in self.plans.values()) and
+              all(nd in (32, 64, 128, 256) for nd, _ in self.dims) and
+              os.environ.get("MINKASI_GB300_GROUP", "1") != "0")
+        if not ok:
+            self._group = False
+            return None
+        views = list(self.views(self.tmp))
+        self._group = K.NoiseGroup([self.plans[d] for d in self.dims], self.ops, views)
+        self._group_key = key
+        return self._group
+
     def noise_all(self) -> None:
         self.prepare_noise()
+        grp = self._noise_group()
+        if grp is not None:
+            grp.apply()
+            return
         for (v, vT, w), view, dims in zip(self.ops, self.views(self.tmp), self.dims):
             self.plans[dims].apply(v, vT, w, view, out=view, rot_mode=self.rot_mode)
 
@@ -162,6 +193,7 @@ class MapmakingOperator:
         return out
 
     def release(self) -> None:
+        self._group = None
         self.tmp = None
         self.ws = None
         self.plans = {}

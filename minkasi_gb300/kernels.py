@@ -536,6 +536,55 @@ class NoisePlan:
             self._h = None
 
 
+class NoiseGroup:
+    """apply_noise in place on many FP32 TODs in one call (mk_noise_group_*):
+    one tensor-core launch per detector count for each of the v and vT
+    rotations, and each TOD's two DCT-I on its own plan.  ``plans[t]``,
+    ``ops[t] = (v, vT, mywt)`` and ``data[t]`` (an (ndet, ndata) float32
+    view) are kept referenced for the life of the group."""
+
+    def __init__(self, plans, ops, data):
+        n = len(plans)
+        if not (n == len(ops) == len(data)) or n == 0:
+            raise ValueError("NoiseGroup: one plan, operand triple and data view per TOD")
+        for p, (v, vT, w), d in zip(plans, ops, data):
+            for t, nm in ((v, "v"), (vT, "vT"), (w, "mywt"), (d, "data")):
+                _dev(t, nm)
+                if t.dtype != torch.float32:
+                    raise TypeError(f"NoiseGroup: {nm} must be float32")
+            if tuple(d.shape) != (p.ndet, p.ndata) or not d.is_contiguous():
+                raise ValueError("NoiseGroup: data must be contiguous (ndet, ndata) views")
+        self._keep = (list(plans), list(ops), list(data))
+        vp = ctypes.c_void_p
+        arr = lambda xs: (vp * n)(*[x for x in xs])
+        h = ctypes.c_void_p()
+        ldw = (ctypes.c_int64 * n)(*[int(w.shape[1]) for _, _, w in ops])
+        check(lib().mk_noise_group_create(ctypes.byref(h), n, arr([p._h.value for p in plans]),
+                                          arr([v.data_ptr() for v, _, _ in ops]),
+                                          arr([vT.data_ptr() for _, vT, _ in ops]),
+                                          arr([w.data_ptr() for _, _, w in ops]), ldw,
+                                          arr([d.data_ptr() for d in data]), _stream()), "noise group")
+        self._h = h
+
+    def apply(self) -> None:
+        check(lib().mk_noise_group_exec(self._h, _stream()), "noise group exec")
+
+    def status(self) -> int:
+        """1 if a tensor-core wait of the group timed out since the last call."""
+        code = ctypes.c_int(0)
+        check(lib().mk_noise_group_status(self._h, ctypes.byref(code), _stream()), "noise group status")
+        return int(code.value)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                lib().mk_noise_group_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+
 # ---------------------------------------------------------------------------
 # map algebra and the PCG recurrence
 # ---------------------------------------------------------------------------

@@ -504,7 +504,9 @@ def train_recipe(config: str, out: Optional[str] = None, device=None, log=print)
     else:
         tv, m = make_todvec(cfg, dev)
     hits = make_hits(tv, m).map.reshape(-1)
-    op64 = tv.engine(m, torch.float64)
+    # the 200-TOD pairs come from the FP32 operator alone: its FP64 twin would
+    # add a 70 GB timestream buffer and 70 GB of FP64 weights
+    op64 = tv.engine(m, torch.float64) if config != "c4" else None
     op32 = tv.engine(m, torch.float32)
     t1 = time.perf_counter()
     pool = 1
@@ -525,6 +527,9 @@ def train_recipe(config: str, out: Optional[str] = None, device=None, log=print)
         epochs, batch = 30, 64
     R, E = torch.cat([R, rw]), torch.cat([E, ew])
     del rw, ew
+    if config == "c4":
+        op32.release()  # the pairs are made; free the timestream buffers before training
+        torch.cuda.empty_cache()
     torch.cuda.synchronize()
     t2 = time.perf_counter()
     net = ConvNet.init(seed=0, device=dev, pool=pool)

@@ -53,3 +53,31 @@ def test_tc_apply_noise_matches_golden(K, gold):
     dd = plan.apply(f(v), f(vT), f(w), f(xx), rot_mode=2).cpu().numpy()
     assert plan.status() == 0
     assert rel(dd[:10], g["dd"]) < 2e-5
+
+
+def test_noise_group_equals_per_tod_filter(monkeypatch):
+    """The one-call filter over all TODs (rotations of all TODs with one
+    detector count in one tensor-core launch, in place) gives bit for bit
+    what the per-TOD apply_noise gives, on TODs of 32 and 64 detectors with
+    untruncated lengths (so some run Bluestein's algorithm)."""
+    from dataclasses import replace
+    from minkasi_gb300 import synth
+    from minkasi_gb300.engine import MapmakingOperator
+    monkeypatch.setenv("MINKASI_GB300_DCT", "0")
+    cfg = replace(synth.CONFIGS["tiny"], ntod=5, ndet_choices=(32, 64), nsamp_range=(3000, 9000),
+                  truncate=False)
+    tv, m = synth.make_todvec(cfg)
+    op = MapmakingOperator(tv, m, torch.float32, tod2map="atomic", rot_mode=2)
+    assert set(op.dct_engines.values()) <= {0, 2} and 2 in op.dct_engines.values()
+    grp = op._noise_group()
+    assert grp is not None
+    g = torch.Generator(device="cuda").manual_seed(3)
+    x = torch.randn(op.tmp.shape, generator=g, dtype=torch.float32, device="cuda")
+    op.tmp.copy_(x)
+    op.noise_all()
+    grouped = op.tmp.clone()
+    assert grp.status() == 0
+    op.tmp.copy_(x)
+    for (v, vT, w), view, dims in zip(op.ops, op.views(op.tmp), op.dims):
+        op.plans[dims].apply(v, vT, w, view, out=view, rot_mode=2)
+    assert torch.equal(grouped, op.tmp)
