@@ -571,13 +571,15 @@ int rot_tc_f32(const float *A, const float *X, int64_t ldx, float *R, int64_t ld
     attr_set[dev] = (int)smem;
   }
   int64_t ntile = (ncol + TILE_M - 1) / TILE_M;
-  // the warp-specialised kernel by default; MINKASI_GB300_ROT_TC_V1=1 keeps
-  // the single-role kernel (for comparisons)
-  static const bool v1 = [] {
-    const char *e = getenv("MINKASI_GB300_ROT_TC_V1");
+  // one TOD: the single-role kernel, measured 10 % faster than the
+  // warp-specialised one on a 256 x 130,978 TOD (both wait on the loads of
+  // X: two 16 KB chunks in flight per SM); MINKASI_GB300_ROT_TC_WS=1 selects
+  // the warp-specialised kernel, which the grouped (many-TOD) launch uses
+  static const bool ws = [] {
+    const char *e = getenv("MINKASI_GB300_ROT_TC_WS");
     return e && e[0] == '1';
   }();
-  if (!v1) {
+  if (ws) {
     const size_t wsmem = ws_smem_bytes(nd);
     int rc = ws_prepare(wsmem);
     if (rc) return rc;

@@ -211,9 +211,13 @@ def test_pooled_training_gradient_directional(L):
     dsq = torch.where(hits > 0, 1 / torch.sqrt(hits.clamp(min=1)), torch.zeros_like(hits))
     R = torch.from_numpy(rng.standard_normal((B, n)).astype(np.float32)).to(cuda)
     E = torch.from_numpy(rng.standard_normal((B, n)).astype(np.float32)).to(cuda)
-    net = L.ConvNet.init(seed=6, scale=0.6, device=cuda, pool=b)
+    # weights with a per-layer gain of about 2 (as in the oracle gradient
+    # test), so that K^T K moves the loss well above FP32 rounding
+    ws = [torch.from_numpy((rng.standard_normal((co, ci, 3, 3)) * 0.2).astype(np.float32)).to(cuda)
+          for ci, co in zip(L.CHANNELS[:-1], L.CHANNELS[1:])]
+    net = L.ConvNet(ws, pool=b)
     loss, grads = L.loss_and_grad(net, dsq, mask, R, E, shape)
-    dirs = [torch.from_numpy(rng.standard_normal(tuple(w.shape)).astype(np.float32)).to(cuda)
+    dirs = [torch.from_numpy((rng.standard_normal(tuple(w.shape)) * 0.2).astype(np.float32)).to(cuda)
             for w in net.weights]
     ana = float(sum((g * d).sum() for g, d in zip(grads, dirs)))
     h = 1e-3
