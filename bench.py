@@ -31,6 +31,8 @@ PCG with the learned preconditioner (weights made by learned.train_recipe),
 on the 1-TOD configuration (all three run to the end) and on the 200-TOD
 configuration (the FP64 Jacobi solve, about two hours there, is its measured
 iteration time times the mixed solve's iteration count, labelled projected).
+The 200-TOD solves run first, in a child process with the whole GPU (they
+peak near 240 GB of HBM).
 
 CPU baselines run in a separate process with no GPU library loaded (this
 script with --impl reference): the reference's tod2map, and its operator per
@@ -79,6 +81,8 @@ def parse():
     ap.add_argument("--cpu-pcg", action="store_true",
                     help="(reference arm) also time the reference CPU operator per PCG iteration")
     ap.add_argument("--method", default=None, help="force the tod2map kernel (atomic|staged|fixed|sorted)")
+    ap.add_argument("--c4-only", action="store_true",
+                    help="(internal) run only the 200-TOD solves and print their record")
     ap.add_argument("--sparse", action="store_true",
                     help="the 200-TOD workload with sparse hits instead: the autotuner's tod2map choice "
                          "and every scatter kernel's GB/s")
@@ -378,10 +382,40 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-def run_ours(args):
-    import torch
+def c4_subprocess(args):
+    """The 200-TOD solves in a fresh process on the whole GPU (they peak near
+    240 GB, so they run before this process allocates anything)."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--c4-only"]
+    env = dict(os.environ)
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
+        env.pop(k, None)
+    try:
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=3000, env=env)
+        lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+        return json.loads(lines[-1]) if lines else {"error": r.stderr[-600:]}
+    except (subprocess.TimeoutExpired, ValueError) as e:
+        return {"error": str(e)}
 
+
+def run_c4_only(args):
+    import torch
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    import minkasi_gb300  # noqa: F401
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        rec = solve_c4(dev)
+        clk.mark(t0, time.perf_counter())
+    rec["clocks"] = clk.summary()
+    print(json.dumps(rec))
+
+
+def run_ours(args):
     rank, world, local = dist_env()
+    c4 = None
+    if world == 1 and not args.no_solver and not args.no_c4:
+        c4 = c4_subprocess(args)
+    import torch
     if world > 1:
         torch.distributed.init_process_group("nccl")
     torch.cuda.set_device(local)
@@ -506,7 +540,7 @@ def run_ours(args):
         clear_plan_cache()
         gc.collect()
         torch.cuda.empty_cache()
-        solver = solver_extras(dev, skip_c4=args.no_c4)
+        solver = solver_extras(dev, c4)
 
     cpu = None
     if rank == 0 and world == 1:
@@ -721,7 +755,7 @@ def solve_c4(dev, tol=1e-6, wall_limit_s=420.0):
     out = {"workload": "c4: 200 TODs, ndet in {32,64,128,256}, nsamp U[5e4,6e5] (truncated), 2048x2048 map "
                        "at 0.5in", "tol": tol, "samples": S, "ntod": tv.ntod,
            "setup_s": time.perf_counter() - t0,
-           "tod2map_kernel_f32": op32.method, "rot_mode_f32": op32.rot_mode,
+           "tod2map_kernel_f32": op32.method, "rot_mode_f32": op32.rot_mode, "rot_mode_f64": op64.rot_mode,
            "dct_engines_f32": sorted(set(int(v) for v in op32.dct_engines.values())),
            "gpu_mem_GB_peak": torch.cuda.max_memory_allocated() / 1e9,
            "learned_weights": os.path.relpath(L.weights_path("c4"), REPO)}
@@ -754,6 +788,7 @@ def solve_c4(dev, tol=1e-6, wall_limit_s=420.0):
     pre_ms = b.copy()
     pre_ms.maps[0].map.copy_(pre.view(m.nx, m.ny))
     ml = L.LearnedPrecon(hits, L.load(L.weights_path("c4"), dev), (m.nx, m.ny))
+    out["learned_pool"] = ml.pool
     budget = None
     for name, kw in (("mixed_jacobi", {}), ("mixed_learned", {"inner_precon": ml})):
         hist = []
@@ -788,17 +823,10 @@ def solve_c4(dev, tol=1e-6, wall_limit_s=420.0):
     return out
 
 
-def solver_extras(dev, skip_c4=False):
-    import gc
-    import torch
-    from minkasi_gb300.noise import clear_plan_cache
-
+def solver_extras(dev, c4=None):
     res = {"c1": solve_c1(dev)}
-    if not skip_c4:
-        clear_plan_cache()
-        gc.collect()
-        torch.cuda.empty_cache()
-        res["c4"] = solve_c4(dev)
+    if c4 is not None:
+        res["c4"] = c4
     return res
 
 
@@ -870,5 +898,7 @@ if __name__ == "__main__":
         run_reference(a)
     elif a.sparse:
         run_sparse(a)
+    elif a.c4_only:
+        run_c4_only(a)
     else:
         run_ours(a)

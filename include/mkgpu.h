@@ -346,7 +346,12 @@ int mk_get_fft4_split(void);
  * detector-rotation GEMM: 0 = automatic, 1 = cuBLAS on the FP64 / FP32 units
  * (DGEMM / SGEMM), 2 = this library's tensor-core kernel (FP32 only: 3xTF32
  * split products, FP32 accumulate), 3 = cuBLAS tensor-core emulation (FP64:
- * fixed-point slices; FP32: BF16x9). */
+ * fixed-point slices; FP32: BF16x9), 4 = FP64 only: this library's exact
+ * slicing of both operands into 8 integer slices of 7 bits after power-of-two
+ * row / column scaling, their products as bf16 tensor-core GEMMs with FP32
+ * accumulation (exact: every sum stays below 2^24), combined in int64 and
+ * rounded to FP64 once (ndet <= 1040; the plan's workspace holds its
+ * scratch, about 1 GB at ndet = 256). */
 typedef struct mk_noise_plan mk_noise_plan;
 int mk_noise_workspace_bytes(int64_t ndet, int64_t ndata, int dtype, size_t *bytes);
 int mk_noise_plan_create(mk_noise_plan **plan, int64_t ndet, int64_t ndata, int dtype,

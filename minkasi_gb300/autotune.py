@@ -106,7 +106,9 @@ def choose_tod2map(op, candidates: Optional[Iterable[str]] = None) -> str:
 
 def choose_rot_mode(op) -> int:
     """Fastest rotation GEMM that agrees with the FP64/FP32 cuBLAS result
-    (rel. 1e-13 in FP64, 1e-6 in FP32) on the largest TOD shape."""
+    (rel. 1e-13 in FP64, 1e-5 in FP32) on the largest TOD shape: cuBLAS on
+    the FP64/FP32 units (1), cuBLAS emulation (3), and this library's
+    tensor-core kernels (2: FP32 3xTF32; 4: FP64 exact integer slices)."""
     forced = os.environ.get("MINKASI_GB300_ROT")
     if forced:
         return int(forced)
@@ -123,7 +125,7 @@ def choose_rot_mode(op) -> int:
     tol = 1e-13 if op.dtype == torch.float64 else 1e-5
     tc_ok = op.dtype == torch.float32 and os.environ.get("MINKASI_GB300_TC", "1") != "0" and \
         nd in (32, 64, 128, 256)
-    modes = [1, 3] + ([2] if tc_ok else [])
+    modes = [1, 3] + ([2] if tc_ok else []) + ([4] if op.dtype == torch.float64 else [])
     times = {}
     for m in modes:
         try:

@@ -40,6 +40,7 @@
 
 #include "mk_common.cuh"
 #include "mk_fft4.cuh"
+#include "mk_ozaki.cuh"
 #include "mk_rot.cuh"
 
 namespace {
@@ -161,14 +162,20 @@ struct DctCore {
   // image (workspace: rebuilt by every rotation)
   int *tc_err = nullptr;
   void *tc_bimg = nullptr;
+  // sliced FP64 rotation on the bf16 tensor cores (FP64 plans): its scratch
+  // in the workspace
+  void *oz_ws = nullptr;
+  size_t oz_bytes = 0;
   // device memory the plan owns: the status word, then the four-step tables.
   // Never in the workspace, which plans of different shapes may share.
   void *owned = nullptr;
 };
 
-// workspace bytes of the tensor-core rotation's operand image
+// workspace bytes of the tensor-core rotation's operand image (FP32) or of
+// the sliced FP64 rotation's scratch (FP64)
 size_t tc_bytes(int64_t nrow, int dtype) {
-  if (dtype != MK_F32 || !mk::rot_tc_supported(nrow)) return 0;
+  if (dtype == MK_F64) return mk::ozaki_supported(nrow) ? align_up(mk::ozaki_ws_bytes(nrow)) : 0;
+  if (!mk::rot_tc_supported(nrow)) return 0;
   return align_up(mk::rot_tc_bimg_bytes(nrow));
 }
 
@@ -213,7 +220,8 @@ bool use_own(int64_t nrow, int64_t n, int dtype, mk::Fft4Dev *d, bool *blue_ok) 
   return dtype == MK_F32 && e != 1 && (nrow + 1) / 2 <= 65535 && mk::fft4_shape(n, d, *blue_ok);
 }
 
-int core_bytes(int64_t nrow, int64_t n, int dtype, size_t *bytes) {
+// rot: the plan rotates too (noise plans): reserve the rotation scratch
+int core_bytes(int64_t nrow, int64_t n, int dtype, size_t *bytes, bool rot = true) {
   MK_CHECK_ARG(bytes, "workspace size: null output");
   MK_CHECK_ARG(MK_DTYPE_OK(dtype), "workspace size: bad dtype %d", dtype);
   MK_CHECK_ARG(nrow >= 1 && n >= 2, "DCT-I needs nrow >= 1 and n >= 2 (got %lld, %lld)",
@@ -222,7 +230,7 @@ int core_bytes(int64_t nrow, int64_t n, int dtype, size_t *bytes) {
   bool blue_ok;
   if (use_own(nrow, n, dtype, &d, &blue_ok)) {
     *bytes = align_up((size_t)nrow * n * sizeof(float)) + align_up(mk::fft4_t_bytes(d, nrow)) +
-             tc_bytes(nrow, dtype);
+             (rot ? tc_bytes(nrow, dtype) : 0);
     return MK_OK;
   }
   int64_t N = 2 * (n - 1);
@@ -232,13 +240,13 @@ int core_bytes(int64_t nrow, int64_t n, int dtype, size_t *bytes) {
   if (rc) return rc;
   cufftDestroy(h);
   *bytes = align_up((size_t)nrow * N * elt(dtype)) + align_up((size_t)nrow * n * 2 * elt(dtype)) +
-           align_up(work) + tc_bytes(nrow, dtype);
+           align_up(work) + (rot ? tc_bytes(nrow, dtype) : 0);
   return MK_OK;
 }
 
-int core_create(DctCore *c, int64_t nrow, int64_t n, int dtype, void *ws, size_t ws_bytes) {
+int core_create(DctCore *c, int64_t nrow, int64_t n, int dtype, void *ws, size_t ws_bytes, bool rot = true) {
   size_t need = 0;
-  int rc = core_bytes(nrow, n, dtype, &need);
+  int rc = core_bytes(nrow, n, dtype, &need, rot);
   if (rc) return rc;
   MK_CHECK_ARG(ws && ((uintptr_t)ws % ALIGN) == 0, "workspace must be a 256-byte aligned device pointer");
   MK_CHECK_ARG(ws_bytes >= need, "workspace too small: %zu < %zu bytes", ws_bytes, need);
@@ -255,7 +263,7 @@ int core_create(DctCore *c, int64_t nrow, int64_t n, int dtype, void *ws, size_t
     p += align_up((size_t)nrow * n * sizeof(float));
     c->T = (float2 *)p;
     p += align_up(mk::fft4_t_bytes(d, nrow));
-    if (tc_bytes(nrow, dtype)) c->tc_bimg = p;
+    if ((rot ? tc_bytes(nrow, dtype) : 0)) c->tc_bimg = p;
     if ((rc = own_alloc(c, mk::fft4_table_bytes(d))) ||
         (rc = mk::fft4_init(&c->f4, n, (char *)c->owned + 256, blue_ok))) {
       core_free(c);
@@ -271,8 +279,13 @@ int core_create(DctCore *c, int64_t nrow, int64_t n, int dtype, void *ws, size_t
   rc = make_fft(&c->fft, nrow, c->N, dtype, &c->work_bytes);
   if (rc) return rc;
   c->have_fft = true;
-  if (tc_bytes(nrow, dtype)) {
-    c->tc_bimg = (char *)c->work + align_up(c->work_bytes);
+  if ((rot ? tc_bytes(nrow, dtype) : 0)) {
+    if (dtype == MK_F64) {
+      c->oz_ws = (char *)c->work + align_up(c->work_bytes);
+      c->oz_bytes = (rot ? tc_bytes(nrow, dtype) : 0);
+    } else {
+      c->tc_bimg = (char *)c->work + align_up(c->work_bytes);
+    }
     if ((rc = own_alloc(c, 0))) {
       core_free(c);
       return rc;
@@ -390,6 +403,15 @@ int rotate(DctCore *c, int mode, const void *A, const void *X, int64_t ldx, void
     return mk::rot_tc_f32((const float *)A, (const float *)X, ldx, (float *)R, ldr, nrow, ncol,
                           c->tc_bimg, c->tc_err, st, mirror_n, x_stride, halve_ends);
   }
+  if (mode == 4) {
+    MK_CHECK_ARG(dtype == MK_F64 && c->oz_ws, "sliced tensor-core rotation (rot_mode 4) is FP64 only");
+    std::lock_guard<std::mutex> lk(g_blas_mu);
+    cublasHandle_t h;
+    int rc = blas_handle(&h);
+    if (rc) return rc;
+    return mk::ozaki_rotate_f64(h, (const double *)A, (const double *)X, ldx, (double *)R, ldr, nrow, ncol,
+                                c->oz_ws, c->oz_bytes, st);
+  }
   MK_CHECK_ARG(mode == 1 || mode == 3, "bad rot_mode %d", mode);
   return blas_rotate(dtype, A, X, ldx, R, ldr, nrow, ncol, mode == 3, st);
 }
@@ -438,7 +460,7 @@ struct mk_noise_plan {
 };
 
 extern "C" int mk_dct1_workspace_bytes(int64_t nrow, int64_t n, int dtype, size_t *bytes) {
-  return core_bytes(nrow, n, dtype, bytes);
+  return core_bytes(nrow, n, dtype, bytes, false);
 }
 
 extern "C" int mk_dct1_plan_create(mk_dct_plan **plan, int64_t nrow, int64_t n, int dtype,
@@ -447,7 +469,7 @@ extern "C" int mk_dct1_plan_create(mk_dct_plan **plan, int64_t nrow, int64_t n, 
   *plan = nullptr;
   mk_dct_plan *p = new (std::nothrow) mk_dct_plan;
   if (!p) return MK_ERR_NOMEM;
-  int rc = core_create(&p->core, nrow, n, dtype, workspace, workspace_bytes);
+  int rc = core_create(&p->core, nrow, n, dtype, workspace, workspace_bytes, false);
   if (rc) {
     delete p;
     return rc;

@@ -82,7 +82,7 @@ def run(config: str = "c2s", only=None, shape=None) -> dict:
             A = A.to(dev).to(dt).contiguous()
         if "rot" in want:
             ref = plan.rotate(A, dat, rot_mode=1)
-            for mode in ((1, 3) if es == 8 else (1, 2, 3)):
+            for mode in ((1, 3, 4) if es == 8 else (1, 2, 3)):
                 try:
                     y = plan.rotate(A, dat, rot_mode=mode)
                 except K._lib.MkError as e:
@@ -95,7 +95,7 @@ def run(config: str = "c2s", only=None, shape=None) -> dict:
         if "noise" in want:
             w = torch.rand((ndet, n), generator=g, dtype=dt, device=dev)
             o = torch.empty_like(dat)
-            for mode in ((1, 3) if es == 8 else (1, 2)):
+            for mode in ((1, 4) if es == 8 else (1, 2)):
                 try:
                     ms = best_ms(lambda m=mode: plan.apply(A, A.T.contiguous(), w, dat, out=o, rot_mode=m),
                                  reps=3)

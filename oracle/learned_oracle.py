@@ -80,6 +80,34 @@ def loss(ws, dsq, mask, R, E, shape) -> float:
     return float(((res ** 2).sum(axis=1) / (pe ** 2).sum(axis=1)).mean())
 
 
+def pool(x: np.ndarray, b: int) -> np.ndarray:
+    """b x b block mean of [B, C, H, W] maps, pixels outside the map as 0."""
+    B, C, H, W = x.shape
+    Hc, Wc = -(-H // b), -(-W // b)
+    xp = np.zeros((B, C, Hc * b, Wc * b))
+    xp[:, :, :H, :W] = x
+    return xp.reshape(B, C, Hc, b, Wc, b).sum(axis=(3, 5)) / (b * b)
+
+
+def unpool(y: np.ndarray, b: int, H: int, W: int) -> np.ndarray:
+    """The transpose of pool: each fine pixel gets its block's value / b^2."""
+    up = np.repeat(np.repeat(y, b, axis=2), b, axis=3) / (b * b)
+    return up[:, :, :H, :W]
+
+
+def pooled_loss(ws, dsq, mask, R, E, shape, b: int) -> float:
+    """The loss of the multi-scale form M r = dsq (u + P^T K^T K P u)."""
+    B = R.shape[0]
+    u = R * dsq[None, :]
+    z = unpool(ktk(ws, pool(u.reshape(B, 1, *shape), b)), b, *shape).reshape(B, -1)
+    mr = dsq[None, :] * (u + z)
+    pe = _proj(E, mask)
+    a = _proj(mr, mask)
+    c = (a * pe).sum(axis=1) / (a * a).sum(axis=1)
+    res = c[:, None] * a - pe
+    return float(((res ** 2).sum(axis=1) / (pe ** 2).sum(axis=1)).mean())
+
+
 def loss_grad(ws, dsq, mask, R, E, shape) -> Tuple[float, List[np.ndarray]]:
     """Loss and its gradient w.r.t. every weight (backprop through K^T K)."""
     B = R.shape[0]

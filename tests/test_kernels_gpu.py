@@ -329,6 +329,40 @@ def test_apply_noise_golden_f64(K, gold):
     assert rel(x.cpu().numpy(), g["dd"]) < 1e-12
 
 
+@pytest.mark.parametrize("nd,n", [(64, 70_001), (256, 140_000), (37, 1001)])
+def test_sliced_fp64_rotation(K, nd, n):
+    """rot_mode 4: FP64 R = A X from exact 7-bit integer slices on the bf16
+    tensor cores, against numpy's FP64 product, on columns whose scales span
+    1e-200 .. 1e+200 (and all-zero columns), more columns than one block
+    holds, and detector counts that are not tile multiples."""
+    rng = np.random.default_rng(nd)
+    A = np.linalg.qr(rng.standard_normal((nd, nd)))[0]
+    A[:, 3] *= 1e-9                     # entries of very different size in a row
+    X = rng.standard_normal((nd, n)) * 10.0 ** rng.integers(-200, 200, size=n)[None, :]
+    X[:, 5] = 0.0
+    X[7, :] *= 1e-12
+    want = A @ X
+    plan = K.NoisePlan(nd, n, torch.float64)
+    got = plan.rotate(dev(A), dev(X), rot_mode=4).cpu().numpy()
+    # error per column relative to that column's scale (the scales differ by
+    # 10^400, so a matrix-wide relative error would hide the small columns);
+    # 2e-15 leaves room for numpy's own rounding over sums of up to 256 terms
+    scale = np.abs(A).sum(axis=1)[:, None] * np.abs(X).max(axis=0)[None, :] + 1e-300
+    assert np.max(np.abs(got - want) / scale) < 2e-15
+    assert np.array_equal(got[:, 5], np.zeros(nd))
+
+
+def test_apply_noise_golden_f64_sliced_rotation(K, gold):
+    """The reference's apply_noise (noise.npz) with the sliced FP64 rotation."""
+    g = gold("noise.npz")
+    v, vT, w = dev(g["v"]), dev(g["vT"]), dev(g["mywt"])
+    for key_x, key_dd in (("x", "dd"), ("x_short", "dd_short")):
+        x = g[key_x]
+        plan = K.NoisePlan(x.shape[0], x.shape[1], torch.float64)
+        dd = plan.apply(v, vT, w, dev(x), rot_mode=4).cpu().numpy()
+        assert rel(dd, g[key_dd]) < 1e-12, key_x
+
+
 def test_apply_noise_prewhitened_by_folding(K, gold):
     g = gold("noise.npz")
     nv = g["pw_noisevec"]

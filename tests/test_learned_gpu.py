@@ -201,33 +201,25 @@ def test_pooled_stencil_apply(L, dtype):
 
 def test_pooled_training_gradient_directional(L):
     """The pooled loss gradient (P applied to the incoming gradient, then the
-    network's own backward kernels) against a central finite difference of
-    the loss along a random direction of the weights."""
+    network's own backward kernels, FP32) against a central finite
+    difference, in float64, of the oracle's pooled loss along a random
+    direction of the weights."""
     rng = np.random.default_rng(12)
     shape, b, B = (48, 40), 4, 3
     n = shape[0] * shape[1]
-    hits = torch.from_numpy(rng.integers(0, 6, size=n).astype(np.float32)).to(cuda)
-    mask = (hits > 0).float()
-    dsq = torch.where(hits > 0, 1 / torch.sqrt(hits.clamp(min=1)), torch.zeros_like(hits))
-    R = torch.from_numpy(rng.standard_normal((B, n)).astype(np.float32)).to(cuda)
-    E = torch.from_numpy(rng.standard_normal((B, n)).astype(np.float32)).to(cuda)
-    # weights with a per-layer gain of about 2 (as in the oracle gradient
-    # test), so that K^T K moves the loss well above FP32 rounding
-    ws = [torch.from_numpy((rng.standard_normal((co, ci, 3, 3)) * 0.2).astype(np.float32)).to(cuda)
-          for ci, co in zip(L.CHANNELS[:-1], L.CHANNELS[1:])]
-    net = L.ConvNet(ws, pool=b)
-    loss, grads = L.loss_and_grad(net, dsq, mask, R, E, shape)
-    dirs = [torch.from_numpy((rng.standard_normal(tuple(w.shape)) * 0.2).astype(np.float32)).to(cuda)
-            for w in net.weights]
-    ana = float(sum((g * d).sum() for g, d in zip(grads, dirs)))
-    h = 1e-3
-    base = [w.clone() for w in net.weights]
-    vals = []
-    for sgn in (1, -1):
-        for w, w0, d in zip(net.weights, base, dirs):
-            w.copy_(w0 + sgn * h * d)
-        vals.append(L.loss_and_grad(net, dsq, mask, R, E, shape, need_grad=False)[0])
-    for w, w0 in zip(net.weights, base):
-        w.copy_(w0)
-    num = (vals[0] - vals[1]) / (2 * h)
-    assert abs(num - ana) < 2e-2 * max(abs(ana), 1e-6), (num, ana)
+    hits = rng.integers(0, 6, size=n).astype(np.float64)
+    mask = (hits > 0).astype(np.float64)
+    dsq = np.where(hits > 0, 1 / np.sqrt(np.maximum(hits, 1)), 0.0)
+    R = rng.standard_normal((B, n))
+    E = rng.standard_normal((B, n))
+    ws = [rng.standard_normal((co, ci, 3, 3)) * 0.2 for ci, co in zip(L.CHANNELS[:-1], L.CHANNELS[1:])]
+    dirs = [rng.standard_normal(w.shape) * 0.2 for w in ws]
+    net = L.ConvNet([t(w) for w in ws], pool=b)
+    loss, grads = L.loss_and_grad(net, t(dsq), t(mask), t(R), t(E), shape)
+    ana = float(sum((g.cpu().double().numpy() * d).sum() for g, d in zip(grads, dirs)))
+    h = 1e-6
+    lp = lo.pooled_loss([w + h * d for w, d in zip(ws, dirs)], dsq, mask, R, E, shape, b)
+    lm = lo.pooled_loss([w - h * d for w, d in zip(ws, dirs)], dsq, mask, R, E, shape, b)
+    num = (lp - lm) / (2 * h)
+    assert abs(loss - lo.pooled_loss(ws, dsq, mask, R, E, shape, b)) < 1e-4 * abs(loss)
+    assert abs(num - ana) < 1e-2 * abs(num), (num, ana)
