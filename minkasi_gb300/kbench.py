@@ -2,6 +2,7 @@
 
     python -m minkasi_gb300.kbench [--config c2s] [--only tod2map,map2tod,rot,noise,dct,conv,point,pol]
                                    [--shape NDET,NDATA]
+    python -m minkasi_gb300.kbench --config c2 --only iter      # the whole operator (iter64: FP64 too)
 
 Uses the first TOD shape and daisy pointing of a synthetic configuration
 (default c2s: 256 detectors x 130978 samples onto a 1024x1024 map; --shape
@@ -117,6 +118,50 @@ def run(config: str = "c2s", only=None, shape=None) -> dict:
     return out
 
 
+def iter_bench(config: str, dtypes=("f32",), reps: int = 3) -> dict:
+    """The whole configuration's operator A x = P^T N P x, per precision:
+    one application and its parts (map2tod over all TODs, the noise filter,
+    tod2map), the filter both as the one-call group over all TODs and TOD by
+    TOD, and the per-TOD filter time summed over TODs whose transform runs
+    Bluestein's algorithm and over the others."""
+    from . import synth
+    dev = torch.device("cuda", torch.cuda.current_device())
+    cfg = CONFIGS[config]
+    tv, m = synth.make_todvec(cfg, dev)
+    S = tv.get_nsamp()
+    res = {"config": config, "samples": S, "ntod": len(tv.tods)}
+    for tag in dtypes:
+        dt = torch.float32 if tag == "f32" else torch.float64
+        op = tv.engine(m, dt)
+        op.prepare_noise()
+        x = torch.randn(m.npix, dtype=dt, device=dev)
+        y = torch.empty_like(x)
+        r = {"rot_mode": op.rot_mode, "tod2map_kernel": op.method,
+             "apply_ms": best_ms(lambda: op.apply(x, y), reps=reps, warm=1),
+             "map2tod_ms": best_ms(lambda: K.map2tod(op.tmp, x, op.ipix, False), reps=reps, warm=1),
+             "tod2map_ms": best_ms(lambda: op.project_out(y), reps=reps, warm=1)}
+        grp = op._noise_group()
+        if grp is not None:
+            r["noise_group_ms"] = best_ms(grp.apply, reps=reps, warm=1)
+        blue = smooth = 0.0
+        nblue = 0
+        for (v, vT, w), view, dims in zip(op.ops, op.views(op.tmp), op.dims):
+            p = op.plans[dims]
+            ms = best_ms(lambda: p.apply(v, vT, w, view, out=view, rot_mode=op.rot_mode), reps=2, warm=1)
+            L1, L2 = p.split
+            if L1 * L2 not in (0, 2 * (dims[1] - 1)):
+                blue += ms
+                nblue += 1
+            else:
+                smooth += ms
+        r.update(noise_per_tod_ms=blue + smooth, noise_bluestein_ms=blue, noise_smooth_ms=smooth,
+                 n_bluestein=nblue, dct_engines={f"{a}x{b}": e for (a, b), e in op.dct_engines.items()})
+        res[tag] = r
+        op.release()
+        torch.cuda.empty_cache()
+    return res
+
+
 def point_pol_bench(cfg, ndet: int, n: int, dev, want) -> dict:
     """Pointing -> pixel (16 B of RA/dec read, 4 B written per sample) and
     the IQU projections with cached cos/sin 2gamma (4 B pixel + 16 B angle
@@ -210,4 +255,8 @@ if __name__ == "__main__":
     ap.add_argument("--shape", default="", help="NDET,NDATA instead of the configuration's first TOD")
     a = ap.parse_args()
     shape = tuple(int(v) for v in a.shape.split(",")) if a.shape else None
-    print(json.dumps(run(a.config, [s for s in a.only.split(",") if s] or None, shape)))
+    only = [s for s in a.only.split(",") if s] or None
+    if only and only[0] in ("iter", "iter64"):
+        print(json.dumps(iter_bench(a.config, ("f32", "f64") if only[0] == "iter64" else ("f32",))))
+    else:
+        print(json.dumps(run(a.config, only, shape)))
