@@ -379,7 +379,7 @@ int mk_noise_status(mk_noise_plan *plan, int *code, void *stream);
  * TOD's (ndet, ndata) float32 timestream data[t] (the batched operator's
  * pooled buffer): the v and vT detector rotations of all TODs with the same
  * detector count run as one tensor-core launch each (3xTF32, as rot_mode 2),
- * and each TOD's two DCT-I run on its plan (plans[t]: FP32, four-step FFT,
+ * and each TOD's two DCT-I run on its plan (plans[t]: FP32, any DCT engine,
  * ndet in {32, 64, 128, 256}).  Same arithmetic as mk_apply_noise with
  * rot_mode 2 on each TOD, bit for bit.  The group keeps the rotation
  * operand images of v and vT (built at creation: 8 ndet^2 bytes each) and

@@ -9,13 +9,13 @@
 // and k = k2 + L2 k1:
 //   pass A: for each j1, T[j1][k2] = W_L^{j1 k2} sum_j2 e_{j1 + L1 j2} W_L2^{j2 k2}
 //   pass B: for each k2, F[k2 + L2 k1] = sum_j1 T[j1][k2] W_L1^{j1 k1}
-// Each CTA runs 8 transforms of one pass in shared memory (mixed-radix
+// Each CTA runs 8 or 16 transforms of one pass in shared memory (mixed-radix
 // decimation in time, butterflies in place), interleaved over its threads.
 // The first stage of each pass reads its inputs straight from global memory
-// (pass A forms the even extension there); pass A's rows are then twiddled
-// and stored one per warp; pass B's last stage writes only k <= m straight
-// to the rows with the epilogue (plain, times the inverse-spectrum weights,
-// or with columns 0 and m halved).  Twiddles come from tables computed in
+// (pass A forms the even extension there); pass A's last stage twiddles its
+// outputs and stores them to T; pass B's last stage writes only k <= m
+// straight to the rows with the epilogue (plain, times the inverse-spectrum
+// weights, or with columns 0 and m halved).  Twiddles come from tables computed in
 // double precision on the host.
 //
 // Lengths whose 2m has a prime factor above 11 (minkasi's truncate_tod leaves
@@ -27,10 +27,12 @@
 // F is then a circular convolution a (*) b of a smooth length M >= 3m, with
 // a at positions j mod M (z_{|j|} c_{|j|}, zero elsewhere) and b_t = conj(c_t)
 // at t mod M for t in [-m, 2m - 1] (one quarter shorter than the M >= 4m - 1
-// of taking j, k over a whole period).  Pass A forms a from the rows; pass B
-// multiplies by B^ = DFT_M(b) / M and stores U = conj(DFT(a) B^); pass A and
-// pass B run again on U, and the last stage writes c_k conj(DFT(U)_k) for
-// k <= m with the usual epilogue.
+// of taking j, k over a whole period).  Pass A forms a from the rows; a
+// middle pass finishes DFT(a) column by column, multiplies by
+// B^ = DFT_M(b) / M, conjugates (U = conj(DFT(a) B^)) and runs the first
+// step of DFT(U) on the same column in shared memory; pass B on the
+// transposed shape finishes DFT(U) and writes c_k conj(DFT(U)_k) for k <= m
+// with the usual epilogue (three passes; four when L1 takes one stage).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -46,6 +48,7 @@ struct Fft4Dev {
   int64_t Lx;       // even-extension length 2m
   bool blue;        // Bluestein: L = M, chirp and bhat set
   int L1, L2, nb32;  // nb32 = ceil(L2 / 32)
+  int fba, fbb;      // transforms per CTA of pass A (length L2) and pass B (length L1): 8 or 16
   int nr1, nr2;
   int r1[FFT4_MAXR], r2[FFT4_MAXR];
   // per stage: span Ns of the earlier stages, 1 / Ns, offset of its twiddles
@@ -58,6 +61,9 @@ struct Fft4Dev {
   const float2 *tlane, *tblk;
   const float2 *chirp;  // Bluestein: c_t, t <= m
   const float2 *bhat;   // Bluestein: DFT_M(b) / M
+  // Bluestein's middle pass: W_M^{k2 o1} = tblk2[k2 nb32b + o1 / 32] * tlane2[32 k2 + o1 % 32]
+  const float2 *tlane2, *tblk2;
+  int nb32b;  // ceil(L1 / 32)
 };
 
 // epilogues of pass B

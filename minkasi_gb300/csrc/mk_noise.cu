@@ -595,8 +595,8 @@ extern "C" int mk_noise_group_create(mk_noise_group **group, int ntod, mk_noise_
     MK_CHECK_ARG(plans[t] && v[t] && vT[t] && mywt[t] && data[t], "mk_noise_group_create: TOD %d: null pointer",
                  t);
     const DctCore &c = plans[t]->core;
-    MK_CHECK_ARG(c.own && c.dtype == MK_F32 && mk::rot_tc_supported(c.nrow),
-                 "mk_noise_group_create: TOD %d: needs an FP32 four-step plan with ndet in {32,64,128,256}", t);
+    MK_CHECK_ARG(c.dtype == MK_F32 && mk::rot_tc_supported(c.nrow),
+                 "mk_noise_group_create: TOD %d: needs an FP32 plan with ndet in {32,64,128,256}", t);
     MK_CHECK_ARG(ldw[t] >= c.n, "mk_noise_group_create: TOD %d: ldw below ndata", t);
   }
   mk_noise_group *g = new (std::nothrow) mk_noise_group;
@@ -678,10 +678,26 @@ extern "C" int mk_noise_group_exec(mk_noise_group *g, void *stream) {
     if ((rc = mk::rot_tc_group(cl.jobs_v, cl.njobs, cl.ntile, cl.ndet, g->err, st))) return rc;
   for (const auto &t : g->tods) {
     DctCore *c = t.core;
-    if ((rc = mk::fft4_dct(c->f4, t.data, c->n, c->nrow, c->T, t.data, c->n, mk::FFT4_FILTER, t.w, t.ldw, st)))
-      return rc;
-    if ((rc = mk::fft4_dct(c->f4, t.data, c->n, c->nrow, c->T, t.data, c->n, mk::FFT4_HALVE, nullptr, 0, st)))
-      return rc;
+    if (c->own) {
+      if ((rc = mk::fft4_dct(c->f4, t.data, c->n, c->nrow, c->T, t.data, c->n, mk::FFT4_FILTER, t.w, t.ldw, st)))
+        return rc;
+      if ((rc = mk::fft4_dct(c->f4, t.data, c->n, c->nrow, c->T, t.data, c->n, mk::FFT4_HALVE, nullptr, 0, st)))
+        return rc;
+      continue;
+    }
+    // a cuFFT plan: extension, transform, filter + extension, transform,
+    // real part with the end columns halved, back into the TOD
+    const int64_t n = c->n, N = c->N, nd = c->nrow;
+    const dim3 gr = rows_grid(n, nd);
+    k_extend<float><<<gr, 256, 0, st>>>(t.data, n, (float *)c->E, n, N, nd);
+    if ((rc = mk::launch_status("noise group/extend"))) return rc;
+    if ((rc = core_fft(c, st))) return rc;
+    k_filter_extend<float, cufftComplex><<<gr, 256, 0, st>>>((const cufftComplex *)c->F, t.w, t.ldw,
+                                                               (float *)c->E, n, N, nd);
+    if ((rc = mk::launch_status("noise group/filter"))) return rc;
+    if ((rc = core_fft(c, st))) return rc;
+    k_real_halve<float, cufftComplex><<<gr, 256, 0, st>>>((const cufftComplex *)c->F, t.data, n, nd);
+    if ((rc = mk::launch_status("noise group/halve"))) return rc;
   }
   for (const auto &cl : g->classes)
     if ((rc = mk::rot_tc_group(cl.jobs_vT, cl.njobs, cl.ntile, cl.ndet, g->err, st))) return rc;

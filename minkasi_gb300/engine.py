@@ -144,16 +144,15 @@ class MapmakingOperator:
             raise ValueError(f"unknown tod2map method {m!r}")
 
     def _noise_group(self):
-        """The one-call filter over all TODs (kernels.NoiseGroup) when every
-        TOD runs the FP32 four-step FFT with tensor-core rotations, else
-        None (then the filter runs TOD by TOD)."""
+        """The one-call filter over all TODs (kernels.NoiseGroup) when the
+        operator is FP32 with tensor-core rotations (every ndet in 32, 64,
+        128, 256), else None (then the filter runs TOD by TOD)."""
         if self._group is False:
             return None
         key = self.tmp.data_ptr()
         if self._group is not None and self._group_key == key:
             return self._group
         ok = (self.dtype == torch.float32 and self.rot_mode == 2 and
-              all(p.engine in (0, 2) for p in self.plans.values()) and
               all(nd in (32, 64, 128, 256) for nd, _ in self.dims) and
               os.environ.get("MINKASI_GB300_GROUP", "1") != "0")
         if not ok:

@@ -156,6 +156,12 @@ def iter_bench(config: str, dtypes=("f32",), reps: int = 3) -> dict:
                 smooth += ms
         r.update(noise_per_tod_ms=blue + smooth, noise_bluestein_ms=blue, noise_smooth_ms=smooth,
                  n_bluestein=nblue, dct_engines={f"{a}x{b}": e for (a, b), e in op.dct_engines.items()})
+        # one more application inside an NVTX range, for a profiler's
+        # launch list of exactly one operator application
+        torch.cuda.synchronize()
+        with torch.cuda.nvtx.range(f"apply_{tag}"):
+            op.apply(x, y)
+            torch.cuda.synchronize()
         res[tag] = r
         op.release()
         torch.cuda.empty_cache()

@@ -233,12 +233,14 @@ def test_dct1_f32_and_roundtrip(K):
     assert rel(back, x) < 2e-6
 
 
+@pytest.mark.parametrize("fb", ["8", "16"])
 @pytest.mark.parametrize("nrow,n", [(1, 2), (1, 3), (2, 5), (3, 13), (4, 100), (5, 331), (2, 4097),
                                     (16, 2311), (9, 694), (8, 600001), (256, 130978)])
-def test_dct1_f32_four_step(K, nrow, n):
+def test_dct1_f32_four_step(K, nrow, n, fb, monkeypatch):
     """FP32 DCT-I through the four-step FFT (every 2(n-1) here factors into
     2, 3, 5, 7, 11; odd nrow leaves the last row pair half empty) against the
-    FP64 oracle."""
+    FP64 oracle, with 8 and with 16 transforms per CTA."""
+    monkeypatch.setenv("MINKASI_GB300_FFT4_FB", fb)
     x = np.random.default_rng(n).standard_normal((nrow, n))
     d = K.DCT1(nrow, n, torch.float32)
     assert d.engine == 0
@@ -248,11 +250,15 @@ def test_dct1_f32_four_step(K, nrow, n):
     assert np.linalg.norm(y - ref) < 2e-6 * np.linalg.norm(ref)
 
 
+@pytest.mark.parametrize("fb,passes", [("8", "3"), ("16", "3"), ("16", "4")])
 @pytest.mark.parametrize("nrow,n", [(3, 38), (3, 1000), (4, 700), (5, 18623), (2, 465551), (16, 144278)])
-def test_dct1_f32_bluestein(K, nrow, n):
+def test_dct1_f32_bluestein(K, nrow, n, fb, passes, monkeypatch):
     """Lengths whose 2(n-1) has a prime factor above 11 (37, 37, 233, 9311,
     9311, 72139): Bluestein's algorithm on the four-step passes, against the
-    FP64 oracle; the last two are c2 TOD lengths."""
+    FP64 oracle (8 and 16 transforms per CTA; the fused middle pass and the
+    four-pass form); the last two are c2 TOD lengths."""
+    monkeypatch.setenv("MINKASI_GB300_FFT4_FB", fb)
+    monkeypatch.setenv("MINKASI_GB300_FFT4_BLUE3", "0" if passes == "4" else "1")
     x = np.random.default_rng(n).standard_normal((nrow, n))
     d = K.DCT1(nrow, n, torch.float32)
     assert d.engine == 2
@@ -374,8 +380,12 @@ def test_apply_noise_prewhitened_by_folding(K, gold):
     assert rel(dd, g["pw_dd"]) < 1e-12
 
 
-@pytest.mark.parametrize("engine", [0, 1])
-def test_apply_noise_f32_close_to_f64(K, gold, engine):
+@pytest.mark.parametrize("engine,fb", [(0, "8"), (0, "16"), (1, "")])
+def test_apply_noise_f32_close_to_f64(K, gold, engine, fb, monkeypatch):
+    """FP32 apply_noise (the filter epilogue of pass B, weights prefetched
+    to shared memory with 8 transforms per CTA, read directly with 16)
+    against the reference's FP64 output."""
+    monkeypatch.setenv("MINKASI_GB300_FFT4_FB", fb)
     g = gold("noise.npz")
     try:
         K.set_dct_engine(engine)

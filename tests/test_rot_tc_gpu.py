@@ -55,20 +55,25 @@ def test_tc_apply_noise_matches_golden(K, gold):
     assert rel(dd[:10], g["dd"]) < 2e-5
 
 
-def test_noise_group_equals_per_tod_filter(monkeypatch):
+@pytest.mark.parametrize("dct", ["0", "1"])
+def test_noise_group_equals_per_tod_filter(monkeypatch, dct):
     """The one-call filter over all TODs (rotations of all TODs with one
     detector count in one tensor-core launch, in place) gives bit for bit
     what the per-TOD apply_noise gives, on TODs of 32 and 64 detectors with
-    untruncated lengths (so some run Bluestein's algorithm)."""
+    untruncated lengths (so some run Bluestein's algorithm), with the
+    four-step FFT and with cuFFT plans."""
     from dataclasses import replace
     from minkasi_gb300 import synth
     from minkasi_gb300.engine import MapmakingOperator
-    monkeypatch.setenv("MINKASI_GB300_DCT", "0")
+    monkeypatch.setenv("MINKASI_GB300_DCT", dct)
     cfg = replace(synth.CONFIGS["tiny"], ntod=5, ndet_choices=(32, 64), nsamp_range=(3000, 9000),
                   truncate=False)
     tv, m = synth.make_todvec(cfg)
     op = MapmakingOperator(tv, m, torch.float32, tod2map="atomic", rot_mode=2)
-    assert set(op.dct_engines.values()) <= {0, 2} and 2 in op.dct_engines.values()
+    if dct == "0":
+        assert set(op.dct_engines.values()) <= {0, 2} and 2 in op.dct_engines.values()
+    else:
+        assert set(op.dct_engines.values()) == {1}
     grp = op._noise_group()
     assert grp is not None
     g = torch.Generator(device="cuda").manual_seed(3)
