@@ -231,14 +231,18 @@ enum { AM_DCT = 0, AM_BLUE = 1, AM_CPLX = 2 };
 #define MK_FFT4_NT16 512
 #endif
 #ifndef MK_FFT4_NT8
-#define MK_FFT4_NT8 256
+#define MK_FFT4_NT8 512
 #endif
 #ifndef MK_FFT4_RMAX
 #define MK_FFT4_RMAX 16  // largest radix held in registers
 #endif
+#ifndef MK_FFT4_MINB8
+#define MK_FFT4_MINB8 2
+#endif
 template <int FB>
 struct Cfg {
   static constexpr int NT = FB == 16 ? MK_FFT4_NT16 : MK_FFT4_NT8;
+  static constexpr int MINB = FB == 16 ? 2 : MK_FFT4_MINB8;
 };
 
 struct PassA {
@@ -384,7 +388,7 @@ __host__ __device__ __forceinline__ int pitch_odd(int Ls) { return Ls | 1; }
 // pass A: rows (2 pair, 2 pair + 1) of x (or the pair's U) -> T[pair]
 // (L1 x L2, twiddled)
 template <int AM, int FB>
-__global__ void __launch_bounds__(Cfg<FB>::NT, 2) k_fft4_a(const float *__restrict__ x, int64_t ldx,
+__global__ void __launch_bounds__(Cfg<FB>::NT, Cfg<FB>::MINB) k_fft4_a(const float *__restrict__ x, int64_t ldx,
                                                     const float2 *__restrict__ U, int64_t nrow,
                                                     float2 *__restrict__ T, const Fft4Dev p, const WrTable wt) {
   extern __shared__ float2 sbuf[];
@@ -456,8 +460,8 @@ struct PassB {
   int L2, k2_0, nb, m, epi;
   bool has2;
   float *o1, *o2;
-  const float *sw;        // FB == 8: prefetched weights, [k1][b][row]
-  const float *w1, *w2;   // FB == 16: the weight rows, read in the last stage
+  const float *sw;        // prefetched weights, [k1][b][row], or null
+  const float *w1, *w2;   // else the weight rows, read in the last stage
   const int *iperm;
 };
 
@@ -499,7 +503,7 @@ __device__ __forceinline__ void bstage(float2 *sbuf, int pitch, int Ls, int Ns, 
         if (BM == BM_BLUE) v[r] = cmul(make_float2(v[r].x, -v[r].y), __ldg(pb.chirp + kk));
         float a = v[r].x, c = v[r].y;
         if (pb.epi == FFT4_FILTER) {
-          if (FB == 8) {
+          if (pb.sw) {
             a *= pb.sw[2 * (k1 * FB + b)];
             c *= pb.sw[2 * (k1 * FB + b) + 1];
           } else {
@@ -553,10 +557,10 @@ __device__ __forceinline__ void bstage_r(int R, float2 *sbuf, int pitch, int Ls,
 // pass B: T[pair] -> DCT rows 2 pair, 2 pair + 1 of out (k <= m) with the
 // epilogue, or (BM_MUL) -> the pair's U
 template <int BM, int FB>
-__global__ void __launch_bounds__(Cfg<FB>::NT, 2) k_fft4_b(const float2 *__restrict__ T, int64_t nrow,
+__global__ void __launch_bounds__(Cfg<FB>::NT, Cfg<FB>::MINB) k_fft4_b(const float2 *__restrict__ T, int64_t nrow,
                                                     float *__restrict__ out, int64_t ldo, float2 *__restrict__ U,
                                                     const float *__restrict__ w, int64_t ldw, int epi,
-                                                    const Fft4Dev p, const WrTable wt) {
+                                                    int wpre, const Fft4Dev p, const WrTable wt) {
   extern __shared__ float2 sbuf[];
   const int L1 = p.L1, L2 = p.L2, pitch = pitch_odd(L1), tid = threadIdx.x;
   const int64_t pair = blockIdx.y, r0 = 2 * pair;
@@ -581,9 +585,9 @@ __global__ void __launch_bounds__(Cfg<FB>::NT, 2) k_fft4_b(const float2 *__restr
     const float *w2 = pb.has2 ? w1 + ldw : w1;
     pb.w1 = w1;
     pb.w2 = w2;
-    if (FB == 8) {
+    if (wpre) {
       // the weights of this tile's outputs, [k1][b][row], prefetched during
-      // the first stages
+      // the first stages (when two CTAs still fit an SM with them)
       float *sw = reinterpret_cast<float *>(sbuf + FB * pitch);
       pb.sw = sw;
 #pragma unroll 4
@@ -797,7 +801,7 @@ __device__ __forceinline__ void cstage_last(const float2 *sbuf, int pitch, int N
 // T[pair] (L1 x L2, from pass A on the chirped rows) -> V[pair] (L2 x L1);
 // needs nr1 >= 2
 template <int FB>
-__global__ void __launch_bounds__(Cfg<FB>::NT, 2) k_fft4_conv(const float2 *__restrict__ T, float2 *__restrict__ V,
+__global__ void __launch_bounds__(Cfg<FB>::NT, Cfg<FB>::MINB) k_fft4_conv(const float2 *__restrict__ T, float2 *__restrict__ V,
                                                      const Fft4Dev p, const WrTable wt) {
   extern __shared__ float2 sbuf[];
   const int L1 = p.L1, pitch = pitch_odd(L1), S = p.nr1;
@@ -1219,7 +1223,11 @@ int fft4_dct(const Fft4Plan &p, const float *x, int64_t ldx, int64_t nrow, float
   const dim3 ga((d.L1 + fa - 1) / fa, (unsigned)npairs), gb((d.L2 + fb - 1) / fb, (unsigned)npairs);
   const size_t smem_a = (size_t)fa * pitch_odd(d.L2) * sizeof(float2);
   const size_t smem_b = (size_t)fb * pitch_odd(d.L1) * sizeof(float2);
-  const size_t smem_w = epi == FFT4_FILTER && fb == 8 ? (size_t)8 * d.L1 * 2 * sizeof(float) : 0;
+  // FILTER weights go through shared memory on 8-transform passes while two
+  // CTAs still fit an SM; otherwise the last stage reads them directly
+  const size_t smem_w8 = (size_t)8 * d.L1 * 2 * sizeof(float);
+  const int wpre = epi == FFT4_FILTER && fb == 8 && smem_b + smem_w8 <= 113 * 1024;
+  const size_t smem_w = wpre ? smem_w8 : 0;
   auto pass_a = [&](int am, const float *xx, int64_t ldxx, const float2 *uu) {
     if (fa == 16) {
       if (am == AM_DCT) k_fft4_a<AM_DCT, 16><<<ga, Cfg<16>::NT, smem_a, st>>>(xx, ldxx, uu, nrow, T, d, wt);
@@ -1231,22 +1239,22 @@ int fft4_dct(const Fft4Plan &p, const float *x, int64_t ldx, int64_t nrow, float
       else k_fft4_a<AM_CPLX, 8><<<ga, Cfg<8>::NT, smem_a, st>>>(xx, ldxx, uu, nrow, T, d, wt);
     }
   };
-  auto pass_b = [&](int bm, float2 *uu, int e, size_t sm) {
+  auto pass_b = [&](int bm, float2 *uu, int e, size_t sm, int wp) {
     if (fb == 16) {
-      if (bm == BM_DCT) k_fft4_b<BM_DCT, 16><<<gb, Cfg<16>::NT, sm, st>>>(T, nrow, out, ldo, uu, w, ldw, e, d, wt);
-      else if (bm == BM_MUL) k_fft4_b<BM_MUL, 16><<<gb, Cfg<16>::NT, sm, st>>>(T, nrow, out, ldo, uu, w, ldw, e, d, wt);
-      else k_fft4_b<BM_BLUE, 16><<<gb, Cfg<16>::NT, sm, st>>>(T, nrow, out, ldo, uu, w, ldw, e, d, wt);
+      if (bm == BM_DCT) k_fft4_b<BM_DCT, 16><<<gb, Cfg<16>::NT, sm, st>>>(T, nrow, out, ldo, uu, w, ldw, e, wp, d, wt);
+      else if (bm == BM_MUL) k_fft4_b<BM_MUL, 16><<<gb, Cfg<16>::NT, sm, st>>>(T, nrow, out, ldo, uu, w, ldw, e, wp, d, wt);
+      else k_fft4_b<BM_BLUE, 16><<<gb, Cfg<16>::NT, sm, st>>>(T, nrow, out, ldo, uu, w, ldw, e, wp, d, wt);
     } else {
-      if (bm == BM_DCT) k_fft4_b<BM_DCT, 8><<<gb, Cfg<8>::NT, sm, st>>>(T, nrow, out, ldo, uu, w, ldw, e, d, wt);
-      else if (bm == BM_MUL) k_fft4_b<BM_MUL, 8><<<gb, Cfg<8>::NT, sm, st>>>(T, nrow, out, ldo, uu, w, ldw, e, d, wt);
-      else k_fft4_b<BM_BLUE, 8><<<gb, Cfg<8>::NT, sm, st>>>(T, nrow, out, ldo, uu, w, ldw, e, d, wt);
+      if (bm == BM_DCT) k_fft4_b<BM_DCT, 8><<<gb, Cfg<8>::NT, sm, st>>>(T, nrow, out, ldo, uu, w, ldw, e, wp, d, wt);
+      else if (bm == BM_MUL) k_fft4_b<BM_MUL, 8><<<gb, Cfg<8>::NT, sm, st>>>(T, nrow, out, ldo, uu, w, ldw, e, wp, d, wt);
+      else k_fft4_b<BM_BLUE, 8><<<gb, Cfg<8>::NT, sm, st>>>(T, nrow, out, ldo, uu, w, ldw, e, wp, d, wt);
     }
   };
   int rc;
   if (!d.blue) {
     pass_a(AM_DCT, x, ldx, nullptr);
     if ((rc = launch_status("fft4 pass A"))) return rc;
-    pass_b(BM_DCT, nullptr, epi, smem_b + smem_w);
+    pass_b(BM_DCT, nullptr, epi, smem_b + smem_w, wpre);
     return launch_status("fft4 pass B");
   }
   float2 *U = T + npairs * d.L;
@@ -1273,18 +1281,21 @@ int fft4_dct(const Fft4Plan &p, const float *x, int64_t ldx, int64_t nrow, float
     std::swap(tr.iperm1, tr.iperm2);
     const dim3 gt((tr.L2 + fa - 1) / fa, (unsigned)npairs);
     const size_t smem_t = (size_t)fa * pitch_odd(tr.L1) * sizeof(float2);
-    const size_t smem_tw = epi == FFT4_FILTER && fa == 8 ? (size_t)8 * tr.L1 * 2 * sizeof(float) : 0;
+    const size_t smem_tw8 = (size_t)8 * tr.L1 * 2 * sizeof(float);
+    const int wpre_t = epi == FFT4_FILTER && fa == 8 && smem_t + smem_tw8 <= 113 * 1024;
+    const size_t smem_tw = wpre_t ? smem_tw8 : 0;
     if (fa == 16)
-      k_fft4_b<BM_BLUE, 16><<<gt, Cfg<16>::NT, smem_t, st>>>(U, nrow, out, ldo, nullptr, w, ldw, epi, tr, wt);
+      k_fft4_b<BM_BLUE, 16><<<gt, Cfg<16>::NT, smem_t, st>>>(U, nrow, out, ldo, nullptr, w, ldw, epi, 0, tr, wt);
     else
-      k_fft4_b<BM_BLUE, 8><<<gt, Cfg<8>::NT, smem_t + smem_tw, st>>>(U, nrow, out, ldo, nullptr, w, ldw, epi, tr, wt);
+      k_fft4_b<BM_BLUE, 8><<<gt, Cfg<8>::NT, smem_t + smem_tw, st>>>(U, nrow, out, ldo, nullptr, w, ldw, epi, wpre_t,
+                                                                    tr, wt);
     return launch_status("fft4 Bluestein last pass");
   }
-  pass_b(BM_MUL, U, FFT4_PLAIN, smem_b);
+  pass_b(BM_MUL, U, FFT4_PLAIN, smem_b, 0);
   if ((rc = launch_status("fft4 Bluestein pass B"))) return rc;
   pass_a(AM_CPLX, nullptr, 0, U);
   if ((rc = launch_status("fft4 Bluestein pass A (second)"))) return rc;
-  pass_b(BM_BLUE, nullptr, epi, smem_b + smem_w);
+  pass_b(BM_BLUE, nullptr, epi, smem_b + smem_w, wpre);
   return launch_status("fft4 Bluestein pass B (second)");
 }
 
