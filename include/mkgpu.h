@@ -291,11 +291,12 @@ int mk_tod2map_fixed_noalloc(void *map, const void *dat, const int32_t *ipix, in
 /* Batched unnormalised DCT-I (FFTW REDFT00) of nrow rows of length n >= 2:
  * X_k = x_0 + (-1)^k x_{n-1} + 2 sum_{j=1}^{n-2} x_j cos(pi j k/(n-1)).
  * The DCT-I is the real part of bins 0..n-1 of the DFT of the even
- * extension (length 2(n-1)).  FP64 plans use a batched cuFFT real-to-complex
- * transform of the extension.  FP32 plans use this library's four-step
- * shared-memory FFT (two rows per complex transform, the extension formed
- * while loading): two kernels per DCT when 2(n-1) factors into 2, 3, 5, 7,
- * 11, four (Bluestein's algorithm) otherwise, cuFFT beyond its length limit.
+ * extension (length 2(n-1)).  Plans of both precisions use this library's
+ * four-step shared-memory FFT (two rows per complex transform, the
+ * extension formed while loading; FP64 plans run it in double precision):
+ * two kernels per DCT when 2(n-1) factors into 2, 3, 5, 7, 11, three
+ * (Bluestein's algorithm) otherwise, and a batched cuFFT real-to-complex
+ * transform of the extension beyond its length limit or with engine 1.
  * `in` and `out` are (nrow, n) dtype-typed and may alias.  The plan uses a
  * workspace of mk_dct1_workspace_bytes() bytes that the CALLER provides
  * (device pointer, 256-byte aligned) and keeps alive while the plan is used.

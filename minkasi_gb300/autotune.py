@@ -166,7 +166,8 @@ def choose_dct_engines(op, shapes: Sequence[Tuple[int, int]]) -> Dict[Tuple[int,
     SPLIT_RANKS closest L1 x L2 splits (the tile shapes of its two passes)
     and cuFFT (engine 1), timed on the shape's first TOD with the rotation
     the shape will use.  Returns {shape: (engine, split rank)}; FP64
-    operators keep the current engine (their plans use cuFFT)."""
+    operators keep the current engine (by default the four-step FFT in
+    double precision)."""
     cur = K.dct_engine()
     if op.dtype != torch.float32:
         return {s: (cur, 0) for s in shapes}

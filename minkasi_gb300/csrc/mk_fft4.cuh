@@ -1,4 +1,4 @@
-// FP32 DCT-I of detector rows by a four-step FFT in shared memory.
+// DCT-I of detector rows by a four-step FFT in shared memory (FP32 and FP64).
 //
 // DCT-I of a row x (length n = m + 1) is the DFT of its even extension
 // e_j = x_{min(j, 2m - j)} (length L = 2m), which is real.  Two rows r, r+1
@@ -9,7 +9,7 @@
 // and k = k2 + L2 k1:
 //   pass A: for each j1, T[j1][k2] = W_L^{j1 k2} sum_j2 e_{j1 + L1 j2} W_L2^{j2 k2}
 //   pass B: for each k2, F[k2 + L2 k1] = sum_j1 T[j1][k2] W_L1^{j1 k1}
-// Each CTA runs 8 or 16 transforms of one pass in shared memory (mixed-radix
+// Each CTA runs 8 or 16 (FP64: 4 or 8) transforms of one pass in shared memory (mixed-radix
 // decimation in time, butterflies in place), interleaved over its threads.
 // The first stage of each pass reads its inputs straight from global memory
 // (pass A forms the even extension there); pass A's last stage twiddles its
@@ -40,6 +40,13 @@
 namespace mk {
 
 constexpr int FFT4_LMAX = 1536;  // longest transform of one pass
+// largest radix the kernels hold in registers, FP32 and FP64
+#ifndef MK_FFT4_RMAX
+#define MK_FFT4_RMAX 16
+#endif
+#ifndef MK_FFT4_RMAX64
+#define MK_FFT4_RMAX64 16
+#endif
 constexpr int FFT4_MAXR = 16;    // most radix stages of one pass
 
 // device view of a plan (kernel argument)
@@ -47,6 +54,7 @@ struct Fft4Dev {
   int64_t n, m, L;  // row length, m = n - 1, transform length (2m, or M for Bluestein)
   int64_t Lx;       // even-extension length 2m
   bool blue;        // Bluestein: L = M, chirp and bhat set
+  bool f64;         // FP64 plan: tables of double2, FP64 kernels
   int L1, L2, nb32;  // nb32 = ceil(L2 / 32)
   int fba, fbb;      // transforms per CTA of pass A (length L2) and pass B (length L1): 8 or 16
   int nr1, nr2;
@@ -54,15 +62,16 @@ struct Fft4Dev {
   // per stage: span Ns of the earlier stages, 1 / Ns, offset of its twiddles
   int ns1[FFT4_MAXR], ns2[FFT4_MAXR], to1[FFT4_MAXR], to2[FFT4_MAXR];
   float inv1[FFT4_MAXR], inv2[FFT4_MAXR];
+  // complex tables (float2 or double2 by precision)
   // stage twiddles W_{Ns R}^{r k} at [to + (r - 1) Ns + k]
-  const float2 *stw1, *stw2;
+  const void *stw1, *stw2;
   const int *iperm1, *iperm2;  // natural index at each digit-reversed (DIT input) position
   // four-step twiddle W_L^{j1 k2} = tblk[j1 nb32 + k2 / 32] * tlane[32 j1 + k2 % 32]
-  const float2 *tlane, *tblk;
-  const float2 *chirp;  // Bluestein: c_t, t <= m
-  const float2 *bhat;   // Bluestein: DFT_M(b) / M
+  const void *tlane, *tblk;
+  const void *chirp;  // Bluestein: c_t, t <= m
+  const void *bhat;   // Bluestein: DFT_M(b) / M
   // Bluestein's middle pass: W_M^{k2 o1} = tblk2[k2 nb32b + o1 / 32] * tlane2[32 k2 + o1 % 32]
-  const float2 *tlane2, *tblk2;
+  const void *tlane2, *tblk2;
   int nb32b;  // ceil(L1 / 32)
 };
 
@@ -78,7 +87,7 @@ struct Fft4Plan {
 // radix lists, or, when 2(n-1) has a prime factor above 11 and `bluestein`
 // is set, the smallest splittable M >= 3(n-1); false when neither fits
 // within FFT4_LMAX x FFT4_LMAX.
-bool fft4_shape(int64_t n, Fft4Dev *d, bool bluestein = true);
+bool fft4_shape(int64_t n, Fft4Dev *d, bool bluestein = true, bool f64 = false);
 // the rank of the L1 x L2 split new plans take (0: closest to sqrt(L))
 void fft4_set_split_rank(int r);
 int fft4_split_rank();
@@ -88,10 +97,13 @@ size_t fft4_table_bytes(const Fft4Dev &d);
 size_t fft4_t_bytes(const Fft4Dev &d, int64_t nrow);
 // computes the tables on the host (B^ with a double-precision cuFFT
 // transform) and uploads them to `dev_tables`
-int fft4_init(Fft4Plan *p, int64_t n, void *dev_tables, bool bluestein = true);
+int fft4_init(Fft4Plan *p, int64_t n, void *dev_tables, bool bluestein = true, bool f64 = false);
 // out rows (ld ldo) = DCT-I of x rows (ld ldx) with the given epilogue;
 // T is scratch of fft4_t_bytes; w (ld ldw) only for FFT4_FILTER.
 int fft4_dct(const Fft4Plan &p, const float *x, int64_t ldx, int64_t nrow, float2 *T, float *out,
              int64_t ldo, int epi, const float *w, int64_t ldw, cudaStream_t st);
+// the same for an FP64 plan (fft4_init with f64)
+int fft4_dct_f64(const Fft4Plan &p, const double *x, int64_t ldx, int64_t nrow, double2 *T, double *out,
+                 int64_t ldo, int epi, const double *w, int64_t ldw, cudaStream_t st);
 
 }  // namespace mk

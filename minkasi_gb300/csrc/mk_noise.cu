@@ -151,9 +151,9 @@ std::atomic<int> g_engine{0};
 struct DctCore {
   cufftHandle fft = 0;
   bool have_fft = false;
-  bool own = false;  // four-step FFT (FP32)
+  bool own = false;  // four-step FFT of this library (FP32 or FP64 tables and kernels)
   mk::Fft4Plan f4;
-  float2 *T = nullptr;
+  void *T = nullptr;  // its scratch (complex, in the plan's precision)
   int64_t nrow = 0, n = 0, N = 0;
   int dtype = MK_F64;
   void *E = nullptr, *F = nullptr, *work = nullptr;
@@ -217,7 +217,7 @@ int make_fft(cufftHandle *h, int64_t nrow, int64_t N, int dtype, size_t *work) {
 bool use_own(int64_t nrow, int64_t n, int dtype, mk::Fft4Dev *d, bool *blue_ok) {
   const int e = g_engine.load();
   *blue_ok = e == 0;
-  return dtype == MK_F32 && e != 1 && (nrow + 1) / 2 <= 65535 && mk::fft4_shape(n, d, *blue_ok);
+  return e != 1 && (nrow + 1) / 2 <= 65535 && mk::fft4_shape(n, d, *blue_ok, dtype == MK_F64);
 }
 
 // rot: the plan rotates too (noise plans): reserve the rotation scratch
@@ -229,7 +229,7 @@ int core_bytes(int64_t nrow, int64_t n, int dtype, size_t *bytes, bool rot = tru
   mk::Fft4Dev d;
   bool blue_ok;
   if (use_own(nrow, n, dtype, &d, &blue_ok)) {
-    *bytes = align_up((size_t)nrow * n * sizeof(float)) + align_up(mk::fft4_t_bytes(d, nrow)) +
+    *bytes = align_up((size_t)nrow * n * elt(dtype)) + align_up(mk::fft4_t_bytes(d, nrow)) +
              (rot ? tc_bytes(nrow, dtype) : 0);
     return MK_OK;
   }
@@ -260,12 +260,19 @@ int core_create(DctCore *c, int64_t nrow, int64_t n, int dtype, void *ws, size_t
   if (use_own(nrow, n, dtype, &d, &blue_ok)) {
     c->own = true;
     c->E = p;
-    p += align_up((size_t)nrow * n * sizeof(float));
-    c->T = (float2 *)p;
+    p += align_up((size_t)nrow * n * elt(dtype));
+    c->T = p;
     p += align_up(mk::fft4_t_bytes(d, nrow));
-    if ((rot ? tc_bytes(nrow, dtype) : 0)) c->tc_bimg = p;
+    if ((rot ? tc_bytes(nrow, dtype) : 0)) {
+      if (dtype == MK_F64) {
+        c->oz_ws = p;
+        c->oz_bytes = tc_bytes(nrow, dtype);
+      } else {
+        c->tc_bimg = p;
+      }
+    }
     if ((rc = own_alloc(c, mk::fft4_table_bytes(d))) ||
-        (rc = mk::fft4_init(&c->f4, n, (char *)c->owned + 256, blue_ok))) {
+        (rc = mk::fft4_init(&c->f4, n, (char *)c->owned + 256, blue_ok, dtype == MK_F64))) {
       core_free(c);
       return rc;
     }
@@ -309,11 +316,18 @@ int core_fft(DctCore *c, cudaStream_t st) {
   return MK_OK;
 }
 
+// one four-step DCT-I of the plan's rows (ld n), in the plan's precision
+int own_dct(DctCore *c, const void *in, void *out, int epi, const void *w, int64_t ldw, cudaStream_t st) {
+  if (c->dtype == MK_F64)
+    return mk::fft4_dct_f64(c->f4, (const double *)in, c->n, c->nrow, (double2 *)c->T, (double *)out, c->n, epi,
+                            (const double *)w, ldw, st);
+  return mk::fft4_dct(c->f4, (const float *)in, c->n, c->nrow, (float2 *)c->T, (float *)out, c->n, epi,
+                      (const float *)w, ldw, st);
+}
+
 template <typename T, typename C>
 int dct_exec_t(DctCore *c, const void *in, void *out, cudaStream_t st) {
-  if (c->own)
-    return mk::fft4_dct(c->f4, (const float *)in, c->n, c->nrow, c->T, (float *)out, c->n, mk::FFT4_PLAIN,
-                        nullptr, 0, st);
+  if (c->own) return own_dct(c, in, out, mk::FFT4_PLAIN, nullptr, 0, st);
   dim3 g = rows_grid(c->n, c->nrow);
   k_extend<T><<<g, 256, 0, st>>>((const T *)in, c->n, (T *)c->E, c->n, c->N, c->nrow);
   int rc = mk::launch_status("mk_dct1_exec/extend");
@@ -423,10 +437,10 @@ int apply_noise_t(DctCore *c, const T *v, const T *vT, const T *w, int64_t ldw, 
   dim3 g = rows_grid(n, nd);
   int rc;
   if (c->own) {
-    float *E = (float *)c->E;
+    T *E = (T *)c->E;
     if ((rc = rotate(c, rot_mode, v, dat, n, E, n, nd, n, st))) return rc;
-    if ((rc = mk::fft4_dct(c->f4, E, n, nd, c->T, E, n, mk::FFT4_FILTER, (const float *)w, ldw, st))) return rc;
-    if ((rc = mk::fft4_dct(c->f4, E, n, nd, c->T, E, n, mk::FFT4_HALVE, nullptr, 0, st))) return rc;
+    if ((rc = own_dct(c, E, E, mk::FFT4_FILTER, w, ldw, st))) return rc;
+    if ((rc = own_dct(c, E, E, mk::FFT4_HALVE, nullptr, 0, st))) return rc;
     return rotate(c, rot_mode, vT, E, n, out, n, nd, n, st);
   }
   const bool fused_mirror = (rot_mode == 2);  // the tensor-core epilogue writes the extension
@@ -679,10 +693,8 @@ extern "C" int mk_noise_group_exec(mk_noise_group *g, void *stream) {
   for (const auto &t : g->tods) {
     DctCore *c = t.core;
     if (c->own) {
-      if ((rc = mk::fft4_dct(c->f4, t.data, c->n, c->nrow, c->T, t.data, c->n, mk::FFT4_FILTER, t.w, t.ldw, st)))
-        return rc;
-      if ((rc = mk::fft4_dct(c->f4, t.data, c->n, c->nrow, c->T, t.data, c->n, mk::FFT4_HALVE, nullptr, 0, st)))
-        return rc;
+      if ((rc = own_dct(c, t.data, t.data, mk::FFT4_FILTER, t.w, t.ldw, st))) return rc;
+      if ((rc = own_dct(c, t.data, t.data, mk::FFT4_HALVE, nullptr, 0, st))) return rc;
       continue;
     }
     // a cuFFT plan: extension, transform, filter + extension, transform,

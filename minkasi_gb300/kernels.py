@@ -382,10 +382,10 @@ def _workspace(nbytes: int, device) -> torch.Tensor:
 
 def set_dct_engine(engine: int) -> None:
     """Transform used by DCT / noise plans created from now on: 0 (default)
-    the four-step shared-memory FFT for FP32 rows (through Bluestein's
-    algorithm when 2(n-1) has a prime factor above 11), cuFFT for FP64;
-    1 cuFFT always; 2 the four-step FFT only where 2(n-1) factors into
-    2, 3, 5, 7, 11."""
+    the four-step shared-memory FFT, in the plan's precision (through
+    Bluestein's algorithm when 2(n-1) has a prime factor above 11); 1 cuFFT
+    always; 2 the four-step FFT only where 2(n-1) factors into 2, 3, 5, 7,
+    11."""
     check(lib().mk_set_dct_engine(int(engine)), "set_dct_engine")
 
 

@@ -233,13 +233,13 @@ def test_dct1_f32_and_roundtrip(K):
     assert rel(back, x) < 2e-6
 
 
-@pytest.mark.parametrize("fb", ["8", "16"])
+@pytest.mark.parametrize("fb", ["lo", "hi"])
 @pytest.mark.parametrize("nrow,n", [(1, 2), (1, 3), (2, 5), (3, 13), (4, 100), (5, 331), (2, 4097),
                                     (16, 2311), (9, 694), (8, 600001), (256, 130978)])
 def test_dct1_f32_four_step(K, nrow, n, fb, monkeypatch):
     """FP32 DCT-I through the four-step FFT (every 2(n-1) here factors into
     2, 3, 5, 7, 11; odd nrow leaves the last row pair half empty) against the
-    FP64 oracle, with 8 and with 16 transforms per CTA."""
+    FP64 oracle, with 8 and with 16 transforms per CTA ("lo", "hi")."""
     monkeypatch.setenv("MINKASI_GB300_FFT4_FB", fb)
     x = np.random.default_rng(n).standard_normal((nrow, n))
     d = K.DCT1(nrow, n, torch.float32)
@@ -250,7 +250,7 @@ def test_dct1_f32_four_step(K, nrow, n, fb, monkeypatch):
     assert np.linalg.norm(y - ref) < 2e-6 * np.linalg.norm(ref)
 
 
-@pytest.mark.parametrize("fb,passes", [("8", "3"), ("16", "3"), ("16", "4")])
+@pytest.mark.parametrize("fb,passes", [("lo", "3"), ("hi", "3"), ("hi", "4")])
 @pytest.mark.parametrize("nrow,n", [(3, 38), (3, 1000), (4, 700), (5, 18623), (2, 465551), (16, 144278)])
 def test_dct1_f32_bluestein(K, nrow, n, fb, passes, monkeypatch):
     """Lengths whose 2(n-1) has a prime factor above 11 (37, 37, 233, 9311,
@@ -266,6 +266,28 @@ def test_dct1_f32_bluestein(K, nrow, n, fb, passes, monkeypatch):
     ref = oracle.dct1(x)
     assert rel(y, ref) < 1e-5
     assert np.linalg.norm(y - ref) < 4e-6 * np.linalg.norm(ref)
+
+
+@pytest.mark.parametrize("fb", ["lo", "hi"])
+@pytest.mark.parametrize("nrow,n", [(1, 2), (3, 13), (5, 331), (2, 4097), (9, 694), (3, 1000), (5, 18623),
+                                    (8, 130978), (2, 144278)])
+def test_dct1_f64_four_step(K, nrow, n, fb, monkeypatch):
+    """FP64 DCT-I through the four-step FFT in double precision (Bluestein's
+    algorithm for 1000, 18623 and 144278), narrow and wide tiles, against the
+    FP64 oracle at 1e-12, and against cuFFT's FP64 transform."""
+    monkeypatch.setenv("MINKASI_GB300_FFT4_FB", fb)
+    x = np.random.default_rng(n + 7).standard_normal((nrow, n))
+    d = K.DCT1(nrow, n, torch.float64)
+    assert d.engine in (0, 2)
+    y = d(dev(x)).cpu().numpy()
+    assert rel(y, oracle.dct1(x)) < 1e-12
+    try:
+        K.set_dct_engine(1)
+        ref = K.DCT1(nrow, n, torch.float64)
+        assert ref.engine == 1
+        assert rel(y, ref(dev(x)).cpu().numpy()) < 1e-13
+    finally:
+        K.set_dct_engine(0)
 
 
 def test_dct1_engines_agree_and_fall_back(K):
@@ -380,11 +402,11 @@ def test_apply_noise_prewhitened_by_folding(K, gold):
     assert rel(dd, g["pw_dd"]) < 1e-12
 
 
-@pytest.mark.parametrize("engine,fb", [(0, "8"), (0, "16"), (1, "")])
+@pytest.mark.parametrize("engine,fb", [(0, "lo"), (0, "hi"), (1, "")])
 def test_apply_noise_f32_close_to_f64(K, gold, engine, fb, monkeypatch):
-    """FP32 apply_noise (the filter epilogue of pass B, weights prefetched
-    to shared memory with 8 transforms per CTA, read directly with 16)
-    against the reference's FP64 output."""
+    """FP32 apply_noise (the filter epilogue of pass B, weights staged in
+    shared memory on narrow tiles that leave room for it, read directly
+    otherwise) against the reference's FP64 output."""
     monkeypatch.setenv("MINKASI_GB300_FFT4_FB", fb)
     g = gold("noise.npz")
     try:
