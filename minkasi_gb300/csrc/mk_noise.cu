@@ -22,14 +22,15 @@
 // second rotation reads Re F in place and halves while splitting, so k_mirror
 // and k_real_halve do not run.
 //
-// FP32 plans use the four-step shared-memory FFT of mk_fft4.cu instead of
-// cuFFT (directly when 2(n-1) factors into 2, 3, 5, 7, 11; through
-// Bluestein's algorithm otherwise, up to its length limit):
+// By default plans use the four-step shared-memory FFT of mk_fft4.cu /
+// mk_fft4_f64.cu instead of cuFFT, in the plan's precision (directly when
+// 2(n-1) factors into 2, 3, 5, 7, 11; through Bluestein's algorithm
+// otherwise, up to its length limit):
 //   E = v . dat;  E = DCT(E) * mywt;  E = DCT(E) with columns 0 and n-1
 //   halved;  out = vT . E.
-// Each DCT is two kernels (four with Bluestein) that form the even
-// extension while loading and apply the weights
-// or the halving while storing, two detector rows per complex transform.
+// Each DCT is two kernels (three with Bluestein) that form the even
+// extension while loading and apply the weights or the halving while
+// storing, two detector rows per complex transform.
 #include <cublas_v2.h>
 #include <cufft.h>
 
@@ -144,8 +145,8 @@ dim3 rows_grid(int64_t n, int64_t nrow) {
 }
 
 // ---- plan object -----------------------------------------------------------
-// 0: four-step FFT for FP32 (Bluestein on it for lengths with a prime factor
-// above 11), cuFFT otherwise; 1: cuFFT; 2: four-step for smooth lengths only
+// 0: four-step FFT (Bluestein on it for lengths with a prime factor above
+// 11), cuFFT beyond its limits; 1: cuFFT; 2: four-step for smooth lengths only
 std::atomic<int> g_engine{0};
 
 struct DctCore {
