@@ -51,6 +51,25 @@ def test_map2tod_ragged_lengths_f32_f64(K, n):
         assert np.array_equal(d.cpu().numpy(), ref)
 
 
+@pytest.mark.parametrize("maxrun", [1, 3, 6, 40, 700])
+def test_map2tod_runs_across_lanes(K, maxrun):
+    """Runs of equal pixels of random lengths up to maxrun (so runs cross
+    the 4-sample groups of a lane, whole lanes, and the rows of 32 groups a
+    warp reads), with out-of-range indices mixed in: the gathered values
+    reused across lanes equal map[ipix] bit for bit, in both precisions."""
+    rng = np.random.default_rng(maxrun)
+    npix, n = 1000, 2 * 4096 * 4 + 37
+    lens = rng.integers(1, maxrun + 1, size=n)
+    pix = rng.integers(-3, npix + 3, size=n)  # a few out of range: gathered as 0
+    ipix = np.repeat(pix, lens)[:n].astype(np.int32).reshape(1, n)
+    for dt, tdt in ((np.float64, torch.float64), (np.float32, torch.float32)):
+        m = rng.standard_normal(npix).astype(dt)
+        ref = np.where((ipix >= 0) & (ipix < npix), m[np.clip(ipix, 0, npix - 1)], 0).astype(dt)
+        d = torch.full((1, n), 7.0, dtype=tdt, device=cuda)
+        K.map2tod(d, dev(m), dev(ipix), False)
+        assert np.array_equal(d.cpu().numpy(), ref)
+
+
 def test_map2tod_unaligned_view(K):
     # a view starting one element in: not 16-byte aligned -> scalar kernel
     rng = np.random.default_rng(5)
