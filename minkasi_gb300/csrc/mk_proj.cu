@@ -56,39 +56,13 @@ __global__ void __launch_bounds__(256) k_map2tod_vec(T *__restrict__ dat, const 
     T v[MU][4];
     // a sample on the same pixel as the one before it (runs average about
     // 5 samples) reuses that value: fewer L1 requests for the gathers,
-    // which otherwise bound the kernel.  Within a lane's 4 samples the
-    // value is reused directly; a group whose first sample continues the
-    // previous group's last run (lane - 1's, or lane 31's of the previous
-    // row) takes that lane's last value by shuffle once it is known.
+    // which otherwise bound the kernel
 #pragma unroll
     for (int u = 0; u < MU; u++) {
-      int32_t prevp = __shfl_up_sync(FULL, p[u].w, 1);
-      const int32_t p31 = u > 0 ? __shfl_sync(FULL, p[u - 1].w, 31) : INT32_MIN;
-      const T d31 = u > 0 ? __shfl_sync(FULL, v[u - 1][3], 31) : T(0);
-      if (lane == 0) prevp = p31;
-      const bool dup = p[u].x == prevp;
-      const bool r1 = p[u].y == p[u].x, r2 = r1 && p[u].z == p[u].x, r3 = r2 && p[u].w == p[u].x;
-      T a = dup ? T(0) : gather(map, p[u].x, npix);
-      T b = r1 ? a : gather(map, p[u].y, npix);
-      T c = p[u].z == p[u].y ? b : gather(map, p[u].z, npix);
-      T d = p[u].w == p[u].z ? c : gather(map, p[u].w, npix);
-      // resolve the continued runs left to right: a lane whose left
-      // neighbour is settled takes its last value (at most 32 rounds)
-      bool pend = dup;
-      unsigned pm = __ballot_sync(FULL, pend);
-      while (pm) {
-        T left = __shfl_up_sync(FULL, d, 1);
-        if (lane == 0) left = d31;
-        const bool left_pend = lane > 0 && ((pm >> (lane - 1)) & 1u);
-        if (pend && !left_pend) {
-          a = left;
-          if (r1) b = left;
-          if (r2) c = left;
-          if (r3) d = left;
-          pend = false;
-        }
-        pm = __ballot_sync(FULL, pend);
-      }
+      const T a = gather(map, p[u].x, npix);
+      const T b = p[u].y == p[u].x ? a : gather(map, p[u].y, npix);
+      const T c = p[u].z == p[u].y ? b : gather(map, p[u].z, npix);
+      const T d = p[u].w == p[u].z ? c : gather(map, p[u].w, npix);
       v[u][0] = a;
       v[u][1] = b;
       v[u][2] = c;
