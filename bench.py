@@ -788,7 +788,7 @@ def solve_c4(dev, tol=1e-6, wall_limit_s=420.0):
     pre_ms = b.copy()
     pre_ms.maps[0].map.copy_(pre.view(m.nx, m.ny))
     ml = L.LearnedPrecon(hits, L.load(L.weights_path("c4"), dev), (m.nx, m.ny))
-    out["learned_pool"] = ml.pool
+    out["learned_pools"] = ml.pools
     budget = None
     for name, kw in (("mixed_jacobi", {}), ("mixed_learned", {"inner_precon": ml})):
         hist = []

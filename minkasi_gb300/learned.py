@@ -190,40 +190,69 @@ class LearnedPrecon:
     within 2n pixels of the map edge (the scan footprints of the benchmark
     maps stay well inside), and both are symmetric positive definite."""
 
-    def __init__(self, hits: torch.Tensor, net: ConvNet, shape: Tuple[int, int], stencil: bool = True):
+    def __init__(self, hits: torch.Tensor, net, shape: Tuple[int, int], stencil: bool = True):
         h = hits.reshape(-1).double()
         dsq = torch.where(h > 0, 1.0 / torch.sqrt(torch.clamp(h, min=1e-300)), torch.zeros_like(h))
         self.dsq64 = dsq.contiguous()
         self.dsq32 = dsq.float().contiguous()
-        self.net = net
+        nets = list(net) if isinstance(net, (list, tuple)) else [net]
+        self.nets = nets
+        self.net = nets[0]
         self.shape = tuple(shape)
-        self.pool = net.pool
-        ws = net.weights
-        self.half = 2 * len(ws)
-        self.stencil = bool(stencil) and self.half <= 8
-        if self.pool > 1 and not self.stencil:
-            raise ValueError("a pooled network is applied as a stencil (at most 4 layers)")
-        self.kern = impulse_response(net) if self.stencil else None
+        self.pools = [n.pool for n in nets]
+        self.pool = max(self.pools)
+        self.stencil = bool(stencil) and all(2 * len(n.weights) <= 8 for n in nets)
+        if not self.stencil and (len(nets) > 1 or self.pool > 1):
+            raise ValueError("pooled or multi-level networks are applied as stencils (at most 4 layers each)")
+        # per level: (pool, half-width, stencil kernel, workspace)
+        self.levels = []
+        for n in nets:
+            ws = n.weights
+            half = 2 * len(ws)
+            if self.stencil:
+                nb = int(lib().mk_learned_precon_stencil_work_bytes(self.shape[0], self.shape[1], n.pool))
+                kern = impulse_response(n)
+            else:
+                ch = (ctypes.c_int * (len(ws) + 1))(int(ws[0].shape[1]), *[int(w.shape[0]) for w in ws])
+                nb = int(lib().mk_learned_precon_work_bytes(self.shape[0], self.shape[1], len(ws), ch))
+                kern = None
+            work = torch.empty(max((nb + 3) // 4, 1), dtype=torch.float32, device=hits.device)
+            self.levels.append((n.pool, half, kern, work))
+        self.half = self.levels[0][1]
+        self.kern = self.levels[0][2]
+        self._work = self.levels[0][3]
+        ws = self.net.weights
         self._ch = (ctypes.c_int * (len(ws) + 1))(int(ws[0].shape[1]), *[int(w.shape[0]) for w in ws])
-        if self.stencil:
-            nb = int(lib().mk_learned_precon_stencil_work_bytes(self.shape[0], self.shape[1], self.pool))
-        else:
-            nb = int(lib().mk_learned_precon_work_bytes(self.shape[0], self.shape[1], len(ws), self._ch))
-        self._work = torch.empty(max((nb + 3) // 4, 1), dtype=torch.float32, device=hits.device)
+        self._tmp = {}
+
+    def _stencil(self, level, r: torch.Tensor, z: torch.Tensor, dsq: torch.Tensor) -> None:
+        pool, half, kern, work = level
+        check(lib().mk_learned_precon_stencil(_p(z), _p(r), _p(dsq), self.shape[0], self.shape[1], half,
+                                              _p(kern), pool, _p(work), work.numel() * 4, K.dtype_code(z),
+                                              _stream()), "learned_precon_stencil")
 
     def apply(self, r: torch.Tensor, z: torch.Tensor) -> torch.Tensor:
-        """z = M r for flat maps (float32 or float64): one library call
-        (the stencil, or the 2n layered convolution launches)."""
+        """z = M r for flat maps (float32 or float64): one library call per
+        level (the stencil, or the 2n layered convolution launches).  With
+        several levels M = D^-1/2 (I + sum_l P_l^T C_l P_l) D^-1/2: each
+        level's call gives D^-1/2 (I + P_l^T C_l P_l) D^-1/2 r, and the extra
+        identity terms are taken off."""
         dsq = self.dsq64 if r.dtype == torch.float64 else self.dsq32
         if z.dtype != r.dtype or r.numel() != dsq.numel() or z.numel() != dsq.numel():
             raise ValueError("LearnedPrecon.apply: r and z must be maps of one dtype and the map's size")
         if self.stencil:
             if z.data_ptr() == r.data_ptr():
                 raise ValueError("LearnedPrecon.apply: z must not alias r")
-            check(lib().mk_learned_precon_stencil(_p(z), _p(r), _p(dsq), self.shape[0], self.shape[1],
-                                                  self.half, _p(self.kern), self.pool, _p(self._work),
-                                                  self._work.numel() * 4, K.dtype_code(z), _stream()),
-                  "learned_precon_stencil")
+            self._stencil(self.levels[0], r, z, dsq)
+            if len(self.levels) > 1:
+                t = self._tmp.get(r.dtype)
+                if t is None or t.numel() != r.numel():
+                    t = torch.empty_like(r)
+                    self._tmp[r.dtype] = t
+                for lev in self.levels[1:]:
+                    self._stencil(lev, r, t, dsq)
+                    z.add_(t)
+                z.addcmul_(dsq * dsq, r, value=-(len(self.levels) - 1))
             return z
         ws = self.net.weights
         wp = (ctypes.c_void_p * len(ws))(*[w.data_ptr() for w in ws])
@@ -388,18 +417,27 @@ def _project(v: torch.Tensor, mask: torch.Tensor, nhit: float) -> torch.Tensor:
     return (v - mean) * mask
 
 
-def loss_and_grad(net: ConvNet, dsq: torch.Tensor, mask: torch.Tensor, R: torch.Tensor,
+def _levels(net) -> List["ConvNet"]:
+    return list(net) if isinstance(net, (list, tuple)) else [net]
+
+
+def loss_and_grad(net, dsq: torch.Tensor, mask: torch.Tensor, R: torch.Tensor,
                   E: torch.Tensor, shape, need_grad: bool = True):
     """Mean over the batch of min_c ||c P(M r) - P e||^2 / ||P e||^2 and its
-    weight gradient.  CG is invariant to a scalar scale of M, so each pair's
-    best scale c is taken in closed form; by the envelope theorem the
-    gradient is the partial derivative at that c."""
+    weight gradient (a list per level when ``net`` is a list of levels,
+    M = D^-1/2 (I + sum_l P_l^T K_l^T K_l P_l) D^-1/2).  CG is invariant to
+    a scalar scale of M, so each pair's best scale c is taken in closed form;
+    by the envelope theorem the gradient is the partial derivative at that c."""
+    nets = _levels(net)
     B = R.shape[0]
     nhit = float(mask.sum())
-    b = net.pool
     u = (R * dsq[None, :])
-    uc = pool_maps(u.view(B, 1, *shape), b).contiguous()
-    kk = unpool_maps(net.ktk(uc), b, *shape).reshape(B, -1)
+    ucs = []
+    kk = torch.zeros_like(u)
+    for n in nets:
+        uc = pool_maps(u.view(B, 1, *shape), n.pool).contiguous()
+        ucs.append(uc)
+        kk += unpool_maps(n.ktk(uc), n.pool, *shape).reshape(B, -1)
     mr = dsq[None, :] * (u + kk)
     pe = _project(E, mask, nhit)
     a = _project(mr, mask, nhit)
@@ -412,11 +450,12 @@ def loss_and_grad(net: ConvNet, dsq: torch.Tensor, mask: torch.Tensor, R: torch.
     # dL/d(mr) = 2 c P res / den / B ; mr = dsq*(u + z) -> dL/dz = dsq * dL/dmr
     gmr = 2.0 * c[:, None] * _project(res, mask, nhit) / den[:, None] / B
     gz = (dsq[None, :] * gmr).view(B, 1, *shape)
-    # kk = P^T K^T K P u  ->  dL/dw = grad of K^T K at P u against P gz
-    return loss, net.grad(uc, pool_maps(gz, b).contiguous())
+    # kk_l = P^T K^T K P u  ->  dL/dw_l = grad of K_l^T K_l at P u against P gz
+    grads = [n.grad(uc, pool_maps(gz, n.pool).contiguous()) for n, uc in zip(nets, ucs)]
+    return loss, (grads if isinstance(net, (list, tuple)) else grads[0])
 
 
-def train(net: ConvNet, hits: torch.Tensor, shape, R: torch.Tensor, E: torch.Tensor,
+def train(net, hits: torch.Tensor, shape, R: torch.Tensor, E: torch.Tensor,
           epochs: int = 30, batch: int = 64, lr: float = 3e-3, seed: int = 0, log=None,
           eps: float = 1e-30) -> List[float]:
     """Adam on the relative error loss; returns the per-epoch mean loss.
@@ -431,8 +470,9 @@ def train(net: ConvNet, hits: torch.Tensor, shape, R: torch.Tensor, E: torch.Ten
     h = hits.reshape(-1).float()
     dsq = torch.where(h > 0, 1.0 / torch.sqrt(h.clamp(min=1e-30)), torch.zeros_like(h))
     mask = (h > 0).float()
-    m = [torch.zeros_like(w) for w in net.weights]
-    v = [torch.zeros_like(w) for w in net.weights]
+    weights = [w for n in _levels(net) for w in n.weights]
+    m = [torch.zeros_like(w) for w in weights]
+    v = [torch.zeros_like(w) for w in weights]
     b1, b2 = 0.9, 0.999
     t = 0
     gen = torch.Generator(device="cpu").manual_seed(seed)
@@ -444,8 +484,10 @@ def train(net: ConvNet, hits: torch.Tensor, shape, R: torch.Tensor, E: torch.Ten
         for i in range(0, n - batch + 1, batch):
             idx = perm[i:i + batch].to(dev)
             loss, grads = loss_and_grad(net, dsq, mask, R[idx], E[idx], shape)
+            if isinstance(net, (list, tuple)):
+                grads = [g for gl in grads for g in gl]
             t += 1
-            for j, (w, g) in enumerate(zip(net.weights, grads)):
+            for j, (w, g) in enumerate(zip(weights, grads)):
                 m[j].mul_(b1).add_(g, alpha=1 - b1)
                 v[j].mul_(b2).addcmul_(g, g, value=1 - b2)
                 mh = m[j] / (1 - b1 ** t)
@@ -459,16 +501,32 @@ def train(net: ConvNet, hits: torch.Tensor, shape, R: torch.Tensor, E: torch.Ten
     return hist
 
 
-def save(net: ConvNet, path: str) -> None:
-    np.savez(path, **net.state())
+def save(net, path: str) -> None:
+    """One network, or a list of levels (keys l<i>_w<j>, l<i>_pool)."""
+    if isinstance(net, (list, tuple)):
+        st = {"levels": np.int64(len(net))}
+        for i, n in enumerate(net):
+            st.update({f"l{i}_{k}": v for k, v in n.state().items()})
+        np.savez(path, **st)
+    else:
+        np.savez(path, **net.state())
 
 
-def load(path: str, device=None) -> ConvNet:
-    return ConvNet.from_state(dict(np.load(path)), device)
+def load(path: str, device=None):
+    """A ConvNet, or the list of levels of a multi-level file."""
+    st = dict(np.load(path))
+    if "levels" in st:
+        return [ConvNet.from_state({k[len(f"l{i}_"):]: v for k, v in st.items() if k.startswith(f"l{i}_")},
+                                   device)
+                for i in range(int(st["levels"]))]
+    return ConvNet.from_state(st, device)
 
 
 # ---------------------------------------------------------------- the seeded recipe
 WEIGHTS_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights")
+# the 200-TOD recipe: levels (block sizes of the pooled networks) and epochs
+C4_POOLS = [8]
+C4_EPOCHS = 20
 
 
 def weights_path(config: str) -> str:
@@ -476,20 +534,10 @@ def weights_path(config: str) -> str:
     return os.path.join(WEIGHTS_DIR, f"learned_{config}.npz")
 
 
-def train_recipe(config: str, out: Optional[str] = None, device=None, log=print) -> dict:
-    """Train the preconditioner for a benchmark configuration from seed 0, on
-    the GPU with this module's kernels, and save the weights.
-
-    c1 (1 TOD, 256^2 map): 2500 pairs (r_k, x* - x_k) from FP64 Jacobi solves
-    to 1e-10 on seeded skies (seeds 1000, 1001, ...), 2500 white pairs, Adam
-    for 30 epochs, batch 64.
-    c4 (200 TODs, 2048^2 map at 0.5"): the network acts on the 8 x 8 block
-    mean of the map (pool 8): the 1/f noise there correlates pixels over
-    ~100 pixels along the scan, far beyond the 17-pixel footprint of K^T K on
-    the fine grid.  Each pair costs an FP32 operator application of 8.8e9
-    samples, so 3 known-solution skies (seeds 1000-1002; every 3rd of 300
-    PCG iterates) and 96 white pairs, 20 epochs, batch 8.
-    Returns a record of the run (pair counts, times, losses)."""
+def recipe_pairs(config: str, device=None, log=print) -> dict:
+    """The training pairs of a benchmark configuration's recipe (seeded; see
+    train_recipe): {"hits", "shape", "R", "E", "pool", "epochs", "batch",
+    "setup_s", "pair_gen_s"} with the recipe's default pool and schedule."""
     import time
     from .pcg import MixedOp
     from .projections import make_hits
@@ -497,7 +545,6 @@ def train_recipe(config: str, out: Optional[str] = None, device=None, log=print)
 
     dev = device or torch.device("cuda", torch.cuda.current_device())
     cfg = CONFIGS[config]
-    out = out or weights_path(config)
     t0 = time.perf_counter()
     if config == "c4":
         tv, m, _ = build_large(cfg, dev, log=log)
@@ -514,7 +561,7 @@ def train_recipe(config: str, out: Optional[str] = None, device=None, log=print)
         R, E = known_solution_pairs(MixedOp(op32, m.npix, dev), m, hits, [1000, 1001, 1002],
                                     cfg.pixsize_arcsec, n_iter=300, every=3)
         rw, ew = white_pairs(op32, hits, 96)
-        epochs, batch, pool = 20, 8, 8
+        ep, batch, pool = C4_EPOCHS, 8, 8
     else:
         R, E, seed = [], [], 1000
         while sum(r.shape[0] for r in R) < 2500:
@@ -524,23 +571,63 @@ def train_recipe(config: str, out: Optional[str] = None, device=None, log=print)
             seed += 1
         R, E = torch.cat(R)[:2500], torch.cat(E)[:2500]
         rw, ew = white_pairs(op32, hits, 2500)
-        epochs, batch = 30, 64
+        ep, batch = 30, 64
     R, E = torch.cat([R, rw]), torch.cat([E, ew])
     del rw, ew
-    if config == "c4":
-        op32.release()  # the pairs are made; free the timestream buffers before training
-        torch.cuda.empty_cache()
+    op32.release()  # the pairs are made; free the timestream buffers before training
+    del op32, op64, tv
+    torch.cuda.empty_cache()
     torch.cuda.synchronize()
+    return {"hits": hits, "shape": (m.nx, m.ny), "R": R, "E": E, "pool": pool, "epochs": ep, "batch": batch,
+            "setup_s": t1 - t0, "pair_gen_s": time.perf_counter() - t1}
+
+
+def train_from_pairs(pr: dict, pools: Optional[Sequence[int]] = None, epochs: Optional[int] = None,
+                     device=None):
+    """Train the preconditioner (one level per entry of ``pools``, seeds 0,
+    1, ...) on recipe_pairs' output; returns (network or list of levels,
+    per-epoch losses)."""
+    dev = device or pr["R"].device
+    pools = list(pools) if pools else C4_POOLS if pr["pool"] > 1 else [pr["pool"]]
+    nets = [ConvNet.init(seed=i, device=dev, pool=b) for i, b in enumerate(pools)]
+    net = nets if len(nets) > 1 else nets[0]
+    hist = train(net, pr["hits"], pr["shape"], pr["R"], pr["E"], epochs=epochs or pr["epochs"],
+                 batch=pr["batch"])
+    return net, hist
+
+
+def train_recipe(config: str, out: Optional[str] = None, device=None, log=print,
+                 pools: Optional[Sequence[int]] = None, epochs: Optional[int] = None) -> dict:
+    """Train the preconditioner for a benchmark configuration from seed 0, on
+    the GPU with this module's kernels, and save the weights.
+
+    c1 (1 TOD, 256^2 map): 2500 pairs (r_k, x* - x_k) from FP64 Jacobi solves
+    to 1e-10 on seeded skies (seeds 1000, 1001, ...), 2500 white pairs, Adam
+    for 30 epochs, batch 64.
+    c4 (200 TODs, 2048^2 map at 0.5"): the network acts on the 8 x 8 block
+    mean of the map (pool 8): the 1/f noise there correlates pixels over
+    ~100 pixels along the scan, far beyond the 17-pixel footprint of K^T K on
+    the fine grid.  Each pair costs an FP32 operator application of 8.8e9
+    samples, so 3 known-solution skies (seeds 1000-1002; every 3rd of 300
+    PCG iterates) and 96 white pairs, 20 epochs, batch 8.  ``pools`` (one
+    level per entry) and ``epochs`` override the schedule: 200 epochs, a
+    fine level added to the 8 x 8 one, or 8 x 8 and 32 x 32 levels all took
+    the 200-TOD solve to within 2 % of, or beyond, the default's 250
+    iterations.
+    Returns a record of the run (pair counts, times, losses)."""
+    import time
+    out = out or weights_path(config)
+    pr = recipe_pairs(config, device, log)
     t2 = time.perf_counter()
-    net = ConvNet.init(seed=0, device=dev, pool=pool)
-    hist = train(net, hits, (m.nx, m.ny), R, E, epochs=epochs, batch=batch)
+    net, hist = train_from_pairs(pr, pools, epochs, device)
     torch.cuda.synchronize()
     t3 = time.perf_counter()
     os.makedirs(os.path.dirname(out), exist_ok=True)
     save(net, out)
-    rec = {"config": config, "pool": pool, "pairs": int(R.shape[0]), "epochs": epochs, "batch": batch,
-           "setup_s": t1 - t0, "pair_gen_s": t2 - t1, "train_s": t3 - t2,
-           "loss_first": hist[0], "loss_last": hist[-1], "out": out}
+    rec = {"config": config, "pools": [n.pool for n in _levels(net)], "pairs": int(pr["R"].shape[0]),
+           "epochs": epochs or pr["epochs"], "batch": pr["batch"], "setup_s": pr["setup_s"],
+           "pair_gen_s": pr["pair_gen_s"], "train_s": t3 - t2, "loss_first": hist[0], "loss_last": hist[-1],
+           "out": out}
     log(rec)
     return rec
 

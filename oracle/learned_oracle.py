@@ -108,6 +108,22 @@ def pooled_loss(ws, dsq, mask, R, E, shape, b: int) -> float:
     return float(((res ** 2).sum(axis=1) / (pe ** 2).sum(axis=1)).mean())
 
 
+def multilevel_loss(levels, dsq, mask, R, E, shape) -> float:
+    """The loss of M r = dsq (u + sum_l P_l^T K_l^T K_l P_l u), levels a list
+    of (weights, block size)."""
+    B = R.shape[0]
+    u = R * dsq[None, :]
+    z = np.zeros_like(u)
+    for ws, b in levels:
+        z += unpool(ktk(ws, pool(u.reshape(B, 1, *shape), b)), b, *shape).reshape(B, -1)
+    mr = dsq[None, :] * (u + z)
+    pe = _proj(E, mask)
+    a = _proj(mr, mask)
+    c = (a * pe).sum(axis=1) / (a * a).sum(axis=1)
+    res = c[:, None] * a - pe
+    return float(((res ** 2).sum(axis=1) / (pe ** 2).sum(axis=1)).mean())
+
+
 def loss_grad(ws, dsq, mask, R, E, shape) -> Tuple[float, List[np.ndarray]]:
     """Loss and its gradient w.r.t. every weight (backprop through K^T K)."""
     B = R.shape[0]

@@ -164,3 +164,22 @@ def test_fits_image_roundtrip(tmp_path):
     assert (hdr["NAXIS1"], hdr["NAXIS2"]) == (13, 7)
     assert hdr["CTYPE1"] == "RA---CAR" and hdr["CTYPE2"] == "DEC--CAR"
     assert [hdr[k] for k in ("CRVAL1", "CRVAL2", "CRPIX1", "CRPIX2", "CDELT1", "CDELT2")] == w6
+
+
+def test_learned_weight_files_single_and_multilevel(tmp_path):
+    """A weight file holds one network (w<i>, pool) or a list of levels
+    (levels, l<k>_w<i>, l<k>_pool); load gives back what save was given."""
+    import torch
+    from minkasi_gb300 import learned as L
+    one = L.ConvNet.init(seed=0, device=torch.device("cpu"), pool=8)
+    L.save(one, str(tmp_path / "one.npz"))
+    b1 = L.load(str(tmp_path / "one.npz"), "cpu")
+    assert isinstance(b1, L.ConvNet) and b1.pool == 8
+    assert all(torch.equal(x, y) for x, y in zip(one.weights, b1.weights))
+    two = [L.ConvNet.init(seed=i, device=torch.device("cpu"), pool=b) for i, b in enumerate((1, 8))]
+    L.save(two, str(tmp_path / "two.npz"))
+    b2 = L.load(str(tmp_path / "two.npz"), "cpu")
+    assert isinstance(b2, list) and [n.pool for n in b2] == [1, 8]
+    assert all(torch.equal(x, y) for a, b in zip(two, b2) for x, y in zip(a.weights, b.weights))
+    # the committed weights load
+    assert isinstance(L.load(L.weights_path("c1"), "cpu"), L.ConvNet)

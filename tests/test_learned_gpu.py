@@ -223,3 +223,71 @@ def test_pooled_training_gradient_directional(L):
     num = (lp - lm) / (2 * h)
     assert abs(loss - lo.pooled_loss(ws, dsq, mask, R, E, shape, b)) < 1e-4 * abs(loss)
     assert abs(num - ana) < 1e-2 * abs(num), (num, ana)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_multilevel_apply_is_the_sum_of_levels(L, dtype):
+    """Two levels (fine and 8 x 8 pooled): z = D^-1/2 (u + C1 * u + P^T C8 * P u),
+    the sum of the single-level operators minus one identity term, and
+    symmetric positive definite."""
+    rng = np.random.default_rng(13)
+    shape = (192, 160)
+    n = shape[0] * shape[1]
+    hits_np = rng.integers(0, 5, size=shape).astype(np.float64)
+    hits_np[:64], hits_np[-64:], hits_np[:, :64], hits_np[:, -64:] = 0, 0, 0, 0
+    hits = torch.from_numpy(hits_np.ravel()).to(cuda)
+    n1 = L.ConvNet.init(seed=6, scale=0.4, device=cuda, pool=1)
+    n8 = L.ConvNet.init(seed=7, scale=0.4, device=cuda, pool=8)
+    M = L.LearnedPrecon(hits, [n1, n8], shape)
+    assert M.pools == [1, 8]
+    r = torch.from_numpy(rng.standard_normal(n)).to(cuda, dtype)
+    z, z1, z8 = torch.empty_like(r), torch.empty_like(r), torch.empty_like(r)
+    M.apply(r, z)
+    L.LearnedPrecon(hits, n1, shape).apply(r, z1)
+    L.LearnedPrecon(hits, n8, shape).apply(r, z8)
+    dsq = M.dsq64 if dtype == torch.float64 else M.dsq32
+    want = z1 + z8 - dsq * dsq * r
+    assert rel(z.double().cpu().numpy(), want.double().cpu().numpy()) < 1e-5
+    a64, b64 = r.double(), torch.from_numpy(rng.standard_normal(n)).to(cuda)
+    Ma, Mb = torch.empty_like(a64), torch.empty_like(b64)
+    M.apply(a64, Ma)
+    M.apply(b64, Mb)
+    assert abs(float(b64 @ Ma) - float(a64 @ Mb)) < 1e-5 * float((a64.abs() * b64.abs()).sum())
+    assert float(a64 @ Ma) > 0
+
+
+def test_multilevel_training_gradient_directional(L, tmp_path):
+    """The two-level loss gradient (one list of gradients per level) against
+    a central finite difference, in float64, of the oracle's multi-level loss
+    along a random direction of all weights; save and load keep the levels."""
+    rng = np.random.default_rng(14)
+    shape, B = (48, 40), 3
+    n = shape[0] * shape[1]
+    hits = rng.integers(0, 6, size=n).astype(np.float64)
+    mask = (hits > 0).astype(np.float64)
+    dsq = np.where(hits > 0, 1 / np.sqrt(np.maximum(hits, 1)), 0.0)
+    R = rng.standard_normal((B, n))
+    E = rng.standard_normal((B, n))
+    pools = (1, 4)
+    wss = [[rng.standard_normal((co, ci, 3, 3)) * 0.2 for ci, co in zip(L.CHANNELS[:-1], L.CHANNELS[1:])]
+           for _ in pools]
+    dirs = [[rng.standard_normal(w.shape) * 0.2 for w in ws] for ws in wss]
+    nets = [L.ConvNet([t(w) for w in ws], pool=b) for ws, b in zip(wss, pools)]
+    loss, grads = L.loss_and_grad(nets, t(dsq), t(mask), t(R), t(E), shape)
+    assert len(grads) == 2
+    ana = float(sum((g.cpu().double().numpy() * d).sum()
+                    for gl, dl in zip(grads, dirs) for g, d in zip(gl, dl)))
+    h = 1e-6
+
+    def shifted(sign):
+        return [([w + sign * h * d for w, d in zip(ws, dl)], b) for ws, dl, b in zip(wss, dirs, pools)]
+
+    num = (lo.multilevel_loss(shifted(1), dsq, mask, R, E, shape) -
+           lo.multilevel_loss(shifted(-1), dsq, mask, R, E, shape)) / (2 * h)
+    assert abs(loss - lo.multilevel_loss(list(zip(wss, pools)), dsq, mask, R, E, shape)) < 1e-4 * abs(loss)
+    assert abs(num - ana) < 1e-2 * abs(num), (num, ana)
+    path = str(tmp_path / "ml.npz")
+    L.save(nets, path)
+    back = L.load(path, cuda)
+    assert [b.pool for b in back] == list(pools)
+    assert all(torch.equal(x, y) for a, b in zip(nets, back) for x, y in zip(a.weights, b.weights))
