@@ -298,6 +298,9 @@ bool fft4_shape(int64_t n, Fft4Dev *d, bool bluestein, bool f64) {
   if (!ok) return false;
   t.fba = fb_for(t.L2, f64);
   t.fbb = fb_for(t.L1, f64);
+  // MINKASI_GB300_FFT4_BLUE3=0 makes new Bluestein plans keep the four-pass form
+  const char *e4 = getenv("MINKASI_GB300_FFT4_BLUE3");
+  t.blue4 = t.blue && e4 && std::string(e4) == "0";
   *d = t;
   return true;
 }

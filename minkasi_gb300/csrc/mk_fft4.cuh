@@ -55,6 +55,7 @@ struct Fft4Dev {
   int64_t Lx;       // even-extension length 2m
   bool blue;        // Bluestein: L = M, chirp and bhat set
   bool f64;         // FP64 plan: tables of double2, FP64 kernels
+  bool blue4;       // Bluestein in four passes (U written out) instead of three
   int L1, L2, nb32;  // nb32 = ceil(L2 / 32)
   int fba, fbb;      // transforms per CTA of pass A (length L2) and pass B (length L1): 8 or 16
   int nr1, nr2;

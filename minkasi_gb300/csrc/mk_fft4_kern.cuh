@@ -947,10 +947,7 @@ int dct_launch(const Fft4Plan &p, const RT *x, int64_t ldx, int64_t nrow, C *T, 
   C *U = T + npairs * d.L;
   pass_a(AM_BLUE, x, ldx, nullptr);
   if ((rc = launch_status("fft4 Bluestein pass A"))) return rc;
-  // MINKASI_GB300_FFT4_BLUE3=0 keeps the four-pass form (U written out)
-  const char *e4 = getenv("MINKASI_GB300_FFT4_BLUE3");
-  const bool four_pass = e4 && e4[0] == '0' && e4[1] == 0;
-  if (d.nr1 >= 2 && !four_pass) {
+  if (d.nr1 >= 2 && !d.blue4) {
     // the middle pass T -> V (= U's space), then pass B on the transposed
     // shape: length L2 over the rows of V, outputs o1 + L1 o2
     const size_t smem_c = (size_t)fb * pitch_odd(d.L1) * sizeof(C);
