@@ -235,7 +235,7 @@ __device__ __forceinline__ const C *tab(const void *t) { return static_cast<cons
 // the product (checked exhaustively for all q, Ns < 2048).
 
 // ---- pass A ------------------------------------------------------------
-// A CTA runs FB transforms (FB consecutive j1) with 256 threads.  The
+// A CTA runs FB transforms (FB consecutive j1) with Cfg<FB>::NT threads.  The
 // stages interleave them over the threads (row b = bf % FB), so the first
 // stage reads its inputs straight from the detector rows (FB lanes read FB
 // consecutive samples), forming the even extension, and the middle stages
@@ -455,7 +455,7 @@ __global__ void __launch_bounds__(Cfg<FB>::NT, Cfg<FB>::MINB) k_fft4_a(const RT 
 
 // ---- pass B ------------------------------------------------------------
 // The CTA's FB transforms (FB consecutive k2) are interleaved over its
-// 256 threads: butterfly bf of a stage belongs to row b = bf % FB, so the
+// Cfg<FB>::NT threads: butterfly bf of a stage belongs to row b = bf % FB, so the
 // FB lanes of a row group read or write FB consecutive columns of T / of the
 // output.  The first stage reads its inputs straight from T (natural order:
 // position g R0 + r of the digit-reversed layout holds index
