@@ -6,6 +6,7 @@
 //   MK_FFT4_FBHI / MK_FFT4_FBLO        transforms per CTA, wide and narrow tile
 //   MK_FFT4_NTHI / MK_FFT4_NTLO        threads per CTA for each
 //   MK_FFT4_MINBLO                     CTAs per SM the narrow tile's registers are sized for
+//   (MK_FFT4_MINBHI, default 2: the same for the wide tile)
 // and includes this file once.  dct_launch is the host entry of the
 // precision.
 #include <cufft.h>
@@ -24,7 +25,10 @@ namespace MK_FFT4_NS {
 using C = MK_FFT4_C;
 using RT = MK_FFT4_RT;
 constexpr int FB_HI = MK_FFT4_FBHI, FB_LO = MK_FFT4_FBLO;
-constexpr int NT_HI = MK_FFT4_NTHI, NT_LO = MK_FFT4_NTLO, MINB_LO = MK_FFT4_MINBLO;
+#ifndef MK_FFT4_MINBHI
+#define MK_FFT4_MINBHI 2
+#endif
+constexpr int NT_HI = MK_FFT4_NTHI, NT_LO = MK_FFT4_NTLO, MINB_LO = MK_FFT4_MINBLO, MINB_HI = MK_FFT4_MINBHI;
 constexpr int WR3 = 0, WR5 = 3, WR7 = 8, WR9 = 15, WR11 = 24, WRN = 35;  // offsets into the radix constants
 
 __host__ __device__ __forceinline__ C mkc(RT x, RT y) {
@@ -254,7 +258,7 @@ enum { AM_DCT = 0, AM_BLUE = 1, AM_CPLX = 2 };
 template <int FB>
 struct Cfg {
   static constexpr int NT = FB == FB_HI ? NT_HI : NT_LO;
-  static constexpr int MINB = FB == FB_HI ? 2 : MINB_LO;
+  static constexpr int MINB = FB == FB_HI ? MINB_HI : MINB_LO;
 };
 
 struct PassA {
