@@ -588,7 +588,9 @@ def train_from_pairs(pr: dict, pools: Optional[Sequence[int]] = None, epochs: Op
     1, ...) on recipe_pairs' output; returns (network or list of levels,
     per-epoch losses)."""
     dev = device or pr["R"].device
-    pools = list(pools) if pools else C4_POOLS if pr["pool"] > 1 else [pr["pool"]]
+    if not pools:
+        pools = list(C4_POOLS) if pr["pool"] > 1 else [pr["pool"]]
+    pools = list(pools)
     nets = [ConvNet.init(seed=i, device=dev, pool=b) for i, b in enumerate(pools)]
     net = nets if len(nets) > 1 else nets[0]
     hist = train(net, pr["hits"], pr["shape"], pr["R"], pr["E"], epochs=epochs or pr["epochs"],
